@@ -1,0 +1,914 @@
+// oracle/oracle.cpp -- TEST INFRASTRUCTURE ONLY (see oracle.h).
+//
+// A plain FP64 CPU restatement of libint's Coulomb ERI path, written from the
+// published algorithms the reference implements:
+//   * Boys function: 7th-order Taylor interpolation of F_mmax on a grid plus
+//     downward recursion, asymptotic form + upward recursion at large T
+//     (the FmEval_Taylor scheme of include/libint2/boys.h:519-879).
+//   * Obara-Saika vertical recurrence on centres A and C per primitive
+//     quartet (src/bin/libint/vrr_11_twoprep_11.h:145-223,305-383), summed
+//     over primitives at the (e0|f0) level (src/bin/libint/dg.cc:1177-1189),
+//     then Head-Gordon-Pople horizontal recurrence on the contracted
+//     integrals (src/bin/libint/hrr.h:246-347).
+//   * First derivatives from the Gaussian derivative rule
+//     d/dA_i phi_a = 2 alpha_a phi_{a+1_i} - a_i phi_{a-1_i}
+//     (src/bin/libint/comp_deriv_gauss.h) applied at the contracted level
+//     with exponent-weighted sums, and centre C by translational invariance
+//     (src/bin/libint/master_rrs_list.h:52-55).
+//   * Engine::compute2's canonical swap, primitive screening, Cartesian ->
+//     solid-harmonic transform and un-permutation
+//     (include/libint2/engine.impl.h:1181-1211,1306-1766,1965-2086).
+// It is the checker of the CUDA path, never the thing shipped.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cassert>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------- helpers
+inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+inline int npure(int l) { return 2 * l + 1; }
+// Standard Cartesian order (x-power descending, then y-power descending):
+// include/libint2/cgshell_ordering.h:125-131.
+inline int cart_index(int l, int lx, int ly) {
+  const int i = l - lx;
+  return i * (i + 1) / 2 + (i - ly);
+}
+inline int cum_ncart(int l) { return l * (l + 1) * (l + 2) / 6; }  // #comps < l
+
+double fac(int n) {
+  double r = 1;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+double dfac(int n) {  // n!! with (-1)!! = 0!! = 1
+  double r = 1;
+  for (int i = n; i > 1; i -= 2) r *= i;
+  return r;
+}
+double binom(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  return fac(n) / (fac(k) * fac(n - k));
+}
+inline int parity(int k) { return (k % 2) ? -1 : 1; }
+
+// Cartesian exponents of component c of shell l in standard order.
+void cart_exps(int l, int c, int* e) {
+  e[0] = e[1] = e[2] = 0;
+  int idx = 0;
+  for (int lx = l; lx >= 0; --lx)
+    for (int ly = l - lx; ly >= 0; --ly) {
+      if (idx == c) {
+        e[0] = lx;
+        e[1] = ly;
+        e[2] = l - lx - ly;
+        return;
+      }
+      ++idx;
+    }
+}
+
+// ----------------------------------------------------------------- Boys
+// Grid values F_m(k*dT), m = 0..kTabM, from the MacLaurin series in long
+// double for the top m and downward recursion.
+constexpr double kBoysDT = 0.05;
+constexpr double kBoysTcrit = 36.0;
+constexpr int kBoysOrder = 7;  // Taylor terms i = 0..6
+constexpr int kTabM = 40 + kBoysOrder;
+constexpr int kTabN = int(kBoysTcrit / kBoysDT) + 2;
+
+struct BoysTable {
+  std::vector<double> F;  // [kTabN][kTabM+1]
+  BoysTable() : F(size_t(kTabN) * (kTabM + 1)) {
+    for (int k = 0; k < kTabN; ++k) {
+      const long double T = (long double)k * kBoysDT;
+      // series for F_M(T) = e^{-T} sum_i (2T)^i / ((2M+1)(2M+3)...(2M+2i+1))
+      const int M = kTabM;
+      long double term = 1.0L / (2 * M + 1), sum = term;
+      for (int i = 1; i < 2000; ++i) {
+        term *= 2 * T / (2 * M + 2 * i + 1);
+        sum += term;
+        if (term < sum * 1e-21L) break;
+      }
+      const long double eT = expl(-T);
+      long double f = eT * sum;
+      double* row = &F[size_t(k) * (kTabM + 1)];
+      row[M] = (double)f;
+      for (int m = M - 1; m >= 0; --m) {
+        f = (2 * T * f + eT) / (2 * m + 1);
+        row[m] = (double)f;
+      }
+    }
+  }
+};
+const BoysTable& boys_table() {
+  static BoysTable t;
+  return t;
+}
+
+void boys(double T, int mmax, double* F) {
+  if (T > kBoysTcrit) {
+    // F_0 = (1/2) sqrt(pi/T) erf(sqrt T); erf(sqrt T) == 1 to double here.
+    const double eT = std::exp(-T);
+    const double oo2T = 0.5 / T;
+    F[0] = 0.88622692545275801365 * std::sqrt(1.0 / T);
+    for (int m = 0; m < mmax; ++m) F[m + 1] = ((2 * m + 1) * F[m] - eT) * oo2T;
+    return;
+  }
+  const BoysTable& tab = boys_table();
+  const int k = int(T / kBoysDT + 0.5);
+  const double d = T - k * kBoysDT;  // |d| <= dT/2
+  const double* row = &tab.F[size_t(k) * (kTabM + 1)];
+  // F_M(T_k + d) = sum_i F_{M+i}(T_k) (-d)^i / i!
+  double s = 0, p = 1;
+  for (int i = 0; i < kBoysOrder; ++i) {
+    s += row[mmax + i] * p;
+    p *= -d / (i + 1);
+  }
+  F[mmax] = s;
+  if (mmax > 0) {
+    const double eT = std::exp(-T);
+    for (int m = mmax - 1; m >= 0; --m)
+      F[m] = (2 * T * F[m + 1] + eT) / (2 * m + 1);
+  }
+}
+
+// ------------------------------------------------------- solid harmonics
+// Coefficient of x^lx y^ly z^lz in the real solid harmonic S_{l,m}
+// (Schlegel & Frisch, IJQC 54, 83 (1995), eq. 15), for Cartesian Gaussians
+// that share the normalization of x^l (libint's "standard" convention), so
+// the extra factor sqrt((2l-1)!!/((2lx-1)!!(2ly-1)!!(2lz-1)!!)) appears.
+double solid_coeff(int l, int m, int lx, int ly, int lz) {
+  const int am = std::abs(m);
+  if ((lx + ly - am) % 2 != 0) return 0.0;
+  const int j = (lx + ly - am) / 2;
+  if (j < 0) return 0.0;
+  const int i = am - lx;
+  // cosine-type (m >= 0) needs am - lx even, sine-type needs it odd
+  if ((m >= 0) != (std::abs(i) % 2 == 0)) return 0.0;
+  double pfac = std::sqrt(fac(2 * lx) * fac(2 * ly) * fac(2 * lz) / fac(2 * l) *
+                          fac(l - am) / fac(l) / fac(l + am) /
+                          (fac(lx) * fac(ly) * fac(lz)));
+  pfac /= double(1L << l);
+  pfac *= (m < 0) ? parity((i - 1) / 2) : parity(i / 2);
+  double sum = 0;
+  for (int ii = j; ii <= (l - am) / 2; ++ii) {
+    double t = binom(l, ii) * binom(ii, j) * parity(ii) * fac(2 * (l - ii)) /
+               fac(l - am - 2 * ii);
+    double s1 = 0;
+    for (int k = 0; k <= std::min(j, lx / 2); ++k)
+      if (lx - 2 * k <= am) s1 += binom(j, k) * binom(am, lx - 2 * k) * parity(k);
+    sum += t * s1;
+  }
+  sum *= std::sqrt(dfac(2 * l - 1) /
+                   (dfac(2 * lx - 1) * dfac(2 * ly - 1) * dfac(2 * lz - 1)));
+  return (m == 0) ? pfac * sum : M_SQRT2 * pfac * sum;
+}
+
+// Dense [2l+1][ncart(l)] coefficient matrices, cached.
+const std::vector<double>& sph_matrix(int l) {
+  static std::vector<double> mats[16];
+  static std::once_flag once[16];
+  std::call_once(once[l], [l]() {
+    auto& M = mats[l];
+    M.assign(size_t(npure(l)) * ncart(l), 0.0);
+    for (int p = 0; p < npure(l); ++p)
+      for (int c = 0; c < ncart(l); ++c) {
+        int e[3] = {0, 0, 0};
+        cart_exps(l, c, e);
+        M[size_t(p) * ncart(l) + c] = solid_coeff(l, p - l, e[0], e[1], e[2]);
+      }
+  });
+  return mats[l];
+}
+
+// ------------------------------------------------------------ shell pairs
+struct PrimPair {
+  double P[3], K, oog, nonsph, ln_scr;
+  int p1, p2;
+};
+
+struct ShellView {
+  int l, pure, nprim;
+  const double* O;
+  const double* alpha;
+  const double* coeff;
+  double max_ln_coeff[64];
+};
+
+ShellView view(const orc_basis* bs, int s) {
+  ShellView v;
+  v.l = bs->l[s];
+  v.pure = bs->pure[s];
+  v.nprim = bs->nprim[s];
+  v.O = bs->O + 3 * s;
+  v.alpha = bs->alpha + bs->prim_off[s];
+  v.coeff = bs->coeff + bs->prim_off[s];
+  for (int p = 0; p < v.nprim; ++p)
+    v.max_ln_coeff[p] = std::log(std::abs(v.coeff[p]));
+  return v;
+}
+
+// ShellPair::init, Original (0) / Conservative (1) (shell.h:1138-1256).
+int pair_init(const ShellView& s1, const ShellView& s2, double ln_prec,
+              int method, PrimPair* out) {
+  const double* A = s1.O;
+  const double* B = s2.O;
+  double AB2 = 0;
+  for (int i = 0; i < 3; ++i) AB2 += (A[i] - B[i]) * (A[i] - B[i]);
+  int c = 0;
+  for (int p1 = 0; p1 < s1.nprim; ++p1)
+    for (int p2 = 0; p2 < s2.nprim; ++p2) {
+      const double a1 = s1.alpha[p1], a2 = s2.alpha[p2];
+      const double gamma = a1 + a2, oog = 1 / gamma;
+      const double rho = a1 * a2 * oog;
+      const double mrAB2 = -rho * AB2;
+      double ln_scr = mrAB2 + s1.max_ln_coeff[p1] + s2.max_ln_coeff[p2];
+      if (method == 0 && ln_scr < ln_prec) continue;
+      double P[3];
+      for (int i = 0; i < 3; ++i)
+        P[i] = (AB2 == 0.) ? A[i] : (a1 * A[i] + a2 * B[i]) * oog;
+      double nonsph = 0;
+      if (method == 1) {
+        double mPA = 0, mPB = 0;
+        for (int i = 0; i < 3; ++i) {
+          mPA = std::max(mPA, std::abs(P[i] - A[i]));
+          mPB = std::max(mPB, std::abs(P[i] - B[i]));
+        }
+        const double t1 = std::pow(mPA, s1.l) * std::pow(mPB, s2.l);
+        const double t2 = fac(s1.l) * fac(s2.l) * std::pow(oog, s1.l + s2.l);
+        nonsph = std::max(t1, t2);
+        ln_scr += 1.777485947591722872387900 + std::log(oog) +
+                  std::log(std::max(nonsph, 1.0)) +
+                  std::log(double(s1.nprim * s2.nprim));
+        if (ln_scr < ln_prec) continue;
+      }
+      PrimPair& pp = out[c++];
+      pp.ln_scr = ln_scr;
+      pp.p1 = p1;
+      pp.p2 = p2;
+      pp.K = 5.9149671727956128778 * std::exp(mrAB2) * oog;
+      for (int i = 0; i < 3; ++i) pp.P[i] = P[i];
+      pp.nonsph = nonsph;
+      pp.oog = oog;
+    }
+  return c;
+}
+
+// ------------------------------------------------------------ VRR tables
+// All Cartesian components of shells 0..lmax in one cumulative index.
+struct CartTable {
+  std::vector<int> ex, ey, ez, l;   // exponents and shell of each cum. index
+  std::vector<int> dir;             // build direction (first nonzero of x,y,z)
+  std::vector<int> m1[3];           // cum. index of c - 1_i (or -1)
+  CartTable(int lmax) {
+    for (int L = 0; L <= lmax; ++L)
+      for (int c = 0; c < ncart(L); ++c) {
+        int e[3];
+        cart_exps(L, c, e);
+        ex.push_back(e[0]);
+        ey.push_back(e[1]);
+        ez.push_back(e[2]);
+        l.push_back(L);
+        dir.push_back(e[0] ? 0 : (e[1] ? 1 : 2));
+      }
+    const int n = (int)ex.size();
+    for (int i = 0; i < 3; ++i) m1[i].assign(n, -1);
+    for (int k = 0; k < n; ++k) {
+      int e[3] = {ex[k], ey[k], ez[k]};
+      for (int i = 0; i < 3; ++i)
+        if (e[i] > 0) {
+          int f[3] = {e[0], e[1], e[2]};
+          --f[i];
+          const int L = l[k] - 1;
+          m1[i][k] = cum_ncart(L) + cart_index(L, f[0], f[1]);
+        }
+    }
+  }
+  int idx(int L, const int* e) const { return cum_ncart(L) + cart_index(L, e[0], e[1]); }
+  int expo(int k, int i) const { return i == 0 ? ex[k] : (i == 1 ? ey[k] : ez[k]); }
+};
+const CartTable& cart_table() {
+  static CartTable t(16);
+  return t;
+}
+
+// ---------------------------------------------------------- quartet core
+struct Work {
+  std::vector<double> V;    // VRR [ne][nf][mmax+1]
+  std::vector<double> acc;  // contracted [nw][ne][nf]
+  std::vector<double> t1, t2, t3;
+  PrimPair ppb[64 * 64], ppk[64 * 64];
+};
+
+// HRR on one side: from contracted (e| with e in [la, la+lb] (cum. index
+// rows, each row of length ncol) build (a b| with a in shell la, b in shell
+// lb: out[(a*ncart(lb)+b)*ncol + col].  (a b+1_i| = (a+1_i b| + AB_i (a b|.
+void hrr(int la, int lb, const double* AB, const double* src, int src_rows0,
+         int ncol, double* out, std::vector<double>& tmpA,
+         std::vector<double>& tmpB) {
+  const CartTable& ct = cart_table();
+  // layer k holds (a b| for a in shells [la, la+lb-k], b in shell k.
+  // Represent as map: rowsA = cum index of a (relative to cum_ncart(la)),
+  // b in shell k.
+  const int a0 = cum_ncart(la);
+  const int na_tot = cum_ncart(la + lb + 1) - a0;
+  // current layer: [na_tot][nb_k][ncol]
+  tmpA.assign(size_t(na_tot) * ncol, 0.0);
+  for (int r = 0; r < na_tot; ++r)
+    std::memcpy(&tmpA[size_t(r) * ncol], src + size_t(a0 + r - src_rows0) * ncol,
+                sizeof(double) * ncol);
+  int nbk = 1;
+  for (int k = 1; k <= lb; ++k) {
+    const int na_k = cum_ncart(la + lb - k + 1) - a0;  // a shells la..la+lb-k
+    const int nbn = ncart(k);
+    tmpB.assign(size_t(na_k) * nbn * ncol, 0.0);
+    for (int b = 0; b < nbn; ++b) {
+      int eb[3];
+      cart_exps(k, b, eb);
+      const int i = eb[0] ? 0 : (eb[1] ? 1 : 2);
+      int ebm[3] = {eb[0], eb[1], eb[2]};
+      --ebm[i];
+      const int bm = cart_index(k - 1, ebm[0], ebm[1]);
+      for (int ar = 0; ar < na_k; ++ar) {
+        const int acum = a0 + ar;
+        int ea[3] = {ct.ex[acum], ct.ey[acum], ct.ez[acum]};
+        int eap[3] = {ea[0], ea[1], ea[2]};
+        ++eap[i];
+        const int apcum = ct.idx(ct.l[acum] + 1, eap);
+        const double* s1 = &tmpA[(size_t(apcum - a0) * nbk + bm) * ncol];
+        const double* s2 = &tmpA[(size_t(ar) * nbk + bm) * ncol];
+        double* d = &tmpB[(size_t(ar) * nbn + b) * ncol];
+        for (int c = 0; c < ncol; ++c) d[c] = s1[c] + AB[i] * s2[c];
+      }
+    }
+    tmpA.swap(tmpB);
+    nbk = nbn;
+  }
+  // extract a in shell la
+  const int na = ncart(la), nb = ncart(lb);
+  for (int a = 0; a < na; ++a)
+    std::memcpy(out + size_t(a) * nb * ncol, &tmpA[size_t(a) * nb * ncol],
+                sizeof(double) * nb * ncol);
+}
+
+// Contracted Cartesian shell set (a b|c d) from contracted (e0|f0) data
+// stored as C[e][f] with e rows in [er0, er0+ner), f cols [fc0, fc0+nfc).
+void hrr_both(int la, int lb, int lc, int ld, const double* AB, const double* CD,
+              const double* C, int er0, int ner, int fc0, int nfc, double* out,
+              Work& w) {
+  // bra HRR with ncol = nfc -> [a][b][f]
+  const int na = ncart(la), nb = ncart(lb), nc = ncart(lc), nd = ncart(ld);
+  std::vector<double> braout(size_t(na) * nb * nfc);
+  hrr(la, lb, AB, C, er0, nfc, braout.data(), w.t1, w.t2);
+  // ket HRR per (a,b): rows f, single column -> transpose to [f][ab]
+  const int nab = na * nb;
+  std::vector<double> T(size_t(nfc) * nab);
+  for (int ab = 0; ab < nab; ++ab)
+    for (int f = 0; f < nfc; ++f) T[size_t(f) * nab + ab] = braout[size_t(ab) * nfc + f];
+  std::vector<double> ketout(size_t(nc) * nd * nab);
+  hrr(lc, ld, CD, T.data(), fc0, nab, ketout.data(), w.t1, w.t2);
+  for (int cd = 0; cd < nc * nd; ++cd)
+    for (int ab = 0; ab < nab; ++ab) out[size_t(ab) * nc * nd + cd] = ketout[size_t(cd) * nab + ab];
+}
+
+struct Quartet {
+  int perm[4];  // canonical position k holds target shell perm[k]
+  bool swap_braket, swap_tbra, swap_tket;
+};
+
+// The full Engine::compute2 restatement. Returns values per set, 0 if all
+// primitive quartets were screened.
+int compute_quartet(const orc_basis* bs, const int* tgt, int deriv,
+                    double precision, int method, Work& w, double* out) {
+  const CartTable& ct = cart_table();
+  const int tl[4] = {bs->l[tgt[0]], bs->l[tgt[1]], bs->l[tgt[2]], bs->l[tgt[3]]};
+  Quartet q;
+  q.swap_tbra = tl[0] < tl[1];
+  q.swap_tket = tl[2] < tl[3];
+  q.swap_braket = tl[0] + tl[1] > tl[2] + tl[3];
+  q.perm[0] = q.swap_braket ? (q.swap_tket ? 3 : 2) : (q.swap_tbra ? 1 : 0);
+  q.perm[1] = q.swap_braket ? (q.swap_tket ? 2 : 3) : (q.swap_tbra ? 0 : 1);
+  q.perm[2] = q.swap_braket ? (q.swap_tbra ? 1 : 0) : (q.swap_tket ? 3 : 2);
+  q.perm[3] = q.swap_braket ? (q.swap_tbra ? 0 : 1) : (q.swap_tket ? 2 : 3);
+  ShellView sh[4];
+  for (int k = 0; k < 4; ++k) sh[k] = view(bs, tgt[q.perm[k]]);
+  const int la = sh[0].l, lb = sh[1].l, lc = sh[2].l, ld = sh[3].l;
+  const int L = la + lb + lc + ld;
+  const int mmax = L + deriv;
+  const double ln_prec =
+      precision > 0 ? std::log(precision) : std::numeric_limits<double>::lowest();
+
+  const int npb = pair_init(sh[0], sh[1], ln_prec, method, w.ppb);
+  const int npk = pair_init(sh[2], sh[3], ln_prec, method, w.ppk);
+  const double* A = sh[0].O;
+  const double* B = sh[1].O;
+  const double* C = sh[2].O;
+  const double* D = sh[3].O;
+  double AB[3], CD[3];
+  for (int i = 0; i < 3; ++i) {
+    AB[i] = A[i] - B[i];
+    CD[i] = C[i] - D[i];
+  }
+
+  // ranges of contracted (e0|f0) needed
+  const int emin = deriv ? std::max(la - 1, 0) : la;
+  const int emax = la + lb + deriv;
+  const int fmin = deriv ? std::max(lc - 1, 0) : lc;
+  const int fmax = lc + ld + deriv;
+  const int ne = cum_ncart(emax + 1), nf = cum_ncart(fmax + 1);  // VRR extents
+  const int er0 = cum_ncart(emin), ner = ne - er0;
+  const int fc0 = cum_ncart(fmin), nfc = nf - fc0;
+  const int nw = deriv ? 4 : 1;  // weights 1, 2a_A, 2a_B, 2a_D
+  const int M1 = mmax + 1;
+  w.V.assign(size_t(ne) * nf * M1, 0.0);
+  w.acc.assign(size_t(nw) * ner * nfc, 0.0);
+  auto V = [&](int e, int f, int m) -> double& {
+    return w.V[(size_t(e) * nf + f) * M1 + m];
+  };
+
+  int nkept = 0;
+  double F[64];
+  const double npbraket = double(npb) * npk;
+  for (int pb = 0; pb < npb; ++pb)
+    for (int pk = 0; pk < npk; ++pk) {
+      const PrimPair& bp = w.ppb[pb];
+      const PrimPair& kp = w.ppk[pk];
+      if (!(bp.ln_scr + kp.ln_scr > ln_prec)) continue;
+      const double a0 = sh[0].alpha[bp.p1], a1 = sh[1].alpha[bp.p2];
+      const double a2 = sh[2].alpha[kp.p1], a3 = sh[3].alpha[kp.p2];
+      const double c0123 = sh[0].coeff[bp.p1] * sh[1].coeff[bp.p2] *
+                           sh[2].coeff[kp.p1] * sh[3].coeff[kp.p2];
+      const double zeta = a0 + a1, eta = a2 + a3;
+      const double* P = bp.P;
+      const double* Q = kp.P;
+      const double PQ[3] = {P[0] - Q[0], P[1] - Q[1], P[2] - Q[2]};
+      const double PQ2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
+      const double gpq = zeta + eta;
+      const double oogpq = 1.0 / gpq;
+      double pfac = bp.K * kp.K * std::sqrt(gpq) * oogpq * c0123;
+      if (method == 0 || method == 1) {
+        double mag = std::abs(pfac);
+        if (method == 1) mag *= std::max(1.0, bp.nonsph * kp.nonsph) * npbraket;
+        if (mag < precision) continue;
+      }
+      ++nkept;
+      const double rho = zeta * eta * oogpq;
+      const double T = PQ2 * rho;
+      boys(T, mmax, F);
+      for (int m = 0; m <= mmax; ++m) V(0, 0, m) = F[m] * pfac;
+      double W[3], PA[3], WP[3], QC[3], WQ[3];
+      for (int i = 0; i < 3; ++i) {
+        W[i] = (zeta * P[i] + eta * Q[i]) * oogpq;
+        PA[i] = P[i] - A[i];
+        WP[i] = W[i] - P[i];
+        QC[i] = Q[i] - C[i];
+        WQ[i] = W[i] - Q[i];
+      }
+      const double oo2z = 0.5 / zeta, oo2e = 0.5 / eta, oo2ze = 0.5 * oogpq;
+      const double roz = rho / zeta, roe = rho / eta;
+      // (e0|00)^m
+      for (int e = 1; e < ne; ++e) {
+        const int le = ct.l[e];
+        const int i = ct.dir[e];
+        const int e1 = ct.m1[i][e];
+        const int e2 = ct.m1[i][e1];
+        const double n1 = ct.expo(e1, i);
+        for (int m = 0; m <= mmax - le; ++m) {
+          double v = PA[i] * V(e1, 0, m) + WP[i] * V(e1, 0, m + 1);
+          if (e2 >= 0) v += n1 * oo2z * (V(e2, 0, m) - roz * V(e2, 0, m + 1));
+          V(e, 0, m) = v;
+        }
+      }
+      // (e0|f0)^m
+      for (int f = 1; f < nf; ++f) {
+        const int lf = ct.l[f];
+        const int j = ct.dir[f];
+        const int f1 = ct.m1[j][f];
+        const int f2 = ct.m1[j][f1];
+        const double n1 = ct.expo(f1, j);
+        for (int e = 0; e < ne; ++e) {
+          const int le = ct.l[e];
+          if (le + lf > mmax) continue;
+          const int em = ct.m1[j][e];
+          const double ne_j = ct.expo(e, j);
+          for (int m = 0; m <= mmax - le - lf; ++m) {
+            double v = QC[j] * V(e, f1, m) + WQ[j] * V(e, f1, m + 1);
+            if (f2 >= 0) v += n1 * oo2e * (V(e, f2, m) - roe * V(e, f2, m + 1));
+            if (em >= 0) v += ne_j * oo2ze * V(em, f1, m + 1);
+            V(e, f, m) = v;
+          }
+        }
+      }
+      // contraction at the (e0|f0) level
+      const double wts[4] = {1.0, 2 * a0, 2 * a1, 2 * a3};
+      for (int wi = 0; wi < nw; ++wi) {
+        double* ac = &w.acc[size_t(wi) * ner * nfc];
+        for (int e = er0; e < ne; ++e)
+          for (int f = fc0; f < nf; ++f) {
+            if (ct.l[e] + ct.l[f] > mmax) continue;
+            ac[size_t(e - er0) * nfc + (f - fc0)] += wts[wi] * V(e, f, 0);
+          }
+      }
+    }
+  if (nkept == 0) return 0;
+
+  // Cartesian sets in the canonical frame
+  const int nca = ncart(la), ncb = ncart(lb), ncc = ncart(lc), ncd = ncart(ld);
+  const size_t ncart4 = size_t(nca) * ncb * ncc * ncd;
+  const int nsets = deriv ? 12 : 1;
+  std::vector<double> cart(nsets * ncart4, 0.0);
+  if (!deriv) {
+    hrr_both(la, lb, lc, ld, AB, CD, w.acc.data(), er0, ner, fc0, nfc,
+             cart.data(), w);
+  } else {
+    std::vector<double> tmp;
+    auto shellset = [&](int wi, int a, int b, int c, int d) {
+      tmp.assign(size_t(ncart(a)) * ncart(b) * ncart(c) * ncart(d), 0.0);
+      hrr_both(a, b, c, d, AB, CD, &w.acc[size_t(wi) * ner * nfc], er0, ner,
+               fc0, nfc, tmp.data(), w);
+    };
+    // d/dA_i = (a+1_i b|cd)_{2aA} - a_i (a-1_i b|cd)
+    // d/dB_i = (a b+1_i|cd)_{2aB} - b_i (a b-1_i|cd)
+    // d/dD_i = (ab|c d+1_i)_{2aD} - d_i (ab|c d-1_i)
+    const int lsh[4] = {la, lb, lc, ld};
+    const int wsel[4] = {1, 2, -1, 3};
+    for (int ctr : {0, 1, 3}) {
+      int lu[4] = {la, lb, lc, ld};
+      lu[ctr] += 1;
+      std::vector<double> up;
+      shellset(wsel[ctr], lu[0], lu[1], lu[2], lu[3]);
+      up = tmp;
+      std::vector<double> dn;
+      if (lsh[ctr] > 0) {
+        int lo[4] = {la, lb, lc, ld};
+        lo[ctr] -= 1;
+        shellset(0, lo[0], lo[1], lo[2], lo[3]);
+        dn = tmp;
+      }
+      int nl[4] = {nca, ncb, ncc, ncd};
+      int nu[4] = {nca, ncb, ncc, ncd};
+      nu[ctr] = ncart(lsh[ctr] + 1);
+      int nlo[4] = {nca, ncb, ncc, ncd};
+      nlo[ctr] = lsh[ctr] > 0 ? ncart(lsh[ctr] - 1) : 0;
+      for (int xyz = 0; xyz < 3; ++xyz) {
+        double* dst = &cart[size_t(ctr * 3 + xyz) * ncart4];
+        size_t o = 0;
+        int ix[4];
+        for (ix[0] = 0; ix[0] < nl[0]; ++ix[0])
+          for (ix[1] = 0; ix[1] < nl[1]; ++ix[1])
+            for (ix[2] = 0; ix[2] < nl[2]; ++ix[2])
+              for (ix[3] = 0; ix[3] < nl[3]; ++ix[3], ++o) {
+                int e[3];
+                cart_exps(lsh[ctr], ix[ctr], e);
+                int eu[3] = {e[0], e[1], e[2]};
+                ++eu[xyz];
+                int iu[4] = {ix[0], ix[1], ix[2], ix[3]};
+                iu[ctr] = cart_index(lsh[ctr] + 1, eu[0], eu[1]);
+                double v = up[((size_t(iu[0]) * nu[1] + iu[1]) * nu[2] + iu[2]) * nu[3] + iu[3]];
+                if (e[xyz] > 0) {
+                  int ed[3] = {e[0], e[1], e[2]};
+                  --ed[xyz];
+                  int id[4] = {ix[0], ix[1], ix[2], ix[3]};
+                  id[ctr] = cart_index(lsh[ctr] - 1, ed[0], ed[1]);
+                  v -= e[xyz] * dn[((size_t(id[0]) * nlo[1] + id[1]) * nlo[2] + id[2]) * nlo[3] + id[3]];
+                }
+                dst[o] = v;
+              }
+      }
+    }
+    // translational invariance: d/dC = -(d/dA + d/dB + d/dD)
+    for (int xyz = 0; xyz < 3; ++xyz) {
+      double* dC = &cart[size_t(6 + xyz) * ncart4];
+      const double* dA = &cart[size_t(0 + xyz) * ncart4];
+      const double* dB = &cart[size_t(3 + xyz) * ncart4];
+      const double* dD = &cart[size_t(9 + xyz) * ncart4];
+      for (size_t o = 0; o < ncart4; ++o) dC[o] = -(dA[o] + dB[o] + dD[o]);
+    }
+  }
+
+  // Cartesian -> solid harmonics per index (canonical frame)
+  int n[4];
+  for (int k = 0; k < 4; ++k) n[k] = sh[k].pure ? npure(sh[k].l) : ncart(sh[k].l);
+  const size_t nsph4 = size_t(n[0]) * n[1] * n[2] * n[3];
+  std::vector<double> sph(nsets * nsph4);
+  for (int s = 0; s < nsets; ++s) {
+    std::vector<double> cur(cart.begin() + s * ncart4, cart.begin() + (s + 1) * ncart4);
+    int dims[4] = {nca, ncb, ncc, ncd};
+    for (int k = 0; k < 4; ++k) {
+      if (!sh[k].pure) continue;
+      const auto& M = sph_matrix(sh[k].l);
+      const int nc_k = dims[k], np_k = npure(sh[k].l);
+      size_t outer = 1, inner = 1;
+      for (int t = 0; t < k; ++t) outer *= dims[t];
+      for (int t = k + 1; t < 4; ++t) inner *= dims[t];
+      std::vector<double> nxt(outer * np_k * inner, 0.0);
+      for (size_t o = 0; o < outer; ++o)
+        for (int p = 0; p < np_k; ++p)
+          for (int c = 0; c < nc_k; ++c) {
+            const double coef = M[size_t(p) * nc_k + c];
+            if (coef == 0.0) continue;
+            const double* src = &cur[(o * nc_k + c) * inner];
+            double* dst = &nxt[(o * np_k + p) * inner];
+            for (size_t i = 0; i < inner; ++i) dst[i] += coef * src[i];
+          }
+      cur.swap(nxt);
+      dims[k] = np_k;
+    }
+    std::memcpy(&sph[s * nsph4], cur.data(), nsph4 * sizeof(double));
+  }
+
+  // un-permute into the caller's (tbra1 tbra2|tket1 tket2) order and remap
+  // derivative shell sets to the caller's centres.
+  int tn[4];
+  for (int k = 0; k < 4; ++k) tn[q.perm[k]] = n[k];
+  for (int s = 0; s < nsets; ++s) {
+    int ts = s;
+    if (deriv) ts = q.perm[s / 3] * 3 + s % 3;
+    const double* src = &sph[s * nsph4];
+    double* dst = out + size_t(ts) * nsph4;
+    int it[4];
+    size_t o = 0;
+    for (it[0] = 0; it[0] < tn[0]; ++it[0])
+      for (it[1] = 0; it[1] < tn[1]; ++it[1])
+        for (it[2] = 0; it[2] < tn[2]; ++it[2])
+          for (it[3] = 0; it[3] < tn[3]; ++it[3], ++o) {
+            const size_t ci =
+                ((size_t(it[q.perm[0]]) * n[1] + it[q.perm[1]]) * n[2] + it[q.perm[2]]) * n[3] +
+                it[q.perm[3]];
+            dst[o] = src[ci];
+          }
+  }
+  return (int)nsph4;
+}
+
+int nfunc(const orc_basis* bs, int s) {
+  return bs->pure[s] ? npure(bs->l[s]) : ncart(bs->l[s]);
+}
+
+int nthreads_or_default(int n) {
+#ifdef _OPENMP
+  return n > 0 ? n : omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+}  // namespace
+
+// ===================================================================== C API
+extern "C" {
+
+void orc_boys(double T, int mmax, double* F) { boys(T, mmax, F); }
+
+double orc_solid_coeff(int l, int m, int lx, int ly, int lz) {
+  return solid_coeff(l, m, lx, ly, lz);
+}
+
+void orc_shell_normalize(int l, int nprim, const double* alpha,
+                         const double* coeff_in, double* coeff_out,
+                         double* max_ln_coeff_out) {
+  // Shell::renorm (shell.h:958-999): coefficients refer to unit-normalized
+  // primitives on input; embed N_p = sqrt(2^l (2a)^{l+3/2} /
+  // (pi^{3/2} (2l-1)!!)) and rescale to unit self-overlap.
+  const double sqrt_pi3 = 5.56832799683170784528481798212;
+  std::vector<double> c(coeff_in, coeff_in + nprim);
+  for (int p = 0; p < nprim; ++p)
+    if (alpha[p] != 0) {
+      const double ta = 2 * alpha[p];
+      const double ta_l32 = std::pow(ta, l + 1) * std::sqrt(ta);
+      c[p] *= std::sqrt(std::pow(2, l) * ta_l32 / (sqrt_pi3 * dfac(2 * l - 1)));
+    }
+  double norm = 0;
+  for (int p = 0; p < nprim; ++p)
+    for (int q = 0; q <= p; ++q) {
+      const double g = alpha[p] + alpha[q];
+      norm += (p == q ? 1 : 2) * dfac(2 * l - 1) * sqrt_pi3 * c[p] * c[q] /
+              (std::pow(2, l) * std::pow(g, l + 1) * std::sqrt(g));
+    }
+  const double f = 1 / std::sqrt(norm);
+  for (int p = 0; p < nprim; ++p) {
+    coeff_out[p] = c[p] * f;
+    max_ln_coeff_out[p] = std::log(std::abs(coeff_out[p]));
+  }
+}
+
+int orc_shellpair_init(int l1, int nprim1, const double* alpha1,
+                       const double* coeff1, const double* O1, int l2,
+                       int nprim2, const double* alpha2, const double* coeff2,
+                       const double* O2, double ln_prec, int method, double* P,
+                       double* K, double* oogamma, double* nonsph,
+                       double* ln_scr, int* p1, int* p2) {
+  ShellView a, b;
+  a.l = l1; a.pure = 0; a.nprim = nprim1; a.O = O1; a.alpha = alpha1; a.coeff = coeff1;
+  b.l = l2; b.pure = 0; b.nprim = nprim2; b.O = O2; b.alpha = alpha2; b.coeff = coeff2;
+  for (int p = 0; p < nprim1; ++p) a.max_ln_coeff[p] = std::log(std::abs(coeff1[p]));
+  for (int p = 0; p < nprim2; ++p) b.max_ln_coeff[p] = std::log(std::abs(coeff2[p]));
+  std::vector<PrimPair> pp(size_t(nprim1) * nprim2);
+  const int n = pair_init(a, b, ln_prec, method, pp.data());
+  for (int i = 0; i < n; ++i) {
+    for (int x = 0; x < 3; ++x) P[3 * i + x] = pp[i].P[x];
+    K[i] = pp[i].K;
+    oogamma[i] = pp[i].oog;
+    nonsph[i] = pp[i].nonsph;
+    ln_scr[i] = pp[i].ln_scr;
+    p1[i] = pp[i].p1;
+    p2[i] = pp[i].p2;
+  }
+  return n;
+}
+
+int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
+                        int deriv, double precision, int method, double* out) {
+  if (deriv < 0 || deriv > 1) return -1;
+  thread_local Work w;
+  const int tgt[4] = {s1, s2, s3, s4};
+  return compute_quartet(bs, tgt, deriv, precision, method, w, out);
+}
+
+void orc_schwarz(const orc_basis* bs, double* Kmat, int nthreads) {
+  const int ns = bs->nshell;
+  const int nt = nthreads_or_default(nthreads);
+#pragma omp parallel for schedule(dynamic) num_threads(nt)
+  for (int s1 = 0; s1 < ns; ++s1) {
+    Work w;
+    std::vector<double> buf;
+    for (int s2 = 0; s2 <= s1; ++s2) {
+      const int n = nfunc(bs, s1) * nfunc(bs, s2);
+      buf.assign(size_t(n) * n, 0.0);
+      const int tgt[4] = {s1, s2, s1, s2};
+      const int nv = compute_quartet(bs, tgt, 0, 0.0, 0, w, buf.data());
+      double mx = 0;
+      for (int i = 0; i < nv; ++i) mx = std::max(mx, std::abs(buf[i]));
+      Kmat[size_t(s1) * ns + s2] = Kmat[size_t(s2) * ns + s1] = std::sqrt(mx);
+    }
+  }
+}
+
+int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,
+                      const double* Ks, double thresh, const double* D,
+                      double* J, double* K, int nthreads, int64_t pb_begin,
+                      int64_t pb_end, int64_t* n_integrals) {
+  const int ns = bs->nshell;
+  const int nt = nthreads_or_default(nthreads);
+  std::vector<std::vector<double>> Jt(nt), Kt(nt);
+  int64_t nq = 0, nint = 0;
+  const double eps = std::numeric_limits<double>::epsilon();
+#pragma omp parallel num_threads(nt) reduction(+ : nq, nint)
+  {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#else
+    const int tid = 0;
+#endif
+    Jt[tid].assign(size_t(nbf) * nbf, 0.0);
+    Kt[tid].assign(size_t(nbf) * nbf, 0.0);
+    double* Jl = Jt[tid].data();
+    double* Kl = Kt[tid].data();
+    Work w;
+    std::vector<double> buf;
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t pb = pb_begin; pb < pb_end; ++pb) {
+      // bra pair index pb = s1*(s1+1)/2 + s2, s2 <= s1
+      int s1 = int((std::sqrt(8.0 * pb + 1) - 1) / 2);
+      while (int64_t(s1) * (s1 + 1) / 2 > pb) --s1;
+      while (int64_t(s1 + 1) * (s1 + 2) / 2 <= pb) ++s1;
+      const int s2 = int(pb - int64_t(s1) * (s1 + 1) / 2);
+      const double K12 = Ks[size_t(s1) * ns + s2];
+      for (int s3 = 0; s3 <= s1; ++s3) {
+        const int s4max = (s1 == s3) ? s2 : s3;
+        for (int s4 = 0; s4 <= s4max; ++s4) {
+          if (K12 * Ks[size_t(s3) * ns + s4] < thresh) continue;
+          const int n1 = nfunc(bs, s1), n2 = nfunc(bs, s2), n3 = nfunc(bs, s3),
+                    n4 = nfunc(bs, s4);
+          buf.resize(size_t(n1) * n2 * n3 * n4);
+          const int tgt[4] = {s1, s2, s3, s4};
+          const int nv = compute_quartet(bs, tgt, 0, eps, 0, w, buf.data());
+          ++nq;
+          nint += int64_t(n1) * n2 * n3 * n4;
+          if (nv == 0) continue;
+          const double deg = (s1 == s2 ? 1.0 : 2.0) * (s3 == s4 ? 1.0 : 2.0) *
+                             (s1 == s3 ? (s2 == s4 ? 1.0 : 2.0) : 2.0);
+          const int o1 = bf_off[s1], o2 = bf_off[s2], o3 = bf_off[s3], o4 = bf_off[s4];
+          size_t f = 0;
+          for (int a = o1; a < o1 + n1; ++a)
+            for (int b = o2; b < o2 + n2; ++b)
+              for (int c = o3; c < o3 + n3; ++c)
+                for (int d = o4; d < o4 + n4; ++d, ++f) {
+                  const double v = buf[f] * deg;
+                  Jl[size_t(a) * nbf + b] += D[size_t(c) * nbf + d] * v;
+                  Jl[size_t(c) * nbf + d] += D[size_t(a) * nbf + b] * v;
+                  Kl[size_t(a) * nbf + c] += D[size_t(b) * nbf + d] * v;
+                  Kl[size_t(b) * nbf + d] += D[size_t(a) * nbf + c] * v;
+                  Kl[size_t(a) * nbf + d] += D[size_t(b) * nbf + c] * v;
+                  Kl[size_t(b) * nbf + c] += D[size_t(a) * nbf + d] * v;
+                }
+        }
+      }
+    }
+  }
+  // J = 1/2 sym(Jacc), K = 1/4 sym(Kacc) (libint's G = 2J - K form,
+  // hartree-fock++.cc:1721-1743,1766)
+  for (int t = 0; t < nt; ++t)
+    for (int a = 0; a < nbf; ++a)
+      for (int b = 0; b < nbf; ++b) {
+        J[size_t(a) * nbf + b] += 0.25 * (Jt[t][size_t(a) * nbf + b] + Jt[t][size_t(b) * nbf + a]);
+        K[size_t(a) * nbf + b] += 0.125 * (Kt[t][size_t(a) * nbf + b] + Kt[t][size_t(b) * nbf + a]);
+      }
+  if (n_integrals) *n_integrals = nint;
+  return nq;
+}
+
+int64_t orc_jk(const orc_basis* bs, const int* bf_off, int nbf, const double* Ks,
+               double thresh, const double* D, double* J, double* K,
+               int nthreads) {
+  std::memset(J, 0, sizeof(double) * nbf * nbf);
+  std::memset(K, 0, sizeof(double) * nbf * nbf);
+  const int64_t ns = bs->nshell;
+  return orc_jk_sample(bs, bf_off, nbf, Ks, thresh, D, J, K, nthreads, 0,
+                       ns * (ns + 1) / 2, nullptr);
+}
+
+int64_t orc_jk_grad(const orc_basis* bs, const int* bf_off, int nbf,
+                    int natoms, const double* Ks, double thresh,
+                    const double* D, double* gJ, double* gK, int nthreads) {
+  const int ns = bs->nshell;
+  const int nt = nthreads_or_default(nthreads);
+  std::vector<std::vector<double>> gJt(nt, std::vector<double>(3 * natoms, 0.0));
+  std::vector<std::vector<double>> gKt(nt, std::vector<double>(3 * natoms, 0.0));
+  int64_t nq = 0;
+  const double eps = std::numeric_limits<double>::epsilon();
+#pragma omp parallel num_threads(nt) reduction(+ : nq)
+  {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#else
+    const int tid = 0;
+#endif
+    Work w;
+    std::vector<double> buf;
+#pragma omp for schedule(dynamic, 1)
+    for (int s1 = 0; s1 < ns; ++s1)
+      for (int s2 = 0; s2 <= s1; ++s2) {
+        const double K12 = Ks[size_t(s1) * ns + s2];
+        for (int s3 = 0; s3 <= s1; ++s3) {
+          const int s4max = (s1 == s3) ? s2 : s3;
+          for (int s4 = 0; s4 <= s4max; ++s4) {
+            if (K12 * Ks[size_t(s3) * ns + s4] < thresh) continue;
+            const int n1 = nfunc(bs, s1), n2 = nfunc(bs, s2),
+                      n3 = nfunc(bs, s3), n4 = nfunc(bs, s4);
+            const size_t n1234 = size_t(n1) * n2 * n3 * n4;
+            buf.resize(12 * n1234);
+            const int tgt[4] = {s1, s2, s3, s4};
+            const int nv = compute_quartet(bs, tgt, 1, eps, 0, w, buf.data());
+            ++nq;
+            if (nv == 0) continue;
+            const double deg = (s1 == s2 ? 1.0 : 2.0) * (s3 == s4 ? 1.0 : 2.0) *
+                               (s1 == s3 ? (s2 == s4 ? 1.0 : 2.0) : 2.0);
+            const int o1 = bf_off[s1], o2 = bf_off[s2], o3 = bf_off[s3],
+                      o4 = bf_off[s4];
+            const int atoms[4] = {bs->atom[s1], bs->atom[s2], bs->atom[s3], bs->atom[s4]};
+            for (int d = 0; d < 12; ++d) {
+              double sj = 0, sk = 0;
+              const double* v = &buf[d * n1234];
+              size_t f = 0;
+              for (int a = o1; a < o1 + n1; ++a)
+                for (int b = o2; b < o2 + n2; ++b)
+                  for (int c = o3; c < o3 + n3; ++c)
+                    for (int dd = o4; dd < o4 + n4; ++dd, ++f) {
+                      sj += v[f] * D[size_t(a) * nbf + b] * D[size_t(c) * nbf + dd];
+                      sk += v[f] * 0.5 *
+                            (D[size_t(a) * nbf + c] * D[size_t(b) * nbf + dd] +
+                             D[size_t(a) * nbf + dd] * D[size_t(b) * nbf + c]);
+                    }
+              const int at = atoms[d / 3];
+              gJt[tid][3 * at + d % 3] += 0.5 * deg * sj;
+              gKt[tid][3 * at + d % 3] += -0.25 * deg * sk;
+            }
+          }
+        }
+      }
+  }
+  for (int i = 0; i < 3 * natoms; ++i) {
+    gJ[i] = 0;
+    gK[i] = 0;
+    for (int t = 0; t < nt; ++t) {
+      gJ[i] += gJt[t][i];
+      gK[i] += gKt[t][i];
+    }
+  }
+  return nq;
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// oracle/oracle.h -- TEST INFRASTRUCTURE ONLY.
+//
+// FP64 CPU restatement of libint's Coulomb ERI path (libint2::Engine
+// compute2<Operator::coulomb, BraKet::xx_xx, 0|1>), used by tests/ as the
+// checker of the CUDA path, by __graft_entry__.smoke() and by bench.py's
+// cpu_baseline / --impl reference arm.  The product (libint_gb300/) never
+// links, loads or calls it.
+//
+// Reference anchors (paths inside the libint tree):
+//   Shell::renorm                     include/libint2/shell.h:958-999
+//   ShellPair::init (Original/Cons.)  include/libint2/shell.h:1138-1256
+//   Boys F_m(T) (Taylor + recursion)  include/libint2/boys.h:519-879
+//   primitive-quartet data/screening  include/libint2/engine.impl.h:1306-1766
+//   canonical swap / un-permutation   include/libint2/engine.impl.h:1181-1211,1988-2086
+//   OS VRR                            src/bin/libint/vrr_11_twoprep_11.h:88-666
+//   contraction point (e0|f0)         src/bin/libint/dg.cc:1177-1189
+//   HRR                               src/bin/libint/hrr.h:246-347
+//   derivative shell-set order/remap  include/libint2/deriv_map.h:170-262
+//   solid harmonics (IJQC 54,83 eq15) include/libint2/solidharmonics.h:114-174
+//   J/K digestion, Schwarz            tests/hartree-fock/hartree-fock++.cc:1231-1298,1574-1772
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Boys function F_m(T), m = 0..mmax (mmax <= 40).
+void orc_boys(double T, int mmax, double* F);
+
+// Shell::renorm(): embeds primitive normalization and rescales the
+// contraction to unit self-overlap.  coeff_out/max_ln_coeff_out: nprim each.
+void orc_shell_normalize(int l, int nprim, const double* alpha,
+                         const double* coeff_in, double* coeff_out,
+                         double* max_ln_coeff_out);
+
+// Real solid-harmonic coefficient of Cartesian (lx,ly,lz) in S_{l,m}
+// (standard Cartesian normalization, standard m = -l..l ordering).
+double orc_solid_coeff(int l, int m, int lx, int ly, int lz);
+
+// ShellPair::init with Original (0) or Conservative (1) screening.
+// Per surviving primitive pair writes P[3], K, 1/gamma, nonsph, ln_scr, p1, p2.
+int orc_shellpair_init(int l1, int nprim1, const double* alpha1,
+                       const double* coeff1, const double* O1, int l2,
+                       int nprim2, const double* alpha2, const double* coeff2,
+                       const double* O2, double ln_prec, int method, double* P,
+                       double* K, double* oogamma, double* nonsph,
+                       double* ln_scr, int* p1, int* p2);
+
+// A basis: nshell shells, flattened primitive data (normalized coefficients).
+typedef struct {
+  int nshell;
+  const int* l;         // [nshell]
+  const int* pure;      // [nshell]
+  const int* nprim;     // [nshell]
+  const int* prim_off;  // [nshell] offset into alpha/coeff
+  const int* atom;      // [nshell] atom index of the shell centre
+  const double* O;      // [3*nshell]
+  const double* alpha;  // flattened
+  const double* coeff;  // flattened, normalization embedded
+} orc_basis;
+
+// Engine::compute(s1,s2,s3,s4) for shells given by index into the basis.
+// precision: Engine::set_precision(); method: 0 Original, 1 Conservative.
+// Writes nsets (1 or 12) shell sets in libint's buffer order to out.
+// Returns the number of values per set, or 0 if every primitive quartet was
+// screened out (libint returns results()[0] == nullptr), <0 on error.
+int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
+                        int deriv, double precision, int method, double* out);
+
+// Schwarz factors K(s1,s2) = sqrt(max|(s1 s2|s1 s2)|) (precision 0).
+void orc_schwarz(const orc_basis* bs, double* K, int nthreads);
+
+// J/K build over unique shell quartets with |K12*K34| >= schwarz_thresh,
+// FP64 digestion with the 8-fold degeneracy factors.  D, J, K: nbf x nbf,
+// row-major.  bf_off: [nshell] first basis function of each shell.
+// Returns the number of computed (non-screened) shell quartets.
+int64_t orc_jk(const orc_basis* bs, const int* bf_off, int nbf,
+               const double* Kschwarz, double schwarz_thresh, const double* D,
+               double* J, double* K, int nthreads);
+
+// As orc_jk, but only over the quartets [q_begin, q_end) of the canonical
+// quartet enumeration (used to time a bounded sample); J/K accumulate.
+int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,
+                      const double* Kschwarz, double schwarz_thresh,
+                      const double* D, double* J, double* K, int nthreads,
+                      int64_t bra_pair_begin, int64_t bra_pair_end,
+                      int64_t* n_integrals);
+
+// Nuclear gradients of E_J = 1/2 sum D J and E_K = -1/4 sum D K from
+// deriv_order=1 integrals.  gJ, gK: natoms x 3.
+int64_t orc_jk_grad(const orc_basis* bs, const int* bf_off, int nbf,
+                    int natoms, const double* Kschwarz, double schwarz_thresh,
+                    const double* D, double* gJ, double* gK, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
