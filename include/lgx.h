@@ -1,0 +1,190 @@
+/* lgx.h -- C ABI of the GB300-native Coulomb ERI library (liblgx.so).
+ *
+ * The library computes two-electron Coulomb repulsion integrals (ERIs) over
+ * contracted Gaussian shells on one NVIDIA GB300 (sm_103a), with the buffer
+ * layout and conventions of libint2::Engine (Operator::coulomb,
+ * BraKet::xx_xx, deriv_order 0 and 1), plus batched and fused J/K entry
+ * points.  Plain C types only; every call returns an lgx_status and never
+ * aborts.  A context is bound to one CUDA device and one CUDA stream; calls
+ * on one context are serialized, distinct contexts may be used from distinct
+ * threads (the reference's one-Engine-per-thread model).
+ *
+ * Conventions shared with the reference (file:line inside the libint tree):
+ *  - shells carry normalization-embedded contraction coefficients
+ *    (Shell::renorm, include/libint2/shell.h:958-999);
+ *  - Cartesian components in the standard order
+ *    (include/libint2/cgshell_ordering.h:125-131), solid harmonics in the
+ *    standard m = -l..l order (include/libint2/shgshell_ordering.h:56);
+ *  - shell sets are row-major n1*n2*n3*n4 in the caller's shell order
+ *    (include/libint2/engine.h:747-781); first-derivative sets come as 12
+ *    sets ordered A_x,A_y,A_z,B_x,...,D_z
+ *    (include/libint2/deriv_map.h:170-262, build_libint.cc:1062-1085).
+ */
+#ifndef LGX_H
+#define LGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int lgx_status;
+#define LGX_OK 0
+#define LGX_ERR_INVALID_ARG 1   /* bad pointer / size / argument            */
+#define LGX_ERR_CUDA 2          /* a CUDA runtime call failed                */
+#define LGX_ERR_LMAX_EXCEEDED 3 /* Engine::lmax_exceeded (engine.h:893-905)  */
+#define LGX_ERR_NO_BASIS 4      /* batched call before lgx_set_basis         */
+#define LGX_ERR_WATCHDOG 5      /* a device-side bounded wait expired        */
+#define LGX_ERR_TOO_LARGE 6     /* request exceeds a documented size limit   */
+#define LGX_ERR_NO_DEVICE 7     /* no CUDA device / wrong architecture       */
+
+/* Largest angular momentum per shell and derivative order supported. */
+#define LGX_MAX_L 3
+#define LGX_MAX_DERIV 1
+#define LGX_MAX_NPRIM 16
+
+/* Primitive-screening methods (ScreeningMethod, shell.h:1041-1059). */
+#define LGX_SCREEN_ORIGINAL 0
+#define LGX_SCREEN_CONSERVATIVE 1
+
+/* Precision modes of the batched paths. */
+#define LGX_FP64 0  /* every quartet in FP64                                 */
+#define LGX_MIXED 1 /* FP32 VRR/HRR/contraction when K12*K34 < mixed_thresh  */
+
+typedef struct lgx_context lgx_context;
+
+/* One contracted shell (libint2::Shell with one contraction). */
+typedef struct {
+  int32_t l;            /* angular momentum, 0..LGX_MAX_L                    */
+  int32_t pure;         /* 1: solid harmonics, 0: Cartesian                  */
+  int32_t nprim;        /* 1..LGX_MAX_NPRIM                                  */
+  int32_t pad_;
+  double origin[3];     /* bohr                                              */
+  const double* alpha;  /* [nprim] exponents                                 */
+  const double* coeff;  /* [nprim] normalization-embedded coefficients       */
+} lgx_shell;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device` (replaces libint2::initialize(),
+ * include/libint2/initialize.h:76-95, plus Engine construction,
+ * engine.h:502-526).  Fails with LGX_ERR_NO_DEVICE when no usable GPU. */
+lgx_status lgx_create(lgx_context** ctx, int device);
+/* libint2::finalize() counterpart; releases every device resource. */
+lgx_status lgx_destroy(lgx_context* ctx);
+/* Message of the last failed call on this context (never NULL). */
+const char* lgx_last_error(const lgx_context* ctx);
+/* Library version string. */
+const char* lgx_version(void);
+
+/* ------------------------------------------------------- Engine::compute */
+
+/* Engine::compute(s1,s2,s3,s4) / compute2<coulomb,xx_xx,deriv>
+ * (include/libint2/engine.impl.h:140-175,1151-2113).  `shells` are the four
+ * shells in caller order; `precision` is Engine::set_precision()
+ * (engine.h:809-823; <= 0 disables primitive screening); `screening` is one
+ * of LGX_SCREEN_*.  On success writes *nsets (1 or 12) shell sets of
+ * *nvalues doubles each, row-major in the caller's shell order, to the HOST
+ * buffer `out` (capacity `out_capacity` doubles), and *is_null = 1 when every
+ * primitive quartet was screened out (libint returns results()[0]==nullptr,
+ * engine.impl.h:1781-1784; `out` is then untouched). */
+lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4],
+                                int deriv, double precision, int screening,
+                                double* out, size_t out_capacity, int* nsets,
+                                int* nvalues, int* is_null);
+
+/* ----------------------------------------------------------- basis state */
+
+/* Uploads a basis (a libint2::BasisSet, basis.h.in:134-182, flattened):
+ * nshell shells, per-shell l/pure/nprim/atom index, origins [3*nshell]
+ * (bohr), and the flattened exponents / normalization-embedded coefficients
+ * of all shells in order.  Replaces any previous basis of the context. */
+lgx_status lgx_set_basis(lgx_context* ctx, int nshell, const int32_t* l,
+                         const int32_t* pure, const int32_t* nprim,
+                         const int32_t* atom, const double* origins,
+                         const double* alpha, const double* coeff);
+/* Number of basis functions of the current basis. */
+lgx_status lgx_basis_nbf(lgx_context* ctx, int* nbf);
+
+/* Schwarz factors K(s1,s2) = sqrt(max |(s1 s2|s1 s2)|) for every shell pair
+ * of the basis into the HOST array K [nshell*nshell] (compute_schwarz_ints,
+ * tests/hartree-fock/hartree-fock++.cc:1231-1298, infinity norm). */
+lgx_status lgx_schwarz(lgx_context* ctx, double* K);
+
+/* Batched Engine::compute over an explicit quartet list: `quartets` holds
+ * 4*n shell indices (caller order, HOST memory); set q is written at
+ * out + offsets[q] (HOST memory, doubles) in libint's buffer order, nsets
+ * consecutive sets per quartet.  `offsets` may be NULL, in which case sets
+ * are packed back to back in list order.  is_null (optional, n ints)
+ * receives 1 for fully screened quartets.  mode: LGX_FP64 or LGX_MIXED
+ * (FP32 arithmetic for quartets whose Schwarz bound K12*K34 < mixed_thresh). */
+lgx_status lgx_compute_batch(lgx_context* ctx, const int32_t* quartets,
+                             int64_t n, int deriv, int mode,
+                             double mixed_thresh, const int64_t* offsets,
+                             double* out, size_t out_capacity,
+                             int32_t* is_null);
+
+/* Statistics of one J/K (or gradient) pass. */
+typedef struct {
+  int64_t quartets_fp64;   /* shell quartets computed in FP64             */
+  int64_t quartets_fp32;   /* shell quartets computed in FP32             */
+  int64_t integrals;       /* spherical integrals computed (both modes)   */
+  int64_t prim_quartets;   /* primitive quartets entering the VRR         */
+  double kernel_ms;        /* device time of the integral kernels         */
+} lgx_jk_stats;
+
+/* Coulomb and exchange matrices J_ab = sum_cd (ab|cd) D_cd and
+ * K_ab = sum_cd (ac|bd) D_cd over all unique quartets whose Schwarz bound
+ * K12*K34 >= schwarz_thresh, digested with the 8-fold degeneracy factors of
+ * compute_2body_fock (hartree-fock++.cc:1628-1766) in FP64 accumulators.
+ * D, J, K are nbf*nbf row-major HOST arrays (D symmetric). */
+lgx_status lgx_jk(lgx_context* ctx, const double* D, double* J, double* K,
+                  double schwarz_thresh, int mode, double mixed_thresh,
+                  lgx_jk_stats* stats);
+/* Same, with D, J, K in DEVICE memory (no host copies). */
+lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ,
+                         double* dK, double schwarz_thresh, int mode,
+                         double mixed_thresh, lgx_jk_stats* stats);
+
+/* Nuclear gradients of E_J = 1/2 sum D.J and E_K = -1/4 sum D.K from
+ * deriv_order = 1 integrals (compute_2body_fock_deriv<1>,
+ * hartree-fock++.cc:1776-2000, per-atom digestion :1909-1973).
+ * gJ, gK: natoms*3 HOST arrays; natoms = 1 + max atom index of the basis. */
+lgx_status lgx_jk_grad(lgx_context* ctx, const double* D, double* gJ,
+                       double* gK, int natoms, double schwarz_thresh,
+                       lgx_jk_stats* stats);
+
+/* -------------------------------------------------------- host utilities */
+
+/* Shell::renorm (shell.h:958-999): coeff_out = normalization-embedded
+ * coefficients for unit-normalized-primitive input coefficients. */
+lgx_status lgx_shell_normalize(int l, int nprim, const double* alpha,
+                               const double* coeff_in, double* coeff_out);
+
+/* BasisSet(name, atoms) with the G94 reader of basis.h.in:473-621: loads
+ * `<data_dir>/<name>.g94` (name canonicalized: lower case, '*'->'_st_')
+ * for natoms atoms with atomic numbers Z and positions xyz (bohr).
+ * Call with l == NULL to get *nshell and *nprim_total only; then call again
+ * with arrays of that size.  pure follows the reference (l > 1 unless the
+ * Gaussian Cartesian-d convention applies). */
+lgx_status lgx_basis_load(const char* data_dir, const char* name, int natoms,
+                          const int32_t* Z, const double* xyz, int* nshell,
+                          int* nprim_total, int32_t* l, int32_t* pure,
+                          int32_t* nprim, int32_t* atom, double* origins,
+                          double* alpha, double* coeff);
+
+/* Synthetic water cluster: nx*ny*nz molecules, O on a grid with `spacing`
+ * angstrom, each jittered by uniform(-jitter, jitter) angstrom per axis,
+ * H at 0.96 A and 104.5 deg with a uniformly random orientation, from a
+ * seeded mt19937_64.  Writes Z [3*n] and xyz [9*n] (bohr, CODATA 2018
+ * 0.529177210903 A/bohr, atom.h:52-55), atoms ordered O,H,H per molecule. */
+lgx_status lgx_water_cluster(int nx, int ny, int nz, double spacing,
+                             double jitter, uint64_t seed, int32_t* Z,
+                             double* xyz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LGX_H */

@@ -1,0 +1,446 @@
+"""libint_gb300 -- GB300-native Coulomb ERIs with libint2's interface.
+
+Host-side mirror of the reference's Python/C++ interface for the Coulomb
+ERI path (python/src/libint2/libint2.cc, include/libint2/engine.h): Shell,
+BasisSet, Atom, Operator, BraKet, ScreeningMethod, Engine with
+compute(s1, s2, s3, s4) returning libint's buffer order, plus the batched
+J/K and gradient passes.  All arithmetic runs in liblgx.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lgx
+from ._lgx import LgxError
+
+__all__ = ["Shell", "BasisSet", "Atom", "Operator", "BraKet", "ScreeningMethod",
+           "Engine", "Context", "coulomb", "initialize", "finalize", "water_cluster",
+           "LgxError", "MAX_AM", "DATA_PATH"]
+
+MAX_AM = 3
+DATA_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "basis")
+BOHR_TO_ANGSTROM = 0.529177210903  # CODATA 2018 (include/libint2/atom.h:52-55)
+
+
+class Operator(enum.Enum):
+    """libint2::Operator (engine.h:98-184); only coulomb is implemented."""
+    coulomb = 2
+
+
+class BraKet(enum.Enum):
+    """libint2::BraKet; only xx_xx (four-centre) is implemented."""
+    XXXX = 1
+    xx_xx = 1
+
+
+class ScreeningMethod(enum.IntEnum):
+    """libint2::ScreeningMethod (shell.h:1041-1059), primitive screening."""
+    Original = 0
+    Conservative = 1
+
+
+def _ncart(l):
+    return (l + 1) * (l + 2) // 2
+
+
+class Shell:
+    """libint2::Shell with one contraction.  `primitives` are
+    (exponent, coefficient) pairs with coefficients of unit-normalized
+    primitives; normalization is embedded on construction (Shell::renorm,
+    shell.h:958-999).  Python-binding defaults: center at the origin,
+    pure=True (python/src/libint2/libint2.cc:155-160)."""
+
+    def __init__(self, L: int, primitives: Sequence[tuple], center=(0.0, 0.0, 0.0),
+                 pure: bool = True, embed_normalization: bool = True):
+        self.l = int(L)
+        self.alpha = np.ascontiguousarray([float(a) for a, _ in primitives])
+        c_in = np.ascontiguousarray([float(c) for _, c in primitives])
+        self._coeffs_in = c_in.copy()
+        if embed_normalization:
+            out = np.zeros_like(c_in)
+            _lgx.check(_lgx.load().lgx_shell_normalize(self.l, len(c_in), _lgx.ptr(self.alpha),
+                                                        _lgx.ptr(c_in), _lgx.ptr(out)),
+                       None, "lgx_shell_normalize")
+            self.coeff = out
+        else:
+            self.coeff = c_in
+        self.O = np.asarray(center, dtype=float).reshape(3).copy()
+        self.pure = bool(pure)
+
+    @classmethod
+    def from_normalized(cls, L, alpha, coeff, center, pure):
+        s = cls.__new__(cls)
+        s.l = int(L)
+        s.alpha = np.ascontiguousarray(alpha, dtype=float)
+        s.coeff = np.ascontiguousarray(coeff, dtype=float)
+        s._coeffs_in = None
+        s.O = np.asarray(center, dtype=float).reshape(3).copy()
+        s.pure = bool(pure)
+        return s
+
+    def size(self) -> int:
+        return 2 * self.l + 1 if self.pure else _ncart(self.l)
+
+    def nprim(self) -> int:
+        return len(self.alpha)
+
+    @property
+    def coeffs(self):
+        return list(self.coeff)
+
+    def move(self, center):
+        self.O = np.asarray(center, dtype=float).reshape(3).copy()
+        return self
+
+    def _c(self) -> _lgx.LgxShell:
+        r = _lgx.LgxShell()
+        r.l = self.l
+        r.pure = 1 if self.pure else 0
+        r.nprim = len(self.alpha)
+        for x in range(3):
+            r.origin[x] = self.O[x]
+        r.alpha = _lgx.ptr(self.alpha)
+        r.coeff = _lgx.ptr(self.coeff)
+        return r
+
+    def __repr__(self):
+        return "Shell(l=%d, pure=%s, nprim=%d, O=%s)" % (self.l, self.pure, self.nprim(),
+                                                         list(self.O))
+
+
+class Atom(tuple):
+    """(Z, [x, y, z]) in bohr, like libint2::Atom."""
+
+    def __new__(cls, Z, xyz):
+        return super().__new__(cls, (int(Z), tuple(float(v) for v in xyz)))
+
+
+class BasisSet(list):
+    """libint2::BasisSet: shells on atoms from a G94 library file
+    (basis.h.in:134-182, read_g94_basis_library :473-621)."""
+
+    def __init__(self, name_or_shells, atoms=None, data_path: str | None = None):
+        if atoms is None:
+            super().__init__(name_or_shells)
+            self.name = None
+            self.atom_of_shell = [0] * len(self)
+            return
+        super().__init__()
+        self.name = name_or_shells
+        Z = np.ascontiguousarray([int(a[0]) for a in atoms], dtype=np.int32)
+        xyz = np.ascontiguousarray([list(a[1]) for a in atoms], dtype=float).reshape(-1)
+        lib = _lgx.load()
+        ns, np_ = ctypes.c_int(0), ctypes.c_int(0)
+        dpath = (data_path or os.environ.get("LIBINT_DATA_PATH") or DATA_PATH).encode()
+        st = lib.lgx_basis_load(dpath, self.name.encode(), len(Z), _lgx.ptr(Z, ctypes.c_int32),
+                                _lgx.ptr(xyz), ctypes.byref(ns), ctypes.byref(np_),
+                                None, None, None, None, None, None, None)
+        _lgx.check(st, None, "lgx_basis_load(%s)" % self.name)
+        n, m = ns.value, np_.value
+        l = np.zeros(n, np.int32); pure = np.zeros(n, np.int32); nprim = np.zeros(n, np.int32)
+        atom = np.zeros(n, np.int32); O = np.zeros(3 * n); alpha = np.zeros(m); coeff = np.zeros(m)
+        I = ctypes.c_int32
+        st = lib.lgx_basis_load(dpath, self.name.encode(), len(Z), _lgx.ptr(Z, I), _lgx.ptr(xyz),
+                                ctypes.byref(ns), ctypes.byref(np_), _lgx.ptr(l, I),
+                                _lgx.ptr(pure, I), _lgx.ptr(nprim, I), _lgx.ptr(atom, I),
+                                _lgx.ptr(O), _lgx.ptr(alpha), _lgx.ptr(coeff))
+        _lgx.check(st, None, "lgx_basis_load(%s)" % self.name)
+        off = 0
+        for s in range(n):
+            k = int(nprim[s])
+            self.append(Shell.from_normalized(int(l[s]), alpha[off:off + k], coeff[off:off + k],
+                                              O[3 * s:3 * s + 3], bool(pure[s])))
+            off += k
+        self.atom_of_shell = [int(a) for a in atom]
+
+    # flattened views used by the C ABI and the oracle
+    @property
+    def l(self):
+        return np.array([s.l for s in self], np.int32)
+
+    @property
+    def pure(self):
+        return np.array([1 if s.pure else 0 for s in self], np.int32)
+
+    @pure.setter
+    def pure(self, flag):
+        for s in self:
+            s.pure = bool(flag)
+
+    @property
+    def nprim(self):
+        return np.array([s.nprim() for s in self], np.int32)
+
+    @property
+    def origins(self):
+        return np.concatenate([s.O for s in self]) if len(self) else np.zeros(0)
+
+    @property
+    def alpha(self):
+        return np.concatenate([s.alpha for s in self]) if len(self) else np.zeros(0)
+
+    @property
+    def coeff(self):
+        return np.concatenate([s.coeff for s in self]) if len(self) else np.zeros(0)
+
+    @property
+    def atom(self):
+        return np.array(self.atom_of_shell, np.int32)
+
+    @property
+    def nbf(self) -> int:
+        return int(sum(s.size() for s in self))
+
+    def shell2bf(self):
+        out, o = [], 0
+        for s in self:
+            out.append(o)
+            o += s.size()
+        return out
+
+    functions = property(shell2bf)
+
+    def max_nprim(self):
+        return max(s.nprim() for s in self)
+
+    def max_l(self):
+        return max(s.l for s in self)
+
+
+def water_cluster(nx, ny, nz, spacing=3.0, jitter=0.2, seed=0):
+    """(H2O)_{nx*ny*nz} on a grid (angstrom spacing, uniform jitter), random
+    orientations, 0.96 A / 104.5 deg; atoms in bohr as [(Z, (x, y, z))]."""
+    n = nx * ny * nz
+    Z = np.zeros(3 * n, np.int32)
+    xyz = np.zeros(9 * n)
+    _lgx.check(_lgx.load().lgx_water_cluster(nx, ny, nz, spacing, jitter, seed,
+                                             _lgx.ptr(Z, ctypes.c_int32), _lgx.ptr(xyz)),
+               None, "lgx_water_cluster")
+    return [Atom(int(Z[i]), xyz[3 * i:3 * i + 3]) for i in range(3 * n)]
+
+
+class Context:
+    """One GPU context (lgx_context): basis state, batched and J/K passes."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lgx.load()
+        h = ctypes.c_void_p()
+        st = self._lib.lgx_create(ctypes.byref(h), int(device))
+        if st != _lgx.LGX_OK:
+            raise LgxError(st, "lgx_create failed (no usable sm_100+ CUDA device?)")
+        self._h = h
+        self.basis = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lgx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        _lgx.check(st, self._h, what)
+
+    # ------------------------------------------------------------ engine
+    def compute_shellset(self, shells, deriv=0, precision=np.finfo(float).eps,
+                         screening=ScreeningMethod.Original):
+        arr = (_lgx.LgxShell * 4)(*[s._c() for s in shells])
+        nsets = 12 if deriv else 1
+        nv = int(np.prod([s.size() for s in shells]))
+        out = np.zeros(nsets * nv)
+        ns, nvals, isnull = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        st = self._lib.lgx_compute_shellset(self._h, arr, int(deriv), float(precision),
+                                            int(screening), _lgx.ptr(out), out.size,
+                                            ctypes.byref(ns), ctypes.byref(nvals),
+                                            ctypes.byref(isnull))
+        self._check(st, "lgx_compute_shellset")
+        if isnull.value:
+            return None
+        shape = tuple(s.size() for s in shells)
+        return [out[i * nv:(i + 1) * nv].reshape(shape) for i in range(ns.value)]
+
+    # ------------------------------------------------------------- basis
+    def set_basis(self, basis: BasisSet):
+        I = ctypes.c_int32
+        self._arrs = (basis.l, basis.pure, basis.nprim, basis.atom, basis.origins,
+                      basis.alpha, basis.coeff)
+        l, pure, nprim, atom, O, alpha, coeff = self._arrs
+        st = self._lib.lgx_set_basis(self._h, len(basis), _lgx.ptr(l, I), _lgx.ptr(pure, I),
+                                     _lgx.ptr(nprim, I), _lgx.ptr(atom, I), _lgx.ptr(O),
+                                     _lgx.ptr(alpha), _lgx.ptr(coeff))
+        self._check(st, "lgx_set_basis")
+        self.basis = basis
+
+    def schwarz(self):
+        n = len(self.basis)
+        K = np.zeros((n, n))
+        self._check(self._lib.lgx_schwarz(self._h, _lgx.ptr(K)), "lgx_schwarz")
+        return K
+
+    def compute_batch(self, quartets, deriv=0, mode=_lgx.LGX_FP64, mixed_thresh=1e-4):
+        q = np.ascontiguousarray(quartets, dtype=np.int32).reshape(-1, 4)
+        sizes = np.array([s.size() for s in self.basis], np.int64)
+        nv = sizes[q[:, 0]] * sizes[q[:, 1]] * sizes[q[:, 2]] * sizes[q[:, 3]] * (12 if deriv else 1)
+        offs = np.zeros(len(q), np.int64)
+        if len(q):
+            offs[1:] = np.cumsum(nv)[:-1]
+        out = np.zeros(int(nv.sum()) if len(q) else 1)
+        isnull = np.zeros(max(len(q), 1), np.int32)
+        st = self._lib.lgx_compute_batch(self._h, _lgx.ptr(q, ctypes.c_int32), len(q), int(deriv),
+                                         int(mode), float(mixed_thresh),
+                                         _lgx.ptr(offs, ctypes.c_int64), _lgx.ptr(out),
+                                         out.size, _lgx.ptr(isnull, ctypes.c_int32))
+        self._check(st, "lgx_compute_batch")
+        return out, offs, isnull[:len(q)]
+
+    def jk(self, D, schwarz_thresh=1e-12, mode=_lgx.LGX_FP64, mixed_thresh=1e-4):
+        n = self.basis.nbf
+        D = np.ascontiguousarray(D, dtype=float)
+        J = np.zeros((n, n)); K = np.zeros((n, n))
+        stats = _lgx.LgxJkStats()
+        st = self._lib.lgx_jk(self._h, _lgx.ptr(D), _lgx.ptr(J), _lgx.ptr(K),
+                              float(schwarz_thresh), int(mode), float(mixed_thresh),
+                              ctypes.byref(stats))
+        self._check(st, "lgx_jk")
+        return J, K, stats
+
+    def jk_device(self, dD, dJ, dK, schwarz_thresh=1e-12, mode=_lgx.LGX_FP64,
+                  mixed_thresh=1e-4):
+        """D/J/K given as device pointers (ints), e.g. torch tensor data_ptr()."""
+        stats = _lgx.LgxJkStats()
+        st = self._lib.lgx_jk_device(self._h, ctypes.c_void_p(dD), ctypes.c_void_p(dJ),
+                                     ctypes.c_void_p(dK), float(schwarz_thresh), int(mode),
+                                     float(mixed_thresh), ctypes.byref(stats))
+        self._check(st, "lgx_jk_device")
+        return stats
+
+    def jk_grad(self, D, natoms=None, schwarz_thresh=1e-12):
+        if natoms is None:
+            natoms = int(max(self.basis.atom_of_shell)) + 1
+        D = np.ascontiguousarray(D, dtype=float)
+        gJ = np.zeros((natoms, 3)); gK = np.zeros((natoms, 3))
+        stats = _lgx.LgxJkStats()
+        st = self._lib.lgx_jk_grad(self._h, _lgx.ptr(D), _lgx.ptr(gJ), _lgx.ptr(gK),
+                                   int(natoms), float(schwarz_thresh), ctypes.byref(stats))
+        self._check(st, "lgx_jk_grad")
+        return gJ, gK, stats
+
+
+_DEFAULT_CTX = None
+
+
+def _default_context() -> Context:
+    global _DEFAULT_CTX
+    if _DEFAULT_CTX is None:
+        _DEFAULT_CTX = Context(0)
+    return _DEFAULT_CTX
+
+
+def initialize(device: int = 0):
+    """libint2::initialize() (initialize.h:76-95): creates the GPU context."""
+    global _DEFAULT_CTX
+    if _DEFAULT_CTX is None:
+        _DEFAULT_CTX = Context(device)
+
+
+def finalize():
+    global _DEFAULT_CTX
+    if _DEFAULT_CTX is not None:
+        _DEFAULT_CTX.close()
+        _DEFAULT_CTX = None
+
+
+class Engine:
+    """libint2::Engine for Operator.coulomb / BraKet.xx_xx (engine.h:444-1064).
+
+    compute(s1, s2, s3, s4) returns the shell set in libint's buffer order
+    (row-major, caller's shell order), or None when every primitive quartet
+    was screened out; results() holds the last nshellsets() sets.
+    """
+
+    def __init__(self, oper: Operator = Operator.coulomb, max_nprim: int = 10,
+                 max_l: int = MAX_AM, deriv_order: int = 0,
+                 precision: float = float(np.finfo(float).eps), braket=None,
+                 screening: ScreeningMethod = ScreeningMethod.Original,
+                 context: Context | None = None):
+        if oper != Operator.coulomb:
+            raise NotImplementedError("only Operator.coulomb is implemented")
+        if braket not in (None, BraKet.xx_xx):
+            raise NotImplementedError("only BraKet.xx_xx is implemented")
+        if max_l > MAX_AM:
+            raise LgxError(_lgx.LGX_ERR_LMAX_EXCEEDED, "max_l exceeds LGX_MAX_L")
+        if deriv_order not in (0, 1):
+            raise NotImplementedError("deriv_order must be 0 or 1")
+        self.oper = oper
+        self.braket = BraKet.xx_xx
+        self.max_nprim = max_nprim
+        self.max_l = max_l
+        self.deriv_order = deriv_order
+        self.screening = screening
+        self.set_precision(precision)
+        self._ctx = context
+        self._results = [None]
+
+    def set_precision(self, prec: float):
+        self._precision = max(float(prec), 0.0)
+        return self
+
+    def precision(self):
+        return self._precision
+
+    def set(self, screening: ScreeningMethod):
+        self.screening = ScreeningMethod(screening)
+        return self
+
+    def nshellsets(self):
+        return 12 if self.deriv_order else 1
+
+    def results(self):
+        return self._results
+
+    def compute(self, *shells):
+        if len(shells) == 4 and all(isinstance(s, BasisSet) or isinstance(s, list)
+                                    for s in shells) and not isinstance(shells[0], Shell):
+            return self._compute_basis(*shells)
+        if len(shells) != 4:
+            raise NotImplementedError("only four-centre (xx_xx) integrals are implemented")
+        for s in shells:
+            if s.l > self.max_l:
+                raise LgxError(_lgx.LGX_ERR_LMAX_EXCEEDED, "lmax_exceeded")
+        ctx = self._ctx or _default_context()
+        r = ctx.compute_shellset(shells, self.deriv_order, self._precision, self.screening)
+        self._results = r if r is not None else [None] * self.nshellsets()
+        if r is None:
+            return None
+        return r[0] if self.deriv_order == 0 else r
+
+    def _compute_basis(self, A, B, C, D):
+        nb = [sum(s.size() for s in X) for X in (A, B, C, D)]
+        out = np.zeros(nb)
+        offs = [np.cumsum([0] + [s.size() for s in X]) for X in (A, B, C, D)]
+        for i, a in enumerate(A):
+            for j, b in enumerate(B):
+                for k, c in enumerate(C):
+                    for l, d in enumerate(D):
+                        r = self.compute(a, b, c, d)
+                        if r is None:
+                            continue
+                        blk = r if self.deriv_order == 0 else r[0]
+                        out[offs[0][i]:offs[0][i + 1], offs[1][j]:offs[1][j + 1],
+                            offs[2][k]:offs[2][k + 1], offs[3][l]:offs[3][l + 1]] = blk
+        return out
+
+
+def coulomb() -> Engine:
+    """The reference binding's coulomb() factory: precision 1e-15
+    (python/src/libint2/libint2.cc:50-55)."""
+    return Engine(Operator.coulomb, precision=1e-15)

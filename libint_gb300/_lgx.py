@@ -1,0 +1,121 @@
+"""ctypes binding of liblgx.so (the C ABI declared in include/lgx.h).
+
+The product path: every call lands in the CUDA library; there is no CPU
+fallback.  Loading fails loudly when the shared library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+LGX_OK = 0
+LGX_ERR_INVALID_ARG = 1
+LGX_ERR_CUDA = 2
+LGX_ERR_LMAX_EXCEEDED = 3
+LGX_ERR_NO_BASIS = 4
+LGX_ERR_WATCHDOG = 5
+LGX_ERR_TOO_LARGE = 6
+LGX_ERR_NO_DEVICE = 7
+
+LGX_FP64 = 0
+LGX_MIXED = 1
+LGX_SCREEN_ORIGINAL = 0
+LGX_SCREEN_CONSERVATIVE = 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+class LgxShell(ctypes.Structure):
+    _fields_ = [("l", ctypes.c_int32), ("pure", ctypes.c_int32),
+                ("nprim", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("origin", ctypes.c_double * 3), ("alpha", _dp), ("coeff", _dp)]
+
+
+class LgxJkStats(ctypes.Structure):
+    _fields_ = [("quartets_fp64", ctypes.c_int64), ("quartets_fp32", ctypes.c_int64),
+                ("integrals", ctypes.c_int64), ("prim_quartets", ctypes.c_int64),
+                ("kernel_ms", ctypes.c_double)]
+
+
+# Every symbol include/lgx.h declares, with its ctypes signature.
+SIGNATURES = {
+    "lgx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
+    "lgx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "lgx_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "lgx_version": (ctypes.c_char_p, []),
+    "lgx_compute_shellset": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(LgxShell),
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                            _dp, ctypes.c_size_t,
+                                            ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int)]),
+    "lgx_set_basis": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip, _ip,
+                                     _dp, _dp, _dp]),
+    "lgx_basis_nbf": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "lgx_schwarz": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "lgx_compute_batch": (ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.c_int64, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_double, _i64p, _dp,
+                                         ctypes.c_size_t, _ip]),
+    "lgx_jk": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int,
+                              ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
+    "lgx_jk_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                     ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
+    "lgx_jk_grad": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int,
+                                   ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
+    "lgx_shell_normalize": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
+    "lgx_basis_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, _ip, _dp,
+                                      ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int), _ip, _ip, _ip, _ip, _dp,
+                                      _dp, _dp]),
+    "lgx_water_cluster": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                         _ip, _dp]),
+}
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads liblgx.so (building it first when absent and nvcc exists)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("liblgx.so is not built; run __graft_entry__.build()")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+class LgxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("lgx error %d: %s" % (status, msg))
+        self.status = status
+
+
+def check(status: int, ctx=None, what: str = ""):
+    if status != LGX_OK:
+        msg = what
+        if ctx is not None:
+            msg = (what + ": " if what else "") + load().lgx_last_error(ctx).decode()
+        raise LgxError(status, msg)
+
+
+def ptr(a, ct=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(ct))

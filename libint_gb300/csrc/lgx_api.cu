@@ -1,0 +1,1065 @@
+// C ABI of liblgx (include/lgx.h): contexts, basis and shell-pair state,
+// class programs, launch configuration and the batched / J/K passes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/lgx.h"
+#include "lgx_kernels.cuh"
+#include "lgx_program.h"
+
+namespace lgx {
+cudaError_t set_inv_odd_table();
+cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int block,
+                       size_t smem, cudaStream_t st);
+cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npairs,
+                              PrimPairRec* pp, const int* pp_pair, long long npp,
+                              double ln_prec, int method, cudaStream_t st);
+cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J,
+                               double* K, int nbf, cudaStream_t st);
+size_t stage_bytes_per_warp();
+int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
+}  // namespace lgx
+
+using namespace lgx;
+
+namespace {
+
+const char* kVersion = "lgx 0.1 (sm_103a)";
+
+struct DBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+    if (e == cudaSuccess) n = std::max<size_t>(bytes, 256);
+    return e;
+  }
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(bytes, 256));
+    if (e == cudaSuccess) n = std::max<size_t>(bytes, 256);
+    return e;
+  }
+};
+
+struct ProgDev {
+  ClassProgramHost host;
+  DevProg dev;
+  DBuf buf;
+};
+
+inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+inline int nfunc(int l, int pure) { return pure ? 2 * l + 1 : ncart(l); }
+inline long long pidx(int s1, int s2) {  // s1 >= s2
+  return (long long)s1 * (s1 + 1) / 2 + s2;
+}
+
+struct BasisDev {
+  int nshell = 0, nprim_total = 0, nbf = 0, natoms = 0;
+  std::vector<int> l, pure, nprim, prim_off, bf_off, atom;
+  std::vector<double> O, alpha, coeff;
+  DBuf ints, dbls;
+  DevBasis dev{};
+  // pairs
+  std::vector<PairRec> hpairs;
+  std::vector<unsigned char> hswap;
+  long long npp = 0;
+  DBuf pairs, pprims, pp_pair, pair_swap;
+  bool pairs_ok = false;
+  double pairs_lnprec = 0;
+  int pairs_method = -1;
+  // Schwarz
+  std::vector<double> Kpair;  // per pair index
+  bool schwarz_ok = false;
+};
+
+struct BinHost {
+  int cls;  // class index
+  int la, lb, lc, ld;
+  int bra_class, ket_class;
+  long long total[2];   // [0] FP64 space, [1] FP32 space
+  long long integrals[2];
+  DBuf row_start[2], row_j0[2];
+  int nbra;
+};
+
+struct BinCache {
+  bool valid = false;
+  double thresh = -1, mixed = -1;
+  int mode = -1;
+  DBuf class_lists;                 // pair ids of every pair class, sorted
+  std::vector<long long> class_off; // offsets of each class in class_lists
+  std::vector<std::unique_ptr<BinHost>> bins;
+  long long quartets[2] = {0, 0};
+};
+
+}  // namespace
+
+struct lgx_context {
+  int device = 0;
+  int nsm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  DBuf boys, sph;
+  std::map<int, std::unique_ptr<ProgDev>> progs;
+  BasisDev basis, small;
+  DBuf gscratch, counter, errflag, primcount;
+  DBuf items, out, isnull;
+  DBuf Jacc, Kacc, Dd, Jd, Kd, gJ, gK;
+  PinnedBuf pin_in, pin_out;
+  BinCache bins;
+  std::mutex mu;
+};
+
+namespace {
+
+lgx_status fail(lgx_context* c, lgx_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+#define CK(expr)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (expr);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return fail(ctx, LGX_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------- host constants
+// Boys table: F_m(k/32), m < kBoysCols, from the Maclaurin series (top m)
+// and downward recursion in long double.
+std::vector<double> make_boys_table() {
+  std::vector<double> t(size_t(kBoysRows) * kBoysCols);
+  for (int k = 0; k < kBoysRows; ++k) {
+    const long double T = (long double)k * kBoysDT;
+    const int M = kBoysCols - 1;
+    long double term = 1.0L / (2 * M + 1), sum = term;
+    for (int i = 1; i < 4000; ++i) {
+      term *= 2 * T / (2 * M + 2 * i + 1);
+      sum += term;
+      if (term < sum * 1e-22L) break;
+    }
+    const long double eT = expl(-T);
+    long double f = eT * sum;
+    t[size_t(k) * kBoysCols + M] = (double)f;
+    for (int m = M - 1; m >= 0; --m) {
+      f = (2 * T * f + eT) / (2 * m + 1);
+      t[size_t(k) * kBoysCols + m] = (double)f;
+    }
+  }
+  return t;
+}
+
+double fac(int n) {
+  double r = 1;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+double dfac(int n) {
+  double r = 1;
+  for (int i = n; i > 1; i -= 2) r *= i;
+  return r;
+}
+double binom(int n, int k) { return (k < 0 || k > n) ? 0.0 : fac(n) / (fac(k) * fac(n - k)); }
+int par(int k) { return (k % 2) ? -1 : 1; }
+
+// Real solid harmonics in Cartesian Gaussians sharing the x^l normalization
+// (Schlegel & Frisch, IJQC 54, 83 (1995), eq. 15; the coefficient set of
+// SolidHarmonicsCoefficients::coeff, solidharmonics.h:114-174).
+double solid_coeff(int l, int m, int lx, int ly, int lz) {
+  const int am = std::abs(m);
+  if ((lx + ly - am) % 2) return 0.0;
+  const int j = (lx + ly - am) / 2;
+  if (j < 0) return 0.0;
+  const int i = am - lx;
+  if ((m >= 0) != (std::abs(i) % 2 == 0)) return 0.0;
+  double pf = std::sqrt(fac(2 * lx) * fac(2 * ly) * fac(2 * lz) / fac(2 * l) * fac(l - am) /
+                        fac(l) / fac(l + am) / (fac(lx) * fac(ly) * fac(lz)));
+  pf /= double(1 << l);
+  pf *= (m < 0) ? par((i - 1) / 2) : par(i / 2);
+  double sum = 0;
+  for (int ii = j; ii <= (l - am) / 2; ++ii) {
+    const double t = binom(l, ii) * binom(ii, j) * par(ii) * fac(2 * (l - ii)) /
+                     fac(l - am - 2 * ii);
+    double s1 = 0;
+    for (int k = 0; k <= std::min(j, lx / 2); ++k)
+      if (lx - 2 * k <= am) s1 += binom(j, k) * binom(am, lx - 2 * k) * par(k);
+    sum += t * s1;
+  }
+  sum *= std::sqrt(dfac(2 * l - 1) / (dfac(2 * lx - 1) * dfac(2 * ly - 1) * dfac(2 * lz - 1)));
+  return m == 0 ? pf * sum : M_SQRT2 * pf * sum;
+}
+
+std::vector<double> make_sph_table() {
+  std::vector<double> t(110, 0.0);
+  for (int l = 0; l <= 3; ++l) {
+    const int nc = ncart(l);
+    for (int p = 0; p < 2 * l + 1; ++p) {
+      int c = 0;
+      for (int lx = l; lx >= 0; --lx)
+        for (int ly = l - lx; ly >= 0; --ly, ++c)
+          t[sph_off(l) + p * nc + c] = solid_coeff(l, p - l, lx, ly, l - lx - ly);
+    }
+  }
+  return t;
+}
+
+// ------------------------------------------------------------ programs
+lgx_status get_prog(lgx_context* ctx, int la, int lb, int lc, int ld, int deriv,
+                    ProgDev** out) {
+  const int ci = class_index(la, lb, lc, ld);
+  if (ci < 0) return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "angular momentum beyond LGX_MAX_L");
+  const int key = ci * 2 + deriv;
+  auto it = ctx->progs.find(key);
+  if (it != ctx->progs.end()) {
+    *out = it->second.get();
+    return LGX_OK;
+  }
+  auto pd = std::make_unique<ProgDev>();
+  try {
+    pd->host = build_class_program(la, lb, lc, ld, deriv);
+  } catch (const std::exception& e) {
+    return fail(ctx, LGX_ERR_INVALID_ARG, e.what());
+  }
+  const auto& H = pd->host;
+  // layout: [ints: vrr_lev, acc_lev, post_lev, phase_lev] [pad16] [vrr_ops] [acc_ops] [pad16] [post_ops]
+  std::vector<uint32_t> blob;
+  auto pad16 = [&]() {
+    while (blob.size() % 4) blob.push_back(0);
+  };
+  const size_t o_vlev = blob.size();
+  for (int v : H.vrr_lev) blob.push_back(uint32_t(v));
+  const size_t o_alev = blob.size();
+  for (int v : H.acc_lev) blob.push_back(uint32_t(v));
+  const size_t o_plev = blob.size();
+  for (int v : H.post_lev) blob.push_back(uint32_t(v));
+  const size_t o_phlev = blob.size();
+  for (int v : H.phase_lev) blob.push_back(uint32_t(v));
+  pad16();
+  const size_t o_vops = blob.size();
+  blob.insert(blob.end(), H.vrr_ops.begin(), H.vrr_ops.end());
+  pad16();
+  const size_t o_aops = blob.size();
+  blob.insert(blob.end(), H.acc_ops.begin(), H.acc_ops.end());
+  pad16();
+  const size_t o_pops = blob.size();
+  blob.insert(blob.end(), H.post_ops.begin(), H.post_ops.end());
+  pad16();
+  CK(pd->buf.ensure(blob.size() * 4));
+  CK(cudaMemcpyAsync(pd->buf.p, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const uint32_t* base = pd->buf.as<uint32_t>();
+  DevProg& D = pd->dev;
+  D.la = la; D.lb = lb; D.lc = lc; D.ld = ld; D.deriv = deriv; D.mmax = H.mmax;
+  D.nacc = H.nacc; D.nwork = H.nwork; D.leaf_slot0 = H.leaf_slot0;
+  D.nphases = H.nphases; D.sets_per_phase = H.sets_per_phase; D.ncart4 = H.ncart4;
+  D.cart_out = H.cart_out; D.cbuf = H.cbuf; D.sph_tmp = H.sph_tmp;
+  D.nlev = int(H.vrr_lev.size()) - 1;
+  D.npost_lev = int(H.post_lev.size()) - 1;
+  D.vrr_lev = reinterpret_cast<const int*>(base + o_vlev);
+  D.acc_lev = reinterpret_cast<const int*>(base + o_alev);
+  D.post_lev = reinterpret_cast<const int*>(base + o_plev);
+  D.phase_lev = reinterpret_cast<const int*>(base + o_phlev);
+  D.vrr_ops = reinterpret_cast<const uint4*>(base + o_vops);
+  D.acc_ops = reinterpret_cast<const uint2*>(base + o_aops);
+  D.post_ops = reinterpret_cast<const uint4*>(base + o_pops);
+  *out = pd.get();
+  ctx->progs.emplace(key, std::move(pd));
+  return LGX_OK;
+}
+
+// ---------------------------------------------------------------- basis
+lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t* l,
+                        const int32_t* pure, const int32_t* nprim, const int32_t* atom,
+                        const double* origins, const double* alpha, const double* coeff) {
+  if (nshell <= 0 || !l || !pure || !nprim || !origins || !alpha || !coeff)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "lgx_set_basis: null array or empty basis");
+  B.nshell = nshell;
+  B.l.assign(l, l + nshell);
+  B.pure.assign(pure, pure + nshell);
+  B.nprim.assign(nprim, nprim + nshell);
+  B.atom.assign(nshell, 0);
+  if (atom) B.atom.assign(atom, atom + nshell);
+  B.prim_off.resize(nshell);
+  B.bf_off.resize(nshell);
+  int np = 0, nbf = 0, natoms = 0;
+  for (int s = 0; s < nshell; ++s) {
+    if (l[s] < 0 || l[s] > kMaxL)
+      return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "shell angular momentum exceeds LGX_MAX_L");
+    if (nprim[s] <= 0 || nprim[s] > kMaxNprim)
+      return fail(ctx, LGX_ERR_TOO_LARGE, "shell contraction depth exceeds LGX_MAX_NPRIM");
+    if (B.atom[s] < 0) return fail(ctx, LGX_ERR_INVALID_ARG, "negative atom index");
+    B.prim_off[s] = np;
+    B.bf_off[s] = nbf;
+    np += nprim[s];
+    nbf += nfunc(l[s], pure[s]);
+    natoms = std::max(natoms, B.atom[s] + 1);
+  }
+  B.nprim_total = np;
+  B.nbf = nbf;
+  B.natoms = natoms;
+  B.O.assign(origins, origins + 3 * nshell);
+  B.alpha.assign(alpha, alpha + np);
+  B.coeff.assign(coeff, coeff + np);
+  // device copies: ints [l|pure|nprim|prim_off|bf_off|atom], doubles [O|alpha|coeff]
+  std::vector<int> hi;
+  hi.reserve(6 * nshell);
+  for (auto* v : {&B.l, &B.pure, &B.nprim, &B.prim_off, &B.bf_off, &B.atom})
+    hi.insert(hi.end(), v->begin(), v->end());
+  std::vector<double> hd;
+  hd.reserve(3 * nshell + 2 * np);
+  hd.insert(hd.end(), B.O.begin(), B.O.end());
+  hd.insert(hd.end(), B.alpha.begin(), B.alpha.end());
+  hd.insert(hd.end(), B.coeff.begin(), B.coeff.end());
+  CK(B.ints.ensure(hi.size() * sizeof(int)));
+  CK(B.dbls.ensure(hd.size() * sizeof(double)));
+  CK(cudaMemcpyAsync(B.ints.p, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(B.dbls.p, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  const int* ib = B.ints.as<int>();
+  const double* db = B.dbls.as<double>();
+  B.dev.nshell = nshell;
+  B.dev.l = ib;
+  B.dev.pure = ib + nshell;
+  B.dev.nprim = ib + 2 * nshell;
+  B.dev.prim_off = ib + 3 * nshell;
+  B.dev.bf_off = ib + 4 * nshell;
+  B.dev.atom = ib + 5 * nshell;
+  B.dev.O = db;
+  B.dev.alpha = db + 3 * nshell;
+  B.dev.coeff = db + 3 * nshell + np;
+  B.pairs_ok = false;
+  B.schwarz_ok = false;
+  // pair table layout (all s1 >= s2)
+  const long long npairs = (long long)nshell * (nshell + 1) / 2;
+  B.hpairs.resize(npairs);
+  B.hswap.resize(npairs);
+  long long off = 0;
+  for (int s1 = 0; s1 < nshell; ++s1)
+    for (int s2 = 0; s2 <= s1; ++s2) {
+      PairRec& r = B.hpairs[pidx(s1, s2)];
+      r.s1 = s1;
+      r.s2 = s2;
+      r.pp_off = int(off);
+      r.npp = nprim[s1] * nprim[s2];
+      off += r.npp;
+      B.hswap[pidx(s1, s2)] = (l[s2] > l[s1]) ? 1 : 0;
+    }
+  if (off > std::numeric_limits<int>::max())
+    return fail(ctx, LGX_ERR_TOO_LARGE, "too many primitive pairs");
+  B.npp = off;
+  std::vector<int> ppp(off);
+  for (long long p = 0; p < npairs; ++p)
+    for (int k = 0; k < B.hpairs[p].npp; ++k) ppp[B.hpairs[p].pp_off + k] = int(p);
+  CK(B.pairs.ensure(npairs * sizeof(PairRec)));
+  CK(B.pp_pair.ensure(off * sizeof(int)));
+  CK(B.pprims.ensure(off * sizeof(PrimPairRec)));
+  CK(B.pair_swap.ensure(npairs));
+  CK(cudaMemcpyAsync(B.pairs.p, B.hpairs.data(), npairs * sizeof(PairRec),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(B.pp_pair.p, ppp.data(), off * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(B.pair_swap.p, B.hswap.data(), npairs, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status ensure_pairs(lgx_context* ctx, BasisDev& B, double ln_prec, int method) {
+  if (B.pairs_ok && B.pairs_lnprec == ln_prec && B.pairs_method == method) return LGX_OK;
+  CK(launch_shellpairs(B.dev, B.pairs.as<PairRec>(), int(B.hpairs.size()),
+                       B.pprims.as<PrimPairRec>(), B.pp_pair.as<int>(), B.npp, ln_prec,
+                       method, ctx->stream));
+  B.pairs_ok = true;
+  B.pairs_lnprec = ln_prec;
+  B.pairs_method = method;
+  return LGX_OK;
+}
+
+// ------------------------------------------------------ launch helpers
+struct Launch {
+  int grid, block, wpb, stride;
+  size_t smem;
+  bool global;
+};
+
+lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
+                       long long nwork, Launch& L) {
+  const size_t elt = fp32 ? 4 : 8;
+  L.block = 128;
+  L.wpb = 4;
+  L.stride = (P.host.total_slots() + 1) & ~1;
+  const size_t slot_bytes = size_t(L.stride) * elt;
+  const size_t stage = stage_bytes_per_warp();
+  const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
+  L.global = slot_bytes > 40 * 1024 || L.wpb * (stage + slot_bytes) > smem_cap;
+  L.smem = L.wpb * (stage + (L.global ? 0 : slot_bytes));
+  int bps = eri_blocks_per_sm(mode, fp32, L.block, L.smem);
+  if (bps < 1) bps = 1;
+  long long grid = (long long)ctx->nsm * bps;
+  const long long need = (nwork + L.wpb - 1) / L.wpb;
+  grid = std::max<long long>(1, std::min(grid, need));
+  if (L.global) {
+    const size_t per_block = size_t(L.wpb) * slot_bytes;
+    const size_t cap = size_t(2) << 30;  // 2 GiB of per-warp slot scratch at most
+    grid = std::min<long long>(grid, std::max<size_t>(1, cap / per_block));
+    CK(ctx->gscratch.ensure(size_t(grid) * per_block));
+  }
+  L.grid = int(grid);
+  return LGX_OK;
+}
+
+lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
+                   EriArgs a, long long nwork) {
+  Launch L;
+  lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, L);
+  if (s != LGX_OK) return s;
+  a.basis = B.dev;
+  a.pairs = B.pairs.as<PairRec>();
+  a.pprims = B.pprims.as<PrimPairRec>();
+  a.pair_swap = B.pair_swap.as<unsigned char>();
+  a.prog = P.dev;
+  a.boys = ctx->boys.as<double>();
+  a.sph = ctx->sph.as<double>();
+  a.counter = ctx->counter.as<unsigned long long>();
+  a.error_flag = ctx->errflag.as<int>();
+  a.slot_stride = L.stride;
+  a.global_slots = L.global ? 1 : 0;
+  a.gscratch = ctx->gscratch.p;
+  const long long nwarps = (long long)L.grid * L.wpb;
+  a.chunk = int(std::max<long long>(1, std::min<long long>(32, nwork / (nwarps * 8))));
+  a.max_chunks = nwork / a.chunk + 2;
+  CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream));
+  CK(launch_eri(a, mode, fp32, L.grid, L.block, L.smem, ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status check_errflag(lgx_context* ctx) {
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, ctx->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (flag) {
+    CK(cudaMemsetAsync(ctx->errflag.p, 0, sizeof(int), ctx->stream));
+    return fail(ctx, LGX_ERR_WATCHDOG, "device work loop exceeded its bound");
+  }
+  return LGX_OK;
+}
+
+// Canonical quartet (engine.impl.h:1181-1211) -> work item.
+struct Canon {
+  int c[4];  // canonical shells
+  int flags;
+  int la, lb, lc, ld;
+};
+Canon canonicalize(const BasisDev& B, const int* s) {
+  const int l0 = B.l[s[0]], l1 = B.l[s[1]], l2 = B.l[s[2]], l3 = B.l[s[3]];
+  const bool stb = l0 < l1, stk = l2 < l3, sbk = l0 + l1 > l2 + l3;
+  int perm[4];
+  perm[0] = sbk ? (stk ? 3 : 2) : (stb ? 1 : 0);
+  perm[1] = sbk ? (stk ? 2 : 3) : (stb ? 0 : 1);
+  perm[2] = sbk ? (stb ? 1 : 0) : (stk ? 3 : 2);
+  perm[3] = sbk ? (stb ? 0 : 1) : (stk ? 2 : 3);
+  Canon q;
+  for (int k = 0; k < 4; ++k) q.c[k] = s[perm[k]];
+  const bool bsw = q.c[0] < q.c[1];  // stored pair has s1 >= s2
+  const bool ksw = q.c[2] < q.c[3];
+  q.flags = (bsw ? 1 : 0) | (ksw ? 2 : 0) |
+            ((sbk ? 1 : 0) | (stb ? 2 : 0) | (stk ? 4 : 0)) << 2;
+  q.la = B.l[q.c[0]];
+  q.lb = B.l[q.c[1]];
+  q.lc = B.l[q.c[2]];
+  q.ld = B.l[q.c[3]];
+  return q;
+}
+
+// Explicit quartet list -> grouped launches (store mode).
+lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, long long n,
+                        int deriv, int mode, double mixed_thresh, const int64_t* offsets,
+                        double* d_out, int* d_isnull, double precision, int screening,
+                        double* d_kschwarz) {
+  struct G {
+    std::vector<QuartetItem> items;
+    int la, lb, lc, ld;
+    bool fp32;
+  };
+  std::map<int, G> groups;
+  long long run_off = 0;
+  for (long long q = 0; q < n; ++q) {
+    const int* s = quartets + 4 * q;
+    for (int k = 0; k < 4; ++k)
+      if (s[k] < 0 || s[k] >= B.nshell)
+        return fail(ctx, LGX_ERR_INVALID_ARG, "quartet shell index out of range");
+    const Canon c = canonicalize(B, s);
+    QuartetItem it;
+    it.bra_pair = int(pidx(std::max(c.c[0], c.c[1]), std::min(c.c[0], c.c[1])));
+    it.ket_pair = int(pidx(std::max(c.c[2], c.c[3]), std::min(c.c[2], c.c[3])));
+    it.flags = c.flags;
+    it.pad = int(q);
+    long long nv = 1;
+    for (int k = 0; k < 4; ++k) nv *= nfunc(B.l[s[k]], B.pure[s[k]]);
+    const long long nsets = deriv ? 12 : 1;
+    if (mode == kModeSchwarz) {
+      it.out = offsets ? offsets[q] : q;
+    } else {
+      it.out = offsets ? offsets[q] : run_off;
+      run_off += nv * nsets;
+    }
+    bool fp32 = false;
+    if (mode == kModeStore && mixed_thresh > 0 && B.schwarz_ok) {
+      const double bound = B.Kpair[it.bra_pair] * B.Kpair[it.ket_pair];
+      fp32 = bound < mixed_thresh;
+    }
+    const int key = class_index(c.la, c.lb, c.lc, c.ld) * 2 + (fp32 ? 1 : 0);
+    G& g = groups[key];
+    g.la = c.la; g.lb = c.lb; g.lc = c.lc; g.ld = c.ld; g.fp32 = fp32;
+    g.items.push_back(it);
+  }
+  size_t total = 0;
+  for (auto& kv : groups) total += kv.second.items.size();
+  CK(ctx->items.ensure(total * sizeof(QuartetItem)));
+  std::vector<QuartetItem> all;
+  all.reserve(total);
+  std::vector<std::pair<size_t, size_t>> ranges;
+  for (auto& kv : groups) {
+    ranges.push_back({all.size(), kv.second.items.size()});
+    all.insert(all.end(), kv.second.items.begin(), kv.second.items.end());
+  }
+  CK(cudaMemcpyAsync(ctx->items.p, all.data(), total * sizeof(QuartetItem),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  size_t gi = 0;
+  for (auto& kv : groups) {
+    ProgDev* P = nullptr;
+    lgx_status s = get_prog(ctx, kv.second.la, kv.second.lb, kv.second.lc, kv.second.ld,
+                            deriv, &P);
+    if (s != LGX_OK) return s;
+    EriArgs a{};
+    a.precision = precision;
+    a.ln_prec = precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
+    a.screening = screening;
+    a.items = ctx->items.as<QuartetItem>() + ranges[gi].first;
+    a.nitems = (long long)ranges[gi].second;
+    a.implicit = 0;
+    a.out = d_out;
+    a.is_null = d_isnull;
+    a.kschwarz = d_kschwarz;
+    s = run_eri(ctx, B, *P, mode, kv.second.fp32, a, a.nitems);
+    if (s != LGX_OK) return s;
+    ++gi;
+  }
+  return LGX_OK;
+}
+
+lgx_status ensure_schwarz(lgx_context* ctx, BasisDev& B) {
+  if (B.schwarz_ok) return LGX_OK;
+  lgx_status s = ensure_pairs(ctx, B, -std::numeric_limits<double>::max(), 0);
+  if (s != LGX_OK) return s;
+  const long long npairs = (long long)B.hpairs.size();
+  std::vector<int32_t> q(4 * npairs);
+  for (long long p = 0; p < npairs; ++p) {
+    q[4 * p] = B.hpairs[p].s1;
+    q[4 * p + 1] = B.hpairs[p].s2;
+    q[4 * p + 2] = B.hpairs[p].s1;
+    q[4 * p + 3] = B.hpairs[p].s2;
+  }
+  DBuf dK;
+  CK(dK.ensure(npairs * sizeof(double)));
+  s = run_explicit(ctx, B, q.data(), npairs, 0, kModeSchwarz, 0.0, nullptr, nullptr, nullptr,
+                   0.0, 0, dK.as<double>());
+  if (s != LGX_OK) return s;
+  B.Kpair.resize(npairs);
+  CK(cudaMemcpyAsync(B.Kpair.data(), dK.p, npairs * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  s = check_errflag(ctx);
+  if (s != LGX_OK) return s;
+  B.schwarz_ok = true;
+  // the J/K passes use libint's default primitive screening (precision eps)
+  return LGX_OK;
+}
+
+// ------------------------------------------------------------ J/K bins
+int pair_class(int lhi, int llo) { return lhi * (lhi + 1) / 2 + llo; }  // 10 classes
+
+lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, double mixed) {
+  BinCache& C = ctx->bins;
+  if (C.valid && C.thresh == thresh && C.mode == mode && C.mixed == mixed) return LGX_OK;
+  C.valid = false;
+  C.bins.clear();
+  const long long npairs = (long long)B.hpairs.size();
+  double Kmax = 0;
+  for (double k : B.Kpair) Kmax = std::max(Kmax, k);
+  std::vector<std::vector<int>> lists(10);
+  for (long long p = 0; p < npairs; ++p) {
+    if (B.Kpair[p] * Kmax < thresh) continue;
+    const int s1 = B.hpairs[p].s1, s2 = B.hpairs[p].s2;
+    const int lhi = std::max(B.l[s1], B.l[s2]), llo = std::min(B.l[s1], B.l[s2]);
+    lists[pair_class(lhi, llo)].push_back(int(p));
+  }
+  for (auto& v : lists)
+    std::stable_sort(v.begin(), v.end(),
+                     [&](int a, int b) { return B.Kpair[a] > B.Kpair[b]; });
+  C.class_off.assign(11, 0);
+  std::vector<int> flat;
+  for (int c = 0; c < 10; ++c) {
+    C.class_off[c] = (long long)flat.size();
+    flat.insert(flat.end(), lists[c].begin(), lists[c].end());
+  }
+  C.class_off[10] = (long long)flat.size();
+  CK(C.class_lists.ensure(std::max<size_t>(1, flat.size()) * sizeof(int)));
+  if (!flat.empty())
+    CK(cudaMemcpyAsync(C.class_lists.p, flat.data(), flat.size() * sizeof(int),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  int cls_l[10][2];
+  for (int lhi = 0; lhi <= 3; ++lhi)
+    for (int llo = 0; llo <= lhi; ++llo) {
+      cls_l[pair_class(lhi, llo)][0] = lhi;
+      cls_l[pair_class(lhi, llo)][1] = llo;
+    }
+  C.quartets[0] = C.quartets[1] = 0;
+  for (int x = 0; x < 10; ++x)
+    for (int y = 0; y < 10; ++y) {
+      const int Lx = cls_l[x][0] + cls_l[x][1], Ly = cls_l[y][0] + cls_l[y][1];
+      if (!(Lx < Ly || (Lx == Ly && x <= y))) continue;
+      const auto& bra = lists[x];
+      const auto& ket = lists[y];
+      if (bra.empty() || ket.empty()) continue;
+      auto bin = std::make_unique<BinHost>();
+      bin->la = cls_l[x][0]; bin->lb = cls_l[x][1];
+      bin->lc = cls_l[y][0]; bin->ld = cls_l[y][1];
+      bin->bra_class = x;
+      bin->ket_class = y;
+      bin->nbra = int(bra.size());
+      std::vector<long long> rs[2];
+      std::vector<int> j0[2];
+      for (int sp = 0; sp < 2; ++sp) {
+        rs[sp].assign(bra.size() + 1, 0);
+        j0[sp].assign(bra.size(), 0);
+      }
+      // number of kets j (sorted desc) with K_i*K_j >= t
+      auto count_ge = [&](double Ki, double t) -> long long {
+        if (Ki <= 0) return 0;
+        const double need = t / Ki;
+        long long lo = 0, hi = (long long)ket.size();
+        while (lo < hi) {
+          const long long mid = (lo + hi) / 2;
+          if (B.Kpair[ket[mid]] >= need) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+      };
+      for (size_t i = 0; i < bra.size(); ++i) {
+        const double Ki = B.Kpair[bra[i]];
+        long long n = count_ge(Ki, thresh);
+        if (x == y) n = std::min<long long>(n, (long long)i + 1);
+        long long m = n;
+        if (mode == LGX_MIXED) m = std::min(n, count_ge(Ki, mixed));
+        rs[0][i + 1] = rs[0][i] + m;
+        rs[1][i + 1] = rs[1][i] + (n - m);
+        j0[0][i] = 0;
+        j0[1][i] = int(m);
+      }
+      auto nf_pair = [&](int p) {
+        return (long long)nfunc(B.l[B.hpairs[p].s1], B.pure[B.hpairs[p].s1]) *
+               nfunc(B.l[B.hpairs[p].s2], B.pure[B.hpairs[p].s2]);
+      };
+      const long long nfq = nf_pair(bra[0]) * nf_pair(ket[0]);
+      for (int sp = 0; sp < 2; ++sp) {
+        bin->total[sp] = rs[sp].back();
+        bin->integrals[sp] = bin->total[sp] * nfq;
+        C.quartets[sp] += bin->total[sp];
+        CK(bin->row_start[sp].ensure(rs[sp].size() * sizeof(long long)));
+        CK(bin->row_j0[sp].ensure(j0[sp].size() * sizeof(int)));
+        CK(cudaMemcpyAsync(bin->row_start[sp].p, rs[sp].data(), rs[sp].size() * sizeof(long long),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(bin->row_j0[sp].p, j0[sp].data(), j0[sp].size() * sizeof(int),
+                           cudaMemcpyHostToDevice, ctx->stream));
+      }
+      C.bins.push_back(std::move(bin));
+    }
+  CK(cudaStreamSynchronize(ctx->stream));
+  C.valid = true;
+  C.thresh = thresh;
+  C.mode = mode;
+  C.mixed = mixed;
+  return LGX_OK;
+}
+
+lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
+                    EriArgs base, lgx_jk_stats* stats) {
+  BinCache& C = ctx->bins;
+  CK(cudaMemsetAsync(ctx->primcount.p, 0, sizeof(unsigned long long), ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  long long integrals = 0;
+  for (auto& bp : C.bins) {
+    BinHost& bin = *bp;
+    ProgDev* P = nullptr;
+    lgx_status s = get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
+    if (s != LGX_OK) return s;
+    for (int sp = 0; sp < 2; ++sp) {
+      if (bin.total[sp] == 0) continue;
+      const bool fp32 = (sp == 1) && allow_fp32;
+      EriArgs a = base;
+      a.implicit = 1;
+      a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
+      a.bin.ket_pairs = C.class_lists.as<int>() + C.class_off[bin.ket_class];
+      a.bin.row_start = bin.row_start[sp].as<long long>();
+      a.bin.row_j0 = bin.row_j0[sp].as<int>();
+      a.bin.nbra = bin.nbra;
+      a.bin.total = bin.total[sp];
+      a.prim_count = ctx->primcount.as<unsigned long long>();
+      s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp]);
+      if (s != LGX_OK) return s;
+      integrals += bin.integrals[sp];
+    }
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (stats) {
+    CK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    unsigned long long pc = 0;
+    CK(cudaMemcpy(&pc, ctx->primcount.p, sizeof(pc), cudaMemcpyDeviceToHost));
+    stats->quartets_fp64 = C.quartets[0] + (allow_fp32 ? 0 : C.quartets[1]);
+    stats->quartets_fp32 = allow_fp32 ? C.quartets[1] : 0;
+    stats->integrals = integrals;
+    stats->prim_quartets = (int64_t)pc;
+    stats->kernel_ms = ms;
+  }
+  return LGX_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+const char* lgx_version(void) { return kVersion; }
+
+const char* lgx_last_error(const lgx_context* ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+lgx_status lgx_create(lgx_context** out, int device) {
+  if (!out) return LGX_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev)
+    return LGX_ERR_NO_DEVICE;
+  auto ctx = std::make_unique<lgx_context>();
+  lgx_context* c = ctx.get();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) return LGX_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return LGX_ERR_NO_DEVICE;
+  if (prop.major < 10) return LGX_ERR_NO_DEVICE;
+  ctx->nsm = prop.multiProcessorCount;
+  ctx->smem_optin = prop.sharedMemPerBlockOptin;
+  {
+    lgx_context* ctx = c;  // for CK
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    const auto boys = make_boys_table();
+    CK(c->boys.ensure(boys.size() * sizeof(double)));
+    CK(cudaMemcpy(c->boys.p, boys.data(), boys.size() * sizeof(double), cudaMemcpyHostToDevice));
+    const auto sph = make_sph_table();
+    CK(c->sph.ensure(sph.size() * sizeof(double)));
+    CK(cudaMemcpy(c->sph.p, sph.data(), sph.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(set_inv_odd_table());
+    CK(c->counter.ensure(64));
+    CK(c->errflag.ensure(64));
+    CK(c->primcount.ensure(64));
+    CK(cudaMemset(c->errflag.p, 0, 64));
+  }
+  *out = ctx.release();
+  return LGX_OK;
+}
+
+lgx_status lgx_destroy(lgx_context* ctx) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  cudaStream_t st = ctx->stream;
+  delete ctx;
+  if (st) cudaStreamDestroy(st);
+  return LGX_OK;
+}
+
+lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int deriv,
+                                double precision, int screening, double* out,
+                                size_t out_capacity, int* nsets, int* nvalues, int* is_null) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!shells || !out || !nsets || !nvalues || !is_null)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (deriv < 0 || deriv > kMaxDeriv)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "deriv must be 0 or 1");
+  if (screening != LGX_SCREEN_ORIGINAL && screening != LGX_SCREEN_CONSERVATIVE)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "unsupported screening method");
+  CK(cudaSetDevice(ctx->device));
+  int l[4], pure[4], np[4], atom[4] = {0, 1, 2, 3};
+  double O[12];
+  std::vector<double> al, co;
+  long long nv = 1;
+  for (int k = 0; k < 4; ++k) {
+    const lgx_shell& s = shells[k];
+    if (!s.alpha || !s.coeff) return fail(ctx, LGX_ERR_INVALID_ARG, "null shell data");
+    l[k] = s.l;
+    pure[k] = s.pure ? 1 : 0;
+    np[k] = s.nprim;
+    for (int x = 0; x < 3; ++x) O[3 * k + x] = s.origin[x];
+    al.insert(al.end(), s.alpha, s.alpha + s.nprim);
+    co.insert(co.end(), s.coeff, s.coeff + s.nprim);
+    if (s.l < 0 || s.l > kMaxL)
+      return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "shell angular momentum exceeds LGX_MAX_L");
+    nv *= nfunc(s.l, pure[k]);
+  }
+  const int ns = deriv ? 12 : 1;
+  if (size_t(nv * ns) > out_capacity)
+    return fail(ctx, LGX_ERR_TOO_LARGE, "output buffer too small");
+  lgx_status s = upload_basis(ctx, ctx->small, 4, l, pure, np, atom, O, al.data(), co.data());
+  if (s != LGX_OK) return s;
+  const double ln_prec =
+      precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
+  s = ensure_pairs(ctx, ctx->small, ln_prec, screening);
+  if (s != LGX_OK) return s;
+  CK(ctx->out.ensure(size_t(nv * ns) * sizeof(double)));
+  CK(ctx->isnull.ensure(sizeof(int)));
+  const int32_t q[4] = {0, 1, 2, 3};
+  s = run_explicit(ctx, ctx->small, q, 1, deriv, kModeStore, 0.0, nullptr, ctx->out.as<double>(),
+                   ctx->isnull.as<int>(), precision, screening, nullptr);
+  if (s != LGX_OK) return s;
+  int nul = 0;
+  CK(cudaMemcpyAsync(&nul, ctx->isnull.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(out, ctx->out.p, size_t(nv * ns) * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  s = check_errflag(ctx);
+  if (s != LGX_OK) return s;
+  *nsets = ns;
+  *nvalues = int(nv);
+  *is_null = nul;
+  return LGX_OK;
+}
+
+lgx_status lgx_set_basis(lgx_context* ctx, int nshell, const int32_t* l, const int32_t* pure,
+                         const int32_t* nprim, const int32_t* atom, const double* origins,
+                         const double* alpha, const double* coeff) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CK(cudaSetDevice(ctx->device));
+  ctx->bins.valid = false;
+  return upload_basis(ctx, ctx->basis, nshell, l, pure, nprim, atom, origins, alpha, coeff);
+}
+
+lgx_status lgx_basis_nbf(lgx_context* ctx, int* nbf) {
+  if (!ctx || !nbf) return LGX_ERR_INVALID_ARG;
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  *nbf = ctx->basis.nbf;
+  return LGX_OK;
+}
+
+lgx_status lgx_schwarz(lgx_context* ctx, double* K) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!K) return fail(ctx, LGX_ERR_INVALID_ARG, "null output");
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  CK(cudaSetDevice(ctx->device));
+  BasisDev& B = ctx->basis;
+  lgx_status s = ensure_schwarz(ctx, B);
+  if (s != LGX_OK) return s;
+  const int n = B.nshell;
+  for (int s1 = 0; s1 < n; ++s1)
+    for (int s2 = 0; s2 <= s1; ++s2)
+      K[(size_t)s1 * n + s2] = K[(size_t)s2 * n + s1] = B.Kpair[pidx(s1, s2)];
+  return LGX_OK;
+}
+
+lgx_status lgx_compute_batch(lgx_context* ctx, const int32_t* quartets, int64_t n, int deriv,
+                             int mode, double mixed_thresh, const int64_t* offsets, double* out,
+                             size_t out_capacity, int32_t* is_null) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!quartets || n < 0 || !out) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  if (deriv < 0 || deriv > kMaxDeriv) return fail(ctx, LGX_ERR_INVALID_ARG, "bad deriv");
+  if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
+  if (mode == LGX_MIXED && deriv) return fail(ctx, LGX_ERR_INVALID_ARG, "mixed mode is deriv 0");
+  CK(cudaSetDevice(ctx->device));
+  BasisDev& B = ctx->basis;
+  size_t need = 0;
+  for (int64_t q = 0; q < n; ++q) {
+    long long nv = 1;
+    for (int k = 0; k < 4; ++k) {
+      const int s = quartets[4 * q + k];
+      if (s < 0 || s >= B.nshell) return fail(ctx, LGX_ERR_INVALID_ARG, "shell index out of range");
+      nv *= nfunc(B.l[s], B.pure[s]);
+    }
+    nv *= deriv ? 12 : 1;
+    const size_t end = size_t((offsets ? offsets[q] : (int64_t)need) + nv);
+    need = offsets ? std::max(need, end) : end;
+  }
+  if (need > out_capacity) return fail(ctx, LGX_ERR_TOO_LARGE, "output buffer too small");
+  lgx_status s;
+  if (mode == LGX_MIXED) {
+    s = ensure_schwarz(ctx, B);
+    if (s != LGX_OK) return s;
+  }
+  const double eps = std::numeric_limits<double>::epsilon();
+  s = ensure_pairs(ctx, B, std::log(eps), 0);
+  if (s != LGX_OK) return s;
+  CK(ctx->out.ensure(std::max<size_t>(need, 1) * sizeof(double)));
+  CK(ctx->isnull.ensure(std::max<int64_t>(n, 1) * sizeof(int)));
+  CK(cudaMemsetAsync(ctx->out.p, 0, std::max<size_t>(need, 1) * sizeof(double), ctx->stream));
+  s = run_explicit(ctx, B, quartets, n, deriv, kModeStore,
+                   mode == LGX_MIXED ? mixed_thresh : 0.0, offsets, ctx->out.as<double>(),
+                   ctx->isnull.as<int>(), eps, 0, nullptr);
+  if (s != LGX_OK) return s;
+  CK(cudaMemcpyAsync(out, ctx->out.p, need * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  if (is_null)
+    CK(cudaMemcpyAsync(is_null, ctx->isnull.p, n * sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_errflag(ctx);
+}
+
+lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double* dK,
+                         double thresh, int mode, double mixed, lgx_jk_stats* stats) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!dD || !dJ || !dK) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
+  CK(cudaSetDevice(ctx->device));
+  BasisDev& B = ctx->basis;
+  lgx_status s = ensure_schwarz(ctx, B);
+  if (s != LGX_OK) return s;
+  s = build_bins(ctx, B, thresh, mode, mode == LGX_MIXED ? mixed : 0.0);
+  if (s != LGX_OK) return s;
+  const double eps = std::numeric_limits<double>::epsilon();
+  s = ensure_pairs(ctx, B, std::log(eps), 0);
+  if (s != LGX_OK) return s;
+  const size_t nn = size_t(B.nbf) * B.nbf;
+  CK(ctx->Jacc.ensure(nn * sizeof(double)));
+  CK(ctx->Kacc.ensure(nn * sizeof(double)));
+  CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
+  EriArgs a{};
+  a.precision = eps;
+  a.ln_prec = std::log(eps);
+  a.screening = 0;
+  a.D = dD;
+  a.Jacc = ctx->Jacc.as<double>();
+  a.Kacc = ctx->Kacc.as<double>();
+  a.nbf = B.nbf;
+  s = run_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, stats);
+  if (s != LGX_OK) return s;
+  CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
+                        ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_errflag(ctx);
+}
+
+lgx_status lgx_jk(lgx_context* ctx, const double* D, double* J, double* K, double thresh,
+                  int mode, double mixed, lgx_jk_stats* stats) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  if (!D || !J || !K) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  const size_t nn = size_t(ctx->basis.nbf) * ctx->basis.nbf;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->Dd.ensure(nn * sizeof(double)));
+    CK(ctx->Jd.ensure(nn * sizeof(double)));
+    CK(ctx->Kd.ensure(nn * sizeof(double)));
+    CK(cudaMemcpyAsync(ctx->Dd.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  lgx_status s = lgx_jk_device(ctx, ctx->Dd.as<double>(), ctx->Jd.as<double>(),
+                               ctx->Kd.as<double>(), thresh, mode, mixed, stats);
+  if (s != LGX_OK) return s;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CK(cudaMemcpyAsync(J, ctx->Jd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(K, ctx->Kd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_jk_grad(lgx_context* ctx, const double* D, double* gJ, double* gK, int natoms,
+                       double thresh, lgx_jk_stats* stats) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!D || !gJ || !gK) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  BasisDev& B = ctx->basis;
+  if (natoms < B.natoms) return fail(ctx, LGX_ERR_INVALID_ARG, "natoms smaller than atom count");
+  CK(cudaSetDevice(ctx->device));
+  lgx_status s = ensure_schwarz(ctx, B);
+  if (s != LGX_OK) return s;
+  s = build_bins(ctx, B, thresh, LGX_FP64, 0.0);
+  if (s != LGX_OK) return s;
+  const double eps = std::numeric_limits<double>::epsilon();
+  s = ensure_pairs(ctx, B, std::log(eps), 0);
+  if (s != LGX_OK) return s;
+  const size_t nn = size_t(B.nbf) * B.nbf;
+  CK(ctx->Dd.ensure(nn * sizeof(double)));
+  CK(ctx->gJ.ensure(3 * natoms * sizeof(double)));
+  CK(ctx->gK.ensure(3 * natoms * sizeof(double)));
+  CK(cudaMemcpyAsync(ctx->Dd.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->gJ.p, 0, 3 * natoms * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->gK.p, 0, 3 * natoms * sizeof(double), ctx->stream));
+  EriArgs a{};
+  a.precision = eps;
+  a.ln_prec = std::log(eps);
+  a.D = ctx->Dd.as<double>();
+  a.gJ = ctx->gJ.as<double>();
+  a.gK = ctx->gK.as<double>();
+  a.nbf = B.nbf;
+  s = run_bins(ctx, B, kModeGrad, 1, false, a, stats);
+  if (s != LGX_OK) return s;
+  CK(cudaMemcpyAsync(gJ, ctx->gJ.p, 3 * natoms * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(gK, ctx->gK.p, 3 * natoms * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_errflag(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,712 @@
+// Warp-cooperative Coulomb ERI kernel for sm_103a.
+//
+// One warp owns one contracted shell quartet at a time:
+//  1. primitive-quartet prologue, one primitive quartet per lane: libint's
+//     screening (engine.impl.h:1313-1386), pfac, T, the Boys function and
+//     the VRR geometric factors (engine.impl.h:1389-1757); survivors are
+//     compacted with a ballot into a per-warp staging area;
+//  2. for each surviving primitive quartet the 32 lanes execute the class's
+//     VRR program level by level (all ops of a level are independent) and
+//     add the (e0|f0) targets into contracted accumulators (HGP contraction
+//     point, src/bin/libint/dg.cc:1177-1189);
+//  3. the post program (HRR, derivative rule) produces Cartesian shell sets;
+//  4. a Cartesian -> solid-harmonic transform per index
+//     (engine.impl.h:1965-1985) and the mode-specific epilogue: libint-order
+//     store with un-permutation (engine.impl.h:1988-2086), Schwarz maximum,
+//     J/K digestion (hartree-fock++.cc:1709-1743) or gradient digestion
+//     (hartree-fock++.cc:1909-1973).
+// Slots live in shared memory when the class fits, else in a per-warp slice
+// of global scratch (L1/L2 resident).  Work is pulled in chunks from a
+// device counter; every loop is bounded.
+#include "lgx_kernels.cuh"
+
+namespace lgx {
+
+constexpr int kStage = 36;        // doubles staged per primitive quartet
+constexpr int kStF = 0;           // F_m * pfac, m <= 15
+constexpr int kStPA = 16, kStWP = 19, kStQC = 22, kStWQ = 25;
+constexpr int kStOo2z = 28, kStRoz = 29, kStOo2e = 30, kStRoe = 31, kStOo2ze = 32;
+constexpr int kStW = 33;          // 2 alpha_A, 2 alpha_B, 2 alpha_D
+
+__constant__ double c_inv_odd[40];  // 1/(2m+1)
+
+__device__ __forceinline__ double boys_inv_odd(int m) { return c_inv_odd[m]; }
+
+// Boys with the constant-memory reciprocal table (downward recursion).
+__device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
+                                              double T, int mmax, double pfac,
+                                              double* __restrict__ F) {
+  if (T > kBoysTmax) {
+    const double eT = exp(-T);
+    const double rT = 1.0 / T;
+    double f = 0.88622692545275801365 * sqrt(rT);
+    F[0] = f * pfac;
+    const double oo2T = 0.5 * rT;
+    for (int m = 0; m < mmax; ++m) {
+      f = ((2 * m + 1) * f - eT) * oo2T;
+      F[m + 1] = f * pfac;
+    }
+    return;
+  }
+  const int k = __double2int_rn(T * kBoysInvDT);
+  const double d = T - k * kBoysDT;
+  const double* row = tab + k * kBoysCols + mmax;
+  double s = __ldg(row + 6);
+  s = fma(s, -d * (1.0 / 6.0), __ldg(row + 5));
+  s = fma(s, -d * (1.0 / 5.0), __ldg(row + 4));
+  s = fma(s, -d * (1.0 / 4.0), __ldg(row + 3));
+  s = fma(s, -d * (1.0 / 3.0), __ldg(row + 2));
+  s = fma(s, -d * (1.0 / 2.0), __ldg(row + 1));
+  s = fma(s, -d, __ldg(row + 0));
+  F[mmax] = s * pfac;
+  if (mmax > 0) {
+    const double eT = exp(-T);
+    const double twoT = 2.0 * T;
+    for (int m = mmax - 1; m >= 0; --m) {
+      s = fma(twoT, s, eT) * boys_inv_odd(m);
+      F[m] = s * pfac;
+    }
+  }
+}
+
+struct QuartetGeom {
+  int sh[4];       // canonical shells bra1 bra2 ket1 ket2
+  int bra_pp, ket_pp, nbpp, nkpp;
+  bool bra_sw, ket_sw;
+  double A[3], B[3], C[3], D[3];
+};
+
+__device__ __forceinline__ void load_geom(const EriArgs& a, int bpair, int kpair,
+                                          bool bsw, bool ksw, QuartetGeom& g) {
+  const PairRec bp = a.pairs[bpair];
+  const PairRec kp = a.pairs[kpair];
+  g.sh[0] = bsw ? bp.s2 : bp.s1;
+  g.sh[1] = bsw ? bp.s1 : bp.s2;
+  g.sh[2] = ksw ? kp.s2 : kp.s1;
+  g.sh[3] = ksw ? kp.s1 : kp.s2;
+  g.bra_pp = bp.pp_off;
+  g.nbpp = bp.npp;
+  g.ket_pp = kp.pp_off;
+  g.nkpp = kp.npp;
+  g.bra_sw = bsw;
+  g.ket_sw = ksw;
+  for (int x = 0; x < 3; ++x) {
+    g.A[x] = a.basis.O[3 * g.sh[0] + x];
+    g.B[x] = a.basis.O[3 * g.sh[1] + x];
+    g.C[x] = a.basis.O[3 * g.sh[2] + x];
+    g.D[x] = a.basis.O[3 * g.sh[3] + x];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T sel3(int d, T x, T y, T z) {
+  return d == 0 ? x : (d == 1 ? y : z);
+}
+
+// Steps 1-2: contracted (e0|f0) accumulators in slots[0, nacc).  Returns the
+// number of primitive quartets that survived screening.
+template <typename T>
+__device__ int contract_quartet(const EriArgs& a, const QuartetGeom& g,
+                                T* __restrict__ slots,
+                                double* __restrict__ stage, int lane) {
+  const DevProg& P = a.prog;
+  for (int i = lane; i < P.nacc; i += 32) slots[i] = T(0);
+  const int nq = g.nbpp * g.nkpp;
+  int kept = 0;
+  const double npbraket = double(nq);
+  for (int base = 0; base < nq; base += 32) {
+    const int idx = base + lane;
+    bool keep = false;
+    double pfac = 0, T_ = 0, zeta = 0, eta = 0, P_[3], Q_[3], wA = 0, wB = 0, wD = 0;
+    if (idx < nq) {
+      const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
+      const PrimPairRec bp = a.pprims[g.bra_pp + ib];
+      const PrimPairRec kp = a.pprims[g.ket_pp + ik];
+      if (bp.ln_scr + kp.ln_scr > a.ln_prec) {
+        zeta = bp.a1 + bp.a2;
+        eta = kp.a1 + kp.a2;
+        const double gpq = zeta + eta;
+        const double oogpq = 1.0 / gpq;
+        pfac = bp.Kc * kp.Kc * sqrt(gpq) * oogpq;
+        double mag = fabs(pfac);
+        if (a.screening == 1) mag *= fmax(1.0, bp.nonsph * kp.nonsph) * npbraket;
+        keep = !(mag < a.precision);
+        for (int x = 0; x < 3; ++x) {
+          P_[x] = bp.P[x];
+          Q_[x] = kp.P[x];
+        }
+        const double PQx = P_[0] - Q_[0], PQy = P_[1] - Q_[1], PQz = P_[2] - Q_[2];
+        T_ = (PQx * PQx + PQy * PQy + PQz * PQz) * (zeta * eta * oogpq);
+        wA = 2.0 * (g.bra_sw ? bp.a2 : bp.a1);
+        wB = 2.0 * (g.bra_sw ? bp.a1 : bp.a2);
+        wD = 2.0 * (g.ket_sw ? kp.a1 : kp.a2);
+      }
+    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      const int pos = __popc(ballot & ((1u << lane) - 1u));
+      double* st = stage + pos * kStage;
+      boys_to_stage(a.boys, T_, P.mmax, pfac, st + kStF);
+      const double gpq = zeta + eta;
+      const double oogpq = 1.0 / gpq;
+      const double rho = zeta * eta * oogpq;
+      const double ooz = 1.0 / zeta, ooe = 1.0 / eta;
+      for (int x = 0; x < 3; ++x) {
+        const double W = (zeta * P_[x] + eta * Q_[x]) * oogpq;
+        st[kStPA + x] = P_[x] - g.A[x];
+        st[kStWP + x] = W - P_[x];
+        st[kStQC + x] = Q_[x] - g.C[x];
+        st[kStWQ + x] = W - Q_[x];
+      }
+      st[kStOo2z] = 0.5 * ooz;
+      st[kStRoz] = rho * ooz;
+      st[kStOo2e] = 0.5 * ooe;
+      st[kStRoe] = rho * ooe;
+      st[kStOo2ze] = 0.5 * oogpq;
+      st[kStW + 0] = wA;
+      st[kStW + 1] = wB;
+      st[kStW + 2] = wD;
+    }
+    __syncwarp();
+    const int n = __popc(ballot);
+    kept += n;
+    for (int j = 0; j < n; ++j) {
+      const double* st = stage + j * kStage;
+      const T PAx = T(st[kStPA]), PAy = T(st[kStPA + 1]), PAz = T(st[kStPA + 2]);
+      const T WPx = T(st[kStWP]), WPy = T(st[kStWP + 1]), WPz = T(st[kStWP + 2]);
+      const T QCx = T(st[kStQC]), QCy = T(st[kStQC + 1]), QCz = T(st[kStQC + 2]);
+      const T WQx = T(st[kStWQ]), WQy = T(st[kStWQ + 1]), WQz = T(st[kStWQ + 2]);
+      const T oo2z = T(st[kStOo2z]), roz = T(st[kStRoz]);
+      const T oo2e = T(st[kStOo2e]), roe = T(st[kStRoe]);
+      const T oo2ze = T(st[kStOo2ze]);
+      const T w1 = T(st[kStW]), w2 = T(st[kStW + 1]), w3 = T(st[kStW + 2]);
+      for (int m = lane; m <= P.mmax; m += 32) slots[P.leaf_slot0 + m] = T(st[kStF + m]);
+      __syncwarp();
+      for (int k = 0; k < P.nlev; ++k) {
+        if (k > 0) {
+          const int o1 = P.vrr_lev[k + 1];
+          for (int op = P.vrr_lev[k] + lane; op < o1; op += 32) {
+            const uint4 u = __ldg(P.vrr_ops + 2 * op);
+            const uint4 v = __ldg(P.vrr_ops + 2 * op + 1);
+            const unsigned fl = v.z;
+            const int dir = (fl >> 1) & 3;
+            const int n1 = (fl >> 3) & 31;
+            const int ne = (fl >> 8) & 31;
+            T c1, c2, c3, c4;
+            if ((fl & 1u) == 0) {
+              c1 = sel3(dir, PAx, PAy, PAz);
+              c2 = sel3(dir, WPx, WPy, WPz);
+              c3 = oo2z;
+              c4 = roz;
+            } else {
+              c1 = sel3(dir, QCx, QCy, QCz);
+              c2 = sel3(dir, WQx, WQy, WQz);
+              c3 = oo2e;
+              c4 = roe;
+            }
+            T val = c1 * slots[u.y];
+            val = fma(c2, slots[u.z], val);
+            if (n1) val = fma(T(n1) * c3, fma(-c4, slots[v.x], slots[u.w]), val);
+            if (ne) val = fma(T(ne) * oo2ze, slots[v.y], val);
+            slots[u.x] = val;
+          }
+          __syncwarp();
+        }
+        const int a1 = P.acc_lev[k + 1];
+        for (int op = P.acc_lev[k] + lane; op < a1; op += 32) {
+          const uint2 u = __ldg(P.acc_ops + op);
+          const unsigned src = u.y & 0x3FFFFFFFu;
+          const unsigned w = u.y >> 30;
+          const T wt = w == 0 ? T(1) : (w == 1 ? w1 : (w == 2 ? w2 : w3));
+          slots[u.x] = fma(wt, slots[src], slots[u.x]);
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+  }
+  return kept;
+}
+
+// Step 3 for one phase.
+template <typename T>
+__device__ void run_post_phase(const DevProg& P, int ph, const QuartetGeom& g,
+                               T* __restrict__ slots, int lane) {
+  const T ABx = T(g.A[0] - g.B[0]), ABy = T(g.A[1] - g.B[1]), ABz = T(g.A[2] - g.B[2]);
+  const T CDx = T(g.C[0] - g.D[0]), CDy = T(g.C[1] - g.D[1]), CDz = T(g.C[2] - g.D[2]);
+  const int l0 = P.phase_lev[ph], l1 = P.phase_lev[ph + 1];
+  for (int k = l0; k < l1; ++k) {
+    const int o1 = P.post_lev[k + 1];
+    for (int op = P.post_lev[k] + lane; op < o1; op += 32) {
+      const uint4 u = __ldg(P.post_ops + op);
+      const unsigned kind = u.w & 15u;
+      const int dir = (u.w >> 4) & 3;
+      const int n = (u.w >> 8) & 31;
+      T val;
+      if (kind == 0) {
+        val = fma(sel3(dir, ABx, ABy, ABz), slots[u.z], slots[u.y]);
+      } else if (kind == 1) {
+        val = fma(sel3(dir, CDx, CDy, CDz), slots[u.z], slots[u.y]);
+      } else if (kind == 2) {
+        val = slots[u.y];
+        if (n) val = fma(T(-n), slots[u.z], val);
+      } else {
+        val = slots[u.y];
+      }
+      slots[u.x] = val;
+    }
+    __syncwarp();
+  }
+}
+
+// Cartesian -> solid harmonics for the pure indices, ping-ponging between
+// `cart` and `tmp`.  Returns the buffer holding the result; dims updated.
+template <typename T>
+__device__ T* sph_transform(const EriArgs& a, const int* l, const int* pure,
+                            int* dims, T* cart, T* tmp, int lane) {
+  T* src = cart;
+  T* dst = tmp;
+  for (int k = 0; k < 4; ++k) {
+    if (!pure[k]) continue;
+    const int lk = l[k], np = 2 * lk + 1, nc = dims[k];
+    int outer = 1, inner = 1;
+    for (int t = 0; t < k; ++t) outer *= dims[t];
+    for (int t = k + 1; t < 4; ++t) inner *= dims[t];
+    const int total = outer * np * inner;
+    const double* coef = a.sph + sph_off(lk);
+    for (int e = lane; e < total; e += 32) {
+      const int i = e % inner;
+      const int p = (e / inner) % np;
+      const int o = e / (inner * np);
+      const double* cr = coef + p * nc;
+      const T* sp = src + (size_t)o * nc * inner + i;
+      T v = T(0);
+      for (int c = 0; c < nc; ++c) {
+        const double cc = __ldg(cr + c);
+        if (cc != 0.0) v = fma(T(cc), sp[c * inner], v);
+      }
+      dst[e] = v;
+    }
+    __syncwarp();
+    T* t = src;
+    src = dst;
+    dst = t;
+    dims[k] = np;
+  }
+  return src;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// J/K digestion of one spherical shell set V[a][b][c][d] (canonical order).
+template <typename T>
+__device__ void digest_jk(const EriArgs& a, const QuartetGeom& g, const int* dims,
+                          const T* V, double deg, int lane) {
+  const int n0 = dims[0], n1 = dims[1], n2 = dims[2], n3 = dims[3];
+  const int o0 = a.basis.bf_off[g.sh[0]], o1 = a.basis.bf_off[g.sh[1]];
+  const int o2 = a.basis.bf_off[g.sh[2]], o3 = a.basis.bf_off[g.sh[3]];
+  const int nbf = a.nbf;
+  const double* D = a.D;
+  auto v = [&](int i, int j, int k, int l) -> double {
+    return double(V[((i * n1 + j) * n2 + k) * n3 + l]);
+  };
+  // J(a,b) += sum_cd D(c,d) v
+  for (int e = lane; e < n0 * n1; e += 32) {
+    const int i = e / n1, j = e % n1;
+    double s = 0;
+    for (int k = 0; k < n2; ++k)
+      for (int l = 0; l < n3; ++l) s += __ldg(D + (size_t)(o2 + k) * nbf + o3 + l) * v(i, j, k, l);
+    atomicAdd(a.Jacc + (size_t)(o0 + i) * nbf + o1 + j, deg * s);
+  }
+  // J(c,d) += sum_ab D(a,b) v
+  for (int e = lane; e < n2 * n3; e += 32) {
+    const int k = e / n3, l = e % n3;
+    double s = 0;
+    for (int i = 0; i < n0; ++i)
+      for (int j = 0; j < n1; ++j) s += __ldg(D + (size_t)(o0 + i) * nbf + o1 + j) * v(i, j, k, l);
+    atomicAdd(a.Jacc + (size_t)(o2 + k) * nbf + o3 + l, deg * s);
+  }
+  // K(a,c) += sum_bd D(b,d) v ; K(b,d) += sum_ac D(a,c) v
+  for (int e = lane; e < n0 * n2; e += 32) {
+    const int i = e / n2, k = e % n2;
+    double s = 0;
+    for (int j = 0; j < n1; ++j)
+      for (int l = 0; l < n3; ++l) s += __ldg(D + (size_t)(o1 + j) * nbf + o3 + l) * v(i, j, k, l);
+    atomicAdd(a.Kacc + (size_t)(o0 + i) * nbf + o2 + k, deg * s);
+  }
+  for (int e = lane; e < n1 * n3; e += 32) {
+    const int j = e / n3, l = e % n3;
+    double s = 0;
+    for (int i = 0; i < n0; ++i)
+      for (int k = 0; k < n2; ++k) s += __ldg(D + (size_t)(o0 + i) * nbf + o2 + k) * v(i, j, k, l);
+    atomicAdd(a.Kacc + (size_t)(o1 + j) * nbf + o3 + l, deg * s);
+  }
+  // K(a,d) += sum_bc D(b,c) v ; K(b,c) += sum_ad D(a,d) v
+  for (int e = lane; e < n0 * n3; e += 32) {
+    const int i = e / n3, l = e % n3;
+    double s = 0;
+    for (int j = 0; j < n1; ++j)
+      for (int k = 0; k < n2; ++k) s += __ldg(D + (size_t)(o1 + j) * nbf + o2 + k) * v(i, j, k, l);
+    atomicAdd(a.Kacc + (size_t)(o0 + i) * nbf + o3 + l, deg * s);
+  }
+  for (int e = lane; e < n1 * n2; e += 32) {
+    const int j = e / n2, k = e % n2;
+    double s = 0;
+    for (int i = 0; i < n0; ++i)
+      for (int l = 0; l < n3; ++l) s += __ldg(D + (size_t)(o0 + i) * nbf + o3 + l) * v(i, j, k, l);
+    atomicAdd(a.Kacc + (size_t)(o1 + j) * nbf + o2 + k, deg * s);
+  }
+}
+
+// Gradient digestion: sj = sum v D_ab D_cd, sk = sum v (D_ac D_bd + D_ad D_bc)/2.
+template <typename T>
+__device__ void digest_grad(const EriArgs& a, const QuartetGeom& g, const int* dims,
+                            const T* V, double& sj, double& sk, int lane) {
+  const int n0 = dims[0], n1 = dims[1], n2 = dims[2], n3 = dims[3];
+  const int o0 = a.basis.bf_off[g.sh[0]], o1 = a.basis.bf_off[g.sh[1]];
+  const int o2 = a.basis.bf_off[g.sh[2]], o3 = a.basis.bf_off[g.sh[3]];
+  const int nbf = a.nbf;
+  const double* D = a.D;
+  double pj = 0, pk = 0;
+  const int tot = n0 * n1 * n2 * n3;
+  for (int e = lane; e < tot; e += 32) {
+    const int l = e % n3, k = (e / n3) % n2, j = (e / (n3 * n2)) % n1, i = e / (n3 * n2 * n1);
+    const double val = double(V[e]);
+    const double Dab = __ldg(D + (size_t)(o0 + i) * nbf + o1 + j);
+    const double Dcd = __ldg(D + (size_t)(o2 + k) * nbf + o3 + l);
+    const double Dac = __ldg(D + (size_t)(o0 + i) * nbf + o2 + k);
+    const double Dbd = __ldg(D + (size_t)(o1 + j) * nbf + o3 + l);
+    const double Dad = __ldg(D + (size_t)(o0 + i) * nbf + o3 + l);
+    const double Dbc = __ldg(D + (size_t)(o1 + j) * nbf + o2 + k);
+    pj += val * Dab * Dcd;
+    pk += val * 0.5 * (Dac * Dbd + Dad * Dbc);
+  }
+  sj = warp_sum(pj);
+  sk = warp_sum(pk);
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(128)
+eri_warp_kernel(EriArgs a) {
+  extern __shared__ double smem_d[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const DevProg& P = a.prog;
+  double* stage = smem_d + wib * (32 * kStage);
+  T* slots;
+  if (a.global_slots) {
+    const size_t gw = size_t(blockIdx.x) * wpb + wib;
+    slots = reinterpret_cast<T*>(a.gscratch) + gw * size_t(a.slot_stride);
+  } else {
+    T* base = reinterpret_cast<T*>(smem_d + wpb * (32 * kStage));
+    slots = base + size_t(wib) * a.slot_stride;
+  }
+  const long long total = a.implicit ? a.bin.total : a.nitems;
+  long long nchunks = 0;
+  unsigned long long my_prims = 0;
+  while (true) {
+    long long start = 0;
+    if (lane == 0) start = (long long)atomicAdd(a.counter, (unsigned long long)a.chunk);
+    start = __shfl_sync(0xffffffffu, start, 0);
+    if (start >= total) break;
+    if (++nchunks > a.max_chunks) {  // watchdog: cannot happen for valid input
+      if (lane == 0) atomicExch(a.error_flag, 1);
+      break;
+    }
+    const long long end = min(total, start + (long long)a.chunk);
+    // implicit decode state
+    int row = 0;
+    if (a.implicit) {
+      int lo = 0, hi = a.bin.nbra;  // last row with row_start <= start
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (a.bin.row_start[mid] <= start) lo = mid; else hi = mid;
+      }
+      row = lo;
+    }
+    for (long long q = start; q < end; ++q) {
+      int bpair, kpair, flags = 0, orig = 0;
+      long long outoff = 0;
+      if (a.implicit) {
+        while (row + 1 < a.bin.nbra && a.bin.row_start[row + 1] <= q) ++row;
+        const int j = int(q - a.bin.row_start[row]) + a.bin.row_j0[row];
+        bpair = a.bin.bra_pairs[row];
+        kpair = a.bin.ket_pairs[j];
+        flags = (a.pair_swap[bpair] ? 1 : 0) | (a.pair_swap[kpair] ? 2 : 0);
+      } else {
+        const QuartetItem it = a.items[q];
+        bpair = it.bra_pair;
+        kpair = it.ket_pair;
+        flags = it.flags;
+        outoff = it.out;
+        orig = it.pad;
+      }
+      QuartetGeom g;
+      load_geom(a, bpair, kpair, flags & 1, (flags >> 1) & 1, g);
+      const int kept = contract_quartet<T>(a, g, slots, stage, lane);
+      my_prims += kept;
+      if (MODE == kModeStore && a.is_null && lane == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
+      if (kept == 0) {
+        if (MODE == kModeSchwarz && lane == 0) a.kschwarz[outoff] = 0.0;
+        continue;
+      }
+      const int lsh[4] = {P.la, P.lb, P.lc, P.ld};
+      int pure[4];
+      for (int t = 0; t < 4; ++t) pure[t] = a.basis.pure[g.sh[t]];
+      double deg = 1.0;
+      if (MODE == kModeJK || MODE == kModeGrad) {
+        const bool same_pair = (bpair == kpair);
+        deg = (g.sh[0] == g.sh[1] ? 1.0 : 2.0) * (g.sh[2] == g.sh[3] ? 1.0 : 2.0) *
+              (same_pair ? 1.0 : 2.0);
+      }
+      double cj[3] = {0, 0, 0}, ck[3] = {0, 0, 0};
+      for (int ph = 0; ph < P.nphases; ++ph) {
+        run_post_phase<T>(P, ph, g, slots, lane);
+        for (int s = 0; s < P.sets_per_phase; ++s) {
+          int dims[4] = {ncart_of(P.la), ncart_of(P.lb), ncart_of(P.lc), ncart_of(P.ld)};
+          T* cart = slots + P.cart_out + s * P.ncart4;
+          T* V = sph_transform<T>(a, lsh, pure, dims, cart, slots + P.sph_tmp, lane);
+          const int nsph4 = dims[0] * dims[1] * dims[2] * dims[3];
+          if (MODE == kModeSchwarz) {
+            double mx = 0;
+            for (int e = lane; e < nsph4; e += 32) mx = fmax(mx, fabs(double(V[e])));
+            mx = warp_max(mx);
+            if (lane == 0) a.kschwarz[outoff] = sqrt(mx);
+          } else if (MODE == kModeJK) {
+            digest_jk<T>(a, g, dims, V, deg, lane);
+          } else if (MODE == kModeGrad) {
+            double sj, sk;
+            digest_grad<T>(a, g, dims, V, sj, sk, lane);
+            const int ctr = ph == 0 ? 0 : (ph == 1 ? 1 : 3);
+            cj[s] -= sj;
+            ck[s] -= sk;
+            if (lane == 0) {
+              const int at = a.basis.atom[g.sh[ctr]];
+              atomicAdd(a.gJ + 3 * at + s, 0.5 * deg * sj);
+              atomicAdd(a.gK + 3 * at + s, -0.25 * deg * sk);
+            }
+          } else {  // kModeStore
+            const int fl = flags >> 2;
+            const bool sbk = fl & 1, stb = (fl >> 1) & 1, stk = (fl >> 2) & 1;
+            int perm[4];
+            perm[0] = sbk ? (stk ? 3 : 2) : (stb ? 1 : 0);
+            perm[1] = sbk ? (stk ? 2 : 3) : (stb ? 0 : 1);
+            perm[2] = sbk ? (stb ? 1 : 0) : (stk ? 3 : 2);
+            perm[3] = sbk ? (stb ? 0 : 1) : (stk ? 2 : 3);
+            int tn[4];
+            for (int t = 0; t < 4; ++t) tn[perm[t]] = dims[t];
+            const int ctr = P.deriv ? (ph == 0 ? 0 : (ph == 1 ? 1 : 3)) : 0;
+            const int ts = P.deriv ? perm[ctr] * 3 + s : 0;
+            double* o = a.out + outoff + (size_t)ts * nsph4;
+            T* cb = slots + P.cbuf + s * P.ncart4;
+            for (int e = lane; e < nsph4; e += 32) {
+              int ci[4];
+              int r = e;
+              ci[3] = r % dims[3]; r /= dims[3];
+              ci[2] = r % dims[2]; r /= dims[2];
+              ci[1] = r % dims[1]; ci[0] = r / dims[1];
+              int it[4];
+              for (int t = 0; t < 4; ++t) it[perm[t]] = ci[t];
+              const int tidx = ((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3];
+              o[tidx] = double(V[e]);
+              if (P.deriv) cb[e] = (ph == 0 ? T(0) : cb[e]) - V[e];
+            }
+            __syncwarp();
+            if (P.deriv && ph == P.nphases - 1) {
+              // centre C by translational invariance
+              const int tsc = perm[2] * 3 + s;
+              double* oc = a.out + outoff + (size_t)tsc * nsph4;
+              for (int e = lane; e < nsph4; e += 32) {
+                int ci[4];
+                int r = e;
+                ci[3] = r % dims[3]; r /= dims[3];
+                ci[2] = r % dims[2]; r /= dims[2];
+                ci[1] = r % dims[1]; ci[0] = r / dims[1];
+                int it[4];
+                for (int t = 0; t < 4; ++t) it[perm[t]] = ci[t];
+                const int tidx = ((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3];
+                oc[tidx] = double(cb[e]);
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+      if (MODE == kModeGrad && lane == 0) {
+        const int at = a.basis.atom[g.sh[2]];
+        for (int s = 0; s < 3; ++s) {
+          atomicAdd(a.gJ + 3 * at + s, 0.5 * deg * cj[s]);
+          atomicAdd(a.gK + 3 * at + s, -0.25 * deg * ck[s]);
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (a.prim_count && lane == 0) atomicAdd(a.prim_count, my_prims);
+}
+
+// ---------------------------------------------------------- pair kernel
+// ShellPair::init for every pair (s1 >= s2) of the basis, one thread per
+// primitive pair (shell.h:1138-1256, Original/Conservative screening).
+__global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs,
+                                 PrimPairRec* pp, const int* pp_pair, long long npp,
+                                 double ln_prec, int method) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= npp) return;
+  const int pi = pp_pair[t];
+  const PairRec pr = pairs[pi];
+  const int k = int(t - pr.pp_off);
+  const int s1 = pr.s1, s2 = pr.s2;
+  const int n2 = b.nprim[s2];
+  const int p1 = k / n2, p2 = k % n2;
+  const double a1 = b.alpha[b.prim_off[s1] + p1];
+  const double a2 = b.alpha[b.prim_off[s2] + p2];
+  const double c1 = b.coeff[b.prim_off[s1] + p1];
+  const double c2 = b.coeff[b.prim_off[s2] + p2];
+  double A[3], B[3], AB2 = 0;
+  for (int x = 0; x < 3; ++x) {
+    A[x] = b.O[3 * s1 + x];
+    B[x] = b.O[3 * s2 + x];
+    AB2 += (A[x] - B[x]) * (A[x] - B[x]);
+  }
+  const double gamma = a1 + a2, oog = 1.0 / gamma;
+  const double rho = a1 * a2 * oog;
+  const double mrAB2 = -rho * AB2;
+  double ln_scr = mrAB2 + log(fabs(c1)) + log(fabs(c2));
+  PrimPairRec r;
+  for (int x = 0; x < 3; ++x) r.P[x] = (AB2 == 0.0) ? A[x] : (a1 * A[x] + a2 * B[x]) * oog;
+  double nonsph = 0;
+  bool drop = (method == 0 && ln_scr < ln_prec);
+  if (method == 1) {
+    double mPA = 0, mPB = 0;
+    for (int x = 0; x < 3; ++x) {
+      mPA = fmax(mPA, fabs(r.P[x] - A[x]));
+      mPB = fmax(mPB, fabs(r.P[x] - B[x]));
+    }
+    const int l1 = b.l[s1], l2 = b.l[s2];
+    const double fl1 = l1 < 2 ? 1.0 : (l1 == 2 ? 2.0 : 6.0);
+    const double fl2 = l2 < 2 ? 1.0 : (l2 == 2 ? 2.0 : 6.0);
+    const double t1 = pow(mPA, l1) * pow(mPB, l2);
+    const double t2 = fl1 * fl2 * pow(oog, l1 + l2);
+    nonsph = fmax(t1, t2);
+    ln_scr += 1.777485947591722872387900 + log(oog) + log(fmax(nonsph, 1.0)) +
+              log(double(b.nprim[s1] * b.nprim[s2]));
+    drop = ln_scr < ln_prec;
+  }
+  r.Kc = 5.9149671727956128778 * exp(mrAB2) * oog * c1 * c2;
+  r.oog = oog;
+  r.ln_scr = drop ? -1.0e300 : ln_scr;
+  r.nonsph = nonsph;
+  r.a1 = a1;
+  r.a2 = a2;
+  r.pad = 0;
+  pp[t] = r;
+}
+
+// J = (Jacc + Jacc^T)/4, K = (Kacc + Kacc^T)/8 (hartree-fock++.cc:1766 with
+// the G = 2J - K split).
+__global__ void jk_finalize_kernel(const double* Jacc, const double* Kacc, double* J,
+                                   double* K, int nbf) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)nbf * nbf) return;
+  const int i = int(t / nbf), j = int(t % nbf);
+  J[t] = 0.25 * (Jacc[(size_t)i * nbf + j] + Jacc[(size_t)j * nbf + i]);
+  K[t] = 0.125 * (Kacc[(size_t)i * nbf + j] + Kacc[(size_t)j * nbf + i]);
+}
+
+// ----------------------------------------------------------- launchers
+cudaError_t set_inv_odd_table() {
+  double h[40];
+  for (int m = 0; m < 40; ++m) h[m] = 1.0 / (2 * m + 1);
+  return cudaMemcpyToSymbol(c_inv_odd, h, sizeof(h));
+}
+
+template <typename T, int MODE>
+cudaError_t launch_eri_t(const EriArgs& a, int grid, int block, size_t smem,
+                         cudaStream_t st) {
+  auto k = eri_warp_kernel<T, MODE>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, block, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int block,
+                       size_t smem, cudaStream_t st) {
+  if (!fp32) {
+    switch (mode) {
+      case kModeStore: return launch_eri_t<double, kModeStore>(a, grid, block, smem, st);
+      case kModeSchwarz: return launch_eri_t<double, kModeSchwarz>(a, grid, block, smem, st);
+      case kModeJK: return launch_eri_t<double, kModeJK>(a, grid, block, smem, st);
+      case kModeGrad: return launch_eri_t<double, kModeGrad>(a, grid, block, smem, st);
+    }
+  } else {
+    switch (mode) {
+      case kModeStore: return launch_eri_t<float, kModeStore>(a, grid, block, smem, st);
+      case kModeJK: return launch_eri_t<float, kModeJK>(a, grid, block, smem, st);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npairs,
+                              PrimPairRec* pp, const int* pp_pair, long long npp,
+                              double ln_prec, int method, cudaStream_t st) {
+  if (npp == 0) return cudaSuccess;
+  const int block = 256;
+  const long long grid = (npp + block - 1) / block;
+  shellpair_kernel<<<(unsigned)grid, block, 0, st>>>(b, pairs, npairs, pp, pp_pair, npp,
+                                                     ln_prec, method);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J,
+                               double* K, int nbf, cudaStream_t st) {
+  const long long n = (long long)nbf * nbf;
+  const int block = 256;
+  jk_finalize_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(Jacc, Kacc, J,
+                                                                           K, nbf);
+  return cudaGetLastError();
+}
+
+size_t stage_bytes_per_warp() { return size_t(32) * kStage * sizeof(double); }
+
+template <typename T, int MODE>
+int occ_t(int block, size_t smem) {
+  auto k = eri_warp_kernel<T, MODE>;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem) != cudaSuccess) return 1;
+  return n;
+}
+
+int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem) {
+  if (!fp32) {
+    switch (mode) {
+      case kModeStore: return occ_t<double, kModeStore>(block, smem);
+      case kModeSchwarz: return occ_t<double, kModeSchwarz>(block, smem);
+      case kModeJK: return occ_t<double, kModeJK>(block, smem);
+      case kModeGrad: return occ_t<double, kModeGrad>(block, smem);
+    }
+  } else {
+    switch (mode) {
+      case kModeStore: return occ_t<float, kModeStore>(block, smem);
+      case kModeJK: return occ_t<float, kModeJK>(block, smem);
+    }
+  }
+  return 1;
+}
+
+}  // namespace lgx
