@@ -133,6 +133,11 @@ typedef struct {
   int64_t integrals;       /* spherical integrals computed (both modes)   */
   int64_t prim_quartets;   /* primitive quartets entering the VRR         */
   double kernel_ms;        /* device time of the integral kernels         */
+  double pass_ms;          /* device time of the whole pass (incl. zeroing
+                              and the final symmetrization)               */
+  double flops_fp64;       /* algorithmic FP operations done in FP64      */
+  double flops_fp32;       /* algorithmic FP operations done in FP32      */
+  int64_t launches;        /* kernels launched by the pass                */
 } lgx_jk_stats;
 
 /* Coulomb and exchange matrices J_ab = sum_cd (ab|cd) D_cd and

@@ -444,3 +444,16 @@ def coulomb() -> Engine:
     """The reference binding's coulomb() factory: precision 1e-15
     (python/src/libint2/libint2.cc:50-55)."""
     return Engine(Operator.coulomb, precision=1e-15)
+
+
+def random_density(nbf: int, nocc: int, seed: int = 0) -> np.ndarray:
+    """Synthetic symmetric positive semidefinite density D = C C^T, C of shape
+    nbf x nocc with entries N(0, 1)/sqrt(nbf) from numpy's default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    C = rng.standard_normal((nbf, nocc)) / np.sqrt(nbf)
+    return C @ C.T
+
+
+def jk_energies(D, J, K):
+    """E_J = 1/2 sum D.J and E_K = -1/4 sum D.K."""
+    return 0.5 * float(np.sum(D * J)), -0.25 * float(np.sum(D * K))

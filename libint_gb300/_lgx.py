@@ -38,7 +38,9 @@ class LgxShell(ctypes.Structure):
 class LgxJkStats(ctypes.Structure):
     _fields_ = [("quartets_fp64", ctypes.c_int64), ("quartets_fp32", ctypes.c_int64),
                 ("integrals", ctypes.c_int64), ("prim_quartets", ctypes.c_int64),
-                ("kernel_ms", ctypes.c_double)]
+                ("kernel_ms", ctypes.c_double), ("pass_ms", ctypes.c_double),
+                ("flops_fp64", ctypes.c_double), ("flops_fp32", ctypes.c_double),
+                ("launches", ctypes.c_int64)]
 
 
 # Every symbol include/lgx.h declares, with its ctypes signature.

@@ -133,7 +133,7 @@ struct lgx_context {
   int nsm = 0;
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   std::string err;
   DBuf boys, sph;
   std::map<int, std::unique_ptr<ProgDev>> progs;
@@ -719,14 +719,40 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
   return LGX_OK;
 }
 
+// Algorithmic FP operations of the per-primitive-quartet prologue (pair
+// combination, T, the Boys interpolation and downward recursion, VRR
+// factors), counted from the kernel source; exp/sqrt/div count as one each.
+double prologue_flops(int mmax) { return 60.0 + 3.0 * (mmax + 1); }
+
+// FP operations of the Cartesian -> solid-harmonic transform of one set.
+double sph_flops(int la, int lb, int lc, int ld, const int* pure) {
+  const int l[4] = {la, lb, lc, ld};
+  int dims[4];
+  for (int k = 0; k < 4; ++k) dims[k] = ncart(l[k]);
+  double f = 0;
+  for (int k = 0; k < 4; ++k) {
+    if (!pure[k]) continue;
+    double rest = 1;
+    for (int t = 0; t < 4; ++t)
+      if (t != k) rest *= dims[t];
+    f += 2.0 * (2 * l[k] + 1) * dims[k] * rest;
+    dims[k] = 2 * l[k] + 1;
+  }
+  return f;
+}
+
 lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
                     EriArgs base, lgx_jk_stats* stats) {
   BinCache& C = ctx->bins;
-  CK(cudaMemsetAsync(ctx->primcount.p, 0, sizeof(unsigned long long), ctx->stream));
+  const size_t nslots = 2 * C.bins.size() + 1;
+  CK(ctx->primcount.ensure(nslots * sizeof(unsigned long long)));
+  CK(cudaMemsetAsync(ctx->primcount.p, 0, nslots * sizeof(unsigned long long), ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  long long integrals = 0;
-  for (auto& bp : C.bins) {
-    BinHost& bin = *bp;
+  long long integrals = 0, launches = 0;
+  struct Rec { int bin, sp; bool fp32; };
+  std::vector<Rec> recs;
+  for (size_t bi = 0; bi < C.bins.size(); ++bi) {
+    BinHost& bin = *C.bins[bi];
     ProgDev* P = nullptr;
     lgx_status s = get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
     if (s != LGX_OK) return s;
@@ -741,24 +767,49 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       a.bin.row_j0 = bin.row_j0[sp].as<int>();
       a.bin.nbra = bin.nbra;
       a.bin.total = bin.total[sp];
-      a.prim_count = ctx->primcount.as<unsigned long long>();
+      a.prim_count = ctx->primcount.as<unsigned long long>() + 2 * bi + sp;
       s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp]);
       if (s != LGX_OK) return s;
       integrals += bin.integrals[sp];
+      ++launches;
+      recs.push_back({int(bi), sp, fp32});
     }
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
     CK(cudaEventSynchronize(ctx->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    unsigned long long pc = 0;
-    CK(cudaMemcpy(&pc, ctx->primcount.p, sizeof(pc), cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> pc(nslots);
+    CK(cudaMemcpy(pc.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
+                  cudaMemcpyDeviceToHost));
+    long long prims = 0;
+    for (const Rec& r : recs) {
+      const BinHost& bin = *C.bins[r.bin];
+      ProgDev* P = nullptr;
+      get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
+      const unsigned long long np = pc[2 * r.bin + r.sp];
+      prims += (long long)np;
+      int pure[4] = {bin.la > 1, bin.lb > 1, bin.lc > 1, bin.ld > 1};
+      const double q = double(bin.total[r.sp]);
+      const int nsets = deriv ? 12 : 1;
+      const double tflops = double(np) * double(P->host.vrr_flops) +
+                            q * (double(P->host.post_flops) +
+                                 nsets * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure));
+      double nsph = 1;
+      const int lq[4] = {bin.la, bin.lb, bin.lc, bin.ld};
+      for (int k = 0; k < 4; ++k) nsph *= pure[k] ? 2 * lq[k] + 1 : ncart(lq[k]);
+      const double dflops = double(np) * prologue_flops(P->host.mmax) + q * nsets * 12.0 * nsph;
+      if (r.fp32) stats->flops_fp32 += tflops; else stats->flops_fp64 += tflops;
+      stats->flops_fp64 += dflops;
+    }
     stats->quartets_fp64 = C.quartets[0] + (allow_fp32 ? 0 : C.quartets[1]);
     stats->quartets_fp32 = allow_fp32 ? C.quartets[1] : 0;
     stats->integrals = integrals;
-    stats->prim_quartets = (int64_t)pc;
+    stats->prim_quartets = prims;
     stats->kernel_ms = ms;
+    stats->launches = launches;
   }
   return LGX_OK;
 }
@@ -794,6 +845,8 @@ lgx_status lgx_create(lgx_context** out, int device) {
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&c->ev0));
     CK(cudaEventCreate(&c->ev1));
+    CK(cudaEventCreate(&c->ev2));
+    CK(cudaEventCreate(&c->ev3));
     const auto boys = make_boys_table();
     CK(c->boys.ensure(boys.size() * sizeof(double)));
     CK(cudaMemcpy(c->boys.p, boys.data(), boys.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -816,6 +869,8 @@ lgx_status lgx_destroy(lgx_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+  if (ctx->ev3) cudaEventDestroy(ctx->ev3);
   cudaStream_t st = ctx->stream;
   delete ctx;
   if (st) cudaStreamDestroy(st);
@@ -980,6 +1035,7 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   const size_t nn = size_t(B.nbf) * B.nbf;
   CK(ctx->Jacc.ensure(nn * sizeof(double)));
   CK(ctx->Kacc.ensure(nn * sizeof(double)));
+  CK(cudaEventRecord(ctx->ev2, ctx->stream));
   CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
   EriArgs a{};
@@ -994,7 +1050,14 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   if (s != LGX_OK) return s;
   CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
                         ctx->stream));
+  CK(cudaEventRecord(ctx->ev3, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (stats) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3));
+    stats->pass_ms = ms;
+    stats->launches += 1;
+  }
   return check_errflag(ctx);
 }
 

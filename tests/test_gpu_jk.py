@@ -1,0 +1,174 @@
+"""Batched and fused paths on the GPU against the oracle: Schwarz factors,
+explicit quartet batches (FP64 and mixed), J/K digestion with Schwarz
+screening, and deriv_order=1 gradient digestion (against the oracle and
+central finite differences)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def water2(lgx, oracle_mod):
+    atoms = lgx.water_cluster(2, 1, 1, spacing=3.0, jitter=0.2, seed=1)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    D = lgx.random_density(bs.nbf, 10, seed=2)
+    return atoms, bs, ob, D
+
+
+def test_schwarz_matches_oracle(lgx, oracle_mod, water2):
+    _, bs, ob, _ = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    K = ctx.schwarz()
+    Kref = oracle_mod.schwarz(ob)
+    assert np.max(np.abs(K - Kref)) < 1e-12
+    ctx.close()
+
+
+def test_batch_fp64_vs_oracle(lgx, oracle_mod, water2):
+    _, bs, ob, _ = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    rng = np.random.default_rng(4)
+    q = rng.integers(0, len(bs), size=(400, 4))
+    out, offs, isnull = ctx.compute_batch(q)
+    worst = 0.0
+    for i, quad in enumerate(q):
+        ref = oracle_mod.compute_quartet(ob, *[int(x) for x in quad])
+        if ref is None:
+            assert isnull[i] == 1
+            continue
+        n = ref[0].size
+        worst = max(worst, float(np.max(np.abs(out[offs[i]:offs[i] + n] - ref[0].reshape(-1)))))
+    assert worst < 1e-12, worst
+    ctx.close()
+
+
+def test_batch_deriv1_vs_oracle(lgx, oracle_mod, water2):
+    _, bs, ob, _ = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    rng = np.random.default_rng(5)
+    q = rng.integers(0, len(bs), size=(60, 4))
+    out, offs, isnull = ctx.compute_batch(q, deriv=1)
+    for i, quad in enumerate(q):
+        ref = oracle_mod.compute_quartet(ob, *[int(x) for x in quad], deriv=1)
+        if ref is None:
+            continue
+        ref = np.concatenate([r.reshape(-1) for r in ref])
+        assert np.max(np.abs(out[offs[i]:offs[i] + ref.size] - ref)) < 1e-12
+    ctx.close()
+
+
+def test_batch_mixed_error_bound(lgx, oracle_mod, water2):
+    _, bs, ob, _ = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    K = ctx.schwarz()
+    rng = np.random.default_rng(6)
+    q = rng.integers(0, len(bs), size=(400, 4))
+    out, offs, _ = ctx.compute_batch(q, mode=1, mixed_thresh=1e-4)
+    for i, quad in enumerate(q):
+        a, b, c, d = [int(x) for x in quad]
+        ref = oracle_mod.compute_quartet(ob, a, b, c, d)
+        if ref is None:
+            continue
+        err = np.max(np.abs(out[offs[i]:offs[i] + ref[0].size] - ref[0].reshape(-1)))
+        bound = K[a, b] * K[c, d]
+        # FP64 quartets keep the FP64 tolerance; FP32 ones stay far below the bound
+        assert err < (1e-12 if bound >= 1e-4 else max(1e-12, 1e-5 * bound)), (quad, err, bound)
+    ctx.close()
+
+
+@pytest.mark.parametrize("thresh", [0.0, 1e-12])
+def test_jk_fp64_vs_oracle(lgx, oracle_mod, water2, thresh):
+    _, bs, ob, D = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    J, K, st = ctx.jk(D, schwarz_thresh=thresh)
+    Kq = oracle_mod.schwarz(ob)
+    Jr, Kr, nq = oracle_mod.jk(ob, D, Kq, thresh)
+    assert st.quartets_fp64 == nq
+    assert np.max(np.abs(J - Jr)) < 1e-11
+    assert np.max(np.abs(K - Kr)) < 1e-11
+    ej, ek = lgx.jk_energies(D, J, K)
+    ejr, ekr = lgx.jk_energies(D, Jr, Kr)
+    assert abs(ej - ejr) < 1e-11 and abs(ek - ekr) < 1e-11
+    ctx.close()
+
+
+def test_jk_brute_force_definition(lgx, oracle_mod):
+    # J_ab = sum_cd (ab|cd) D_cd, K_ab = sum_cd (ac|bd) D_cd from the full tensor
+    atoms = lgx.water_cluster(1, 1, 1, seed=9)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    D = lgx.random_density(bs.nbf, 5, seed=3)
+    n = bs.nbf
+    off = bs.shell2bf()
+    G = np.zeros((n, n, n, n))
+    for a in range(len(bs)):
+        for b in range(len(bs)):
+            for c in range(len(bs)):
+                for d in range(len(bs)):
+                    r = oracle_mod.compute_quartet(ob, a, b, c, d)
+                    if r is None:
+                        continue
+                    na, nb, nc, nd = r[0].shape
+                    G[off[a]:off[a] + na, off[b]:off[b] + nb,
+                      off[c]:off[c] + nc, off[d]:off[d] + nd] = r[0]
+    Jb = np.einsum("abcd,cd->ab", G, D)
+    Kb = np.einsum("acbd,cd->ab", G, D)
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    J, K, _ = ctx.jk(D, schwarz_thresh=0.0)
+    assert np.max(np.abs(J - Jb)) < 1e-11
+    assert np.max(np.abs(K - Kb)) < 1e-11
+    ctx.close()
+
+
+def test_jk_mixed_energy_error(lgx, water2):
+    _, bs, _, D = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    J64, K64, _ = ctx.jk(D, 1e-12)
+    Jm, Km, st = ctx.jk(D, 1e-12, mode=1, mixed_thresh=1e-4)
+    assert st.quartets_fp32 > 0
+    e64 = lgx.jk_energies(D, J64, K64)
+    em = lgx.jk_energies(D, Jm, Km)
+    assert abs(e64[0] - em[0]) <= 1e-8 and abs(e64[1] - em[1]) <= 1e-8
+    ctx.close()
+
+
+def test_gradient_vs_oracle_and_fd(lgx, oracle_mod, water2):
+    atoms, bs, ob, D = water2
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    natoms = len(atoms)
+    gJ, gK, _ = ctx.jk_grad(D, natoms, 1e-12)
+    Kq = oracle_mod.schwarz(ob)
+    gJr, gKr, _ = oracle_mod.jk_grad(ob, D, Kq, natoms, 1e-12)
+    assert np.max(np.abs(gJ - gJr)) < 1e-10
+    assert np.max(np.abs(gK - gKr)) < 1e-10
+    # translational invariance of the two-electron energies
+    assert np.max(np.abs(gJ.sum(axis=0))) < 1e-9
+    # central finite differences, h = 1e-4 bohr, on two coordinates
+    h = 1e-4
+    for (at, x) in [(0, 0), (4, 2)]:
+        e = []
+        for sgn in (+1, -1):
+            moved = [lgx.Atom(Z, xyz) for Z, xyz in atoms]
+            xyz = list(moved[at][1]); xyz[x] += sgn * h
+            moved[at] = lgx.Atom(moved[at][0], xyz)
+            bsm = lgx.BasisSet("cc-pVDZ", moved)
+            c2 = lgx.Context(0)
+            c2.set_basis(bsm)
+            Jm, Km, _ = c2.jk(D, 0.0)
+            e.append(lgx.jk_energies(D, Jm, Km))
+            c2.close()
+        fdJ = (e[0][0] - e[1][0]) / (2 * h)
+        fdK = (e[0][1] - e[1][1]) / (2 * h)
+        assert abs(fdJ - gJ[at, x]) < 1e-6, (fdJ, gJ[at, x])
+        assert abs(fdK - gK[at, x]) < 1e-6, (fdK, gK[at, x])
+    ctx.close()
