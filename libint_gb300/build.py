@@ -8,6 +8,7 @@ from __future__ import annotations
 import os
 import shutil
 import subprocess
+import sys
 from concurrent.futures import ThreadPoolExecutor
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
@@ -17,7 +18,8 @@ BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liblgx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu"]
+CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu", "lgx_rk_f64_jk.cu", "lgx_rk_f64_store.cu",
+                "lgx_rk_f32.cu"]
 CXX_SOURCES = ["lgx_program.cpp", "lgx_host.cpp"]
 
 
@@ -28,15 +30,29 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblgx")
 
 
+def _generate() -> None:
+    """Regenerates the unrolled per-class code (no-op when unchanged)."""
+    sys.path.insert(0, os.path.join(PKG_DIR, "codegen"))
+    try:
+        import gen_rk
+        gen_rk.main()
+    finally:
+        sys.path.pop(0)
+
+
 def _deps_mtime() -> float:
     t = 0.0
-    for d in (CSRC, os.path.join(ROOT, "include")):
+    for d in (CSRC, os.path.join(CSRC, "gen"), os.path.join(PKG_DIR, "codegen"),
+              os.path.join(ROOT, "include")):
         for f in os.listdir(d):
-            t = max(t, os.path.getmtime(os.path.join(d, f)))
+            fp = os.path.join(d, f)
+            if os.path.isfile(fp):
+                t = max(t, os.path.getmtime(fp))
     return t
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    _generate()
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) >= _deps_mtime()):
         return LIB_PATH

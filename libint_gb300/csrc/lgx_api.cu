@@ -28,6 +28,16 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
                                double* K, int nbf, cudaStream_t st);
 size_t stage_bytes_per_warp();
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
+cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
+#define LGX_DECL_RK(NAME)                                                              \
+  cudaError_t NAME(int la, int lb, int lc, int ld, const EriArgs& a, long long work,    \
+                   int nsm, cudaStream_t st);
+LGX_DECL_RK(rk_launch_f64_jk)
+LGX_DECL_RK(rk_launch_f64_store)
+LGX_DECL_RK(rk_launch_f64_schwarz)
+LGX_DECL_RK(rk_launch_f32_jk)
+LGX_DECL_RK(rk_launch_f32_store)
+#undef LGX_DECL_RK
 }  // namespace lgx
 
 using namespace lgx;
@@ -104,9 +114,12 @@ struct BasisDev {
   // Schwarz
   std::vector<double> Kpair;  // per pair index
   bool schwarz_ok = false;
+  bool std_pure = true;  // every shell has pure == (l >= 2)
+  double avg_npp = 1;    // mean primitive pairs per shell pair
 };
 
 struct BinHost {
+  double nq_avg = 1;  // mean primitive quartets per shell quartet (unscreened)
   int cls;  // class index
   int la, lb, lc, ld;
   int bra_class, ket_class;
@@ -135,8 +148,9 @@ struct lgx_context {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   std::string err;
-  DBuf boys, sph;
+  DBuf boys, boys32, sph, Df;
   std::map<int, std::unique_ptr<ProgDev>> progs;
+  bool use_rk = true;  // register kernels for the small classes
   BasisDev basis, small;
   DBuf gscratch, counter, errflag, primcount;
   DBuf items, out, isnull;
@@ -333,6 +347,9 @@ lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t
   B.nprim_total = np;
   B.nbf = nbf;
   B.natoms = natoms;
+  B.std_pure = true;
+  for (int s = 0; s < nshell; ++s)
+    if ((pure[s] != 0) != (l[s] >= 2)) B.std_pure = false;
   B.O.assign(origins, origins + 3 * nshell);
   B.alpha.assign(alpha, alpha + np);
   B.coeff.assign(coeff, coeff + np);
@@ -445,8 +462,50 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
   return LGX_OK;
 }
 
+// Register kernels exist for classes with la+lb+lc+ld <= 4 (deriv 0) and
+// shells with the standard pure flags; everything else runs on the
+// warp-cooperative program kernel.
+bool rk_eligible(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode) {
+  if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0) return false;
+  if (P.host.la + P.host.lb + P.host.lc + P.host.ld > 4) return false;
+  return mode == kModeJK || mode == kModeStore || mode == kModeSchwarz;
+}
+
+int choose_group(double nq_avg) {
+  int g = 1;
+  while (g < 32 && g * 2 <= nq_avg * 0.5) g *= 2;
+  return g;
+}
+
+lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
+                  EriArgs a, long long nwork, double nq_avg) {
+  a.basis = B.dev;
+  a.pairs = B.pairs.as<PairRec>();
+  a.pprims = B.pprims.as<PrimPairRec>();
+  a.pair_swap = B.pair_swap.as<unsigned char>();
+  a.boys = ctx->boys.as<double>();
+  a.boys32 = ctx->boys32.as<float>();
+  a.sph = ctx->sph.as<double>();
+  a.error_flag = ctx->errflag.as<int>();
+  a.group = choose_group(nq_avg);
+  const int la = P.host.la, lb = P.host.lb, lc = P.host.lc, ld = P.host.ld;
+  cudaError_t e;
+  if (!fp32) {
+    e = mode == kModeJK ? rk_launch_f64_jk(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream)
+        : mode == kModeStore ? rk_launch_f64_store(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream)
+                             : rk_launch_f64_schwarz(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream);
+  } else {
+    e = mode == kModeJK ? rk_launch_f32_jk(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream)
+                        : rk_launch_f32_store(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream);
+  }
+  CK(e);
+  return LGX_OK;
+}
+
 lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
-                   EriArgs a, long long nwork) {
+                   EriArgs a, long long nwork, double nq_avg = 1.0) {
+  if (rk_eligible(ctx, B, P, mode) && !(fp32 && mode == kModeSchwarz))
+    return run_rk(ctx, B, P, mode, fp32, a, nwork, nq_avg);
   Launch L;
   lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, L);
   if (s != LGX_OK) return s;
@@ -578,7 +637,11 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
     a.out = d_out;
     a.is_null = d_isnull;
     a.kschwarz = d_kschwarz;
-    s = run_eri(ctx, B, *P, mode, kv.second.fp32, a, a.nitems);
+    double nq = 0;
+    for (const auto& it : kv.second.items)
+      nq += double(B.hpairs[it.bra_pair].npp) * double(B.hpairs[it.ket_pair].npp);
+    nq /= std::max<size_t>(1, kv.second.items.size());
+    s = run_eri(ctx, B, *P, mode, kv.second.fp32, a, a.nitems, nq);
     if (s != LGX_OK) return s;
     ++gi;
   }
@@ -698,6 +761,12 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
                nfunc(B.l[B.hpairs[p].s2], B.pure[B.hpairs[p].s2]);
       };
       const long long nfq = nf_pair(bra[0]) * nf_pair(ket[0]);
+      {
+        double sb = 0, sk = 0;
+        for (int p : bra) sb += B.hpairs[p].npp;
+        for (int p : ket) sk += B.hpairs[p].npp;
+        bin->nq_avg = (sb / bra.size()) * (sk / ket.size());
+      }
       for (int sp = 0; sp < 2; ++sp) {
         bin->total[sp] = rs[sp].back();
         bin->integrals[sp] = bin->total[sp] * nfq;
@@ -768,7 +837,7 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       a.bin.nbra = bin.nbra;
       a.bin.total = bin.total[sp];
       a.prim_count = ctx->primcount.as<unsigned long long>() + 2 * bi + sp;
-      s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp]);
+      s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg);
       if (s != LGX_OK) return s;
       integrals += bin.integrals[sp];
       ++launches;
@@ -850,6 +919,10 @@ lgx_status lgx_create(lgx_context** out, int device) {
     const auto boys = make_boys_table();
     CK(c->boys.ensure(boys.size() * sizeof(double)));
     CK(cudaMemcpy(c->boys.p, boys.data(), boys.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float> boysf(boys.begin(), boys.end());
+    CK(c->boys32.ensure(boysf.size() * sizeof(float)));
+    CK(cudaMemcpy(c->boys32.p, boysf.data(), boysf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (const char* e = getenv("LGX_DISABLE_RK")) c->use_rk = (e[0] == '0');
     const auto sph = make_sph_table();
     CK(c->sph.ensure(sph.size() * sizeof(double)));
     CK(cudaMemcpy(c->sph.p, sph.data(), sph.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -1038,11 +1111,16 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   CK(cudaEventRecord(ctx->ev2, ctx->stream));
   CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
+  if (mode == LGX_MIXED) {
+    CK(ctx->Df.ensure(nn * sizeof(float)));
+    CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
+  }
   EriArgs a{};
   a.precision = eps;
   a.ln_prec = std::log(eps);
   a.screening = 0;
   a.D = dD;
+  a.Df = ctx->Df.as<float>();
   a.Jacc = ctx->Jacc.as<double>();
   a.Kacc = ctx->Kacc.as<double>();
   a.nbf = B.nbf;

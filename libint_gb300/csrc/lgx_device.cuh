@@ -80,16 +80,23 @@ struct DevBasis {
   const double* coeff;  // flattened, normalization embedded
 };
 
-// One primitive pair of a shell pair (s1, s2) as stored (s1 = first shell).
-struct PrimPairRec {
+// One primitive pair of a shell pair (s1, s2) as stored (s1 = first shell),
+// with FP64 fields for the FP64 kernels and FP32 copies (centre-relative
+// P, so FP32 P-Q differences keep their precision) for the FP32 kernels.
+struct __align__(16) PrimPairRec {
   double P[3];
   double Kc;      // sqrt(2) pi^{5/4} exp(-rho AB^2)/gamma * c1 * c2
   double oog;     // 1/(alpha1 + alpha2)
   double ln_scr;  // ln of the pair screening factor (shell.h:1041-1059)
   double nonsph;  // Conservative screening factor
   double a1, a2;  // exponents of s1 and s2
-  double pad;
+  float fKc, fzeta, foog, fln_scr;
+  float fPA1[3];  // P - O(s1)
+  float fPA2[3];  // P - O(s2)
+  float fa1, fa2;
+  float pad[2];
 };
+static_assert(sizeof(PrimPairRec) == 128, "PrimPairRec layout");
 
 // A shell pair with its primitive-pair range (pair list, shell.h:1079-1329).
 struct PairRec {

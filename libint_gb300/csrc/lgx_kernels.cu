@@ -607,7 +607,17 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs,
   r.nonsph = nonsph;
   r.a1 = a1;
   r.a2 = a2;
-  r.pad = 0;
+  r.fKc = float(r.Kc);
+  r.fzeta = float(gamma);
+  r.foog = float(oog);
+  r.fln_scr = drop ? -3.0e38f : float(ln_scr);
+  for (int x = 0; x < 3; ++x) {
+    r.fPA1[x] = float(r.P[x] - A[x]);
+    r.fPA2[x] = float(r.P[x] - B[x]);
+  }
+  r.fa1 = float(a1);
+  r.fa2 = float(a2);
+  r.pad[0] = r.pad[1] = 0.f;
   pp[t] = r;
 }
 
@@ -679,6 +689,17 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
 }
 
 size_t stage_bytes_per_warp() { return size_t(32) * kStage * sizeof(double); }
+
+__global__ void d2f_kernel(const double* src, float* dst, long long n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = float(src[t]);
+}
+
+cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st) {
+  const int block = 256;
+  d2f_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
 
 template <typename T, int MODE>
 int occ_t(int block, size_t smem) {

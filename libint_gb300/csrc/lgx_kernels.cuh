@@ -39,6 +39,7 @@ struct EriArgs {
   const unsigned char* pair_swap;  // per pair: 1 if its canonical bra1 is s2
   DevProg prog;
   const double* boys;
+  const float* boys32;   // FP32 copy of the Boys table
   const double* sph;
   // screening
   double precision, ln_prec;
@@ -49,6 +50,7 @@ struct EriArgs {
   BinWork bin;
   int implicit;   // 1: use bin, 0: use items
   int chunk;
+  int group;           // register kernels: lanes per quartet (power of 2)
   unsigned long long* counter;
   // slots
   int slot_stride;     // slots per warp (elements of T)
@@ -59,6 +61,7 @@ struct EriArgs {
   int* is_null;        // kModeStore, per item (may be null)
   double* kschwarz;    // kModeSchwarz
   const double* D;     // kModeJK / kModeGrad
+  const float* Df;     // FP32 copy of D (FP32 register kernels)
   double* Jacc;
   double* Kacc;
   double* gJ;

@@ -1,0 +1,454 @@
+// Register-resident ERI kernel: G lanes (1, 2, 4, ..., 32) per contracted
+// shell quartet.  The lanes of a group split the primitive quartets, each
+// runs the prologue (screening, pfac, T, Boys, VRR factors) and the class's
+// unrolled VRR with the contracted (e0|f0) accumulators in registers; the
+// group then reduces the accumulators with shuffles, applies the unrolled
+// HRR and solid-harmonic transform, and splits the epilogue (J/K digestion,
+// store, Schwarz maximum) between its lanes.
+//
+// Prologue precision follows the kernel's arithmetic type T: FP64 kernels
+// evaluate everything in FP64 (libint's algorithm, engine.impl.h:1306-1766);
+// FP32 kernels use the FP32 copies of the primitive-pair data, with P-Q
+// formed from centre-relative offsets plus the FP64 centre difference A-C
+// so that it keeps FP32 relative precision.
+#pragma once
+#include "gen/rk_classes.cuh"
+
+namespace lgx {
+
+__device__ __forceinline__ double rk_exp(double x) { return exp(x); }
+__device__ __forceinline__ float rk_exp(float x) { return __expf(x); }
+__device__ __forceinline__ double rk_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rk_rsqrt(float x) { return rsqrtf(x); }
+
+// Boys F_0..F_MMAX(T) (times nothing).  FP64: 7-term Taylor about the grid
+// point (every m directly when MMAX <= 2, else the top m plus the downward
+// recursion); FP32: 4-term Taylor on the same grid.  T > kBoysTmax:
+// asymptotic F_0 and upward recursion.
+template <int MMAX>
+__device__ __forceinline__ void rk_boys(const double* __restrict__ tab, double T, double* F) {
+  if (T > kBoysTmax) {
+    const double rT = 1.0 / T;
+    const double oo2T = 0.5 * rT;
+    const double eT = exp(-T);
+    double f = 0.88622692545275801365 * sqrt(rT);
+    F[0] = f;
+#pragma unroll
+    for (int m = 0; m < MMAX; ++m) {
+      f = ((2 * m + 1) * f - eT) * oo2T;
+      F[m + 1] = f;
+    }
+    return;
+  }
+  const int k = __double2int_rn(T * kBoysInvDT);
+  const double d = T - k * kBoysDT;
+  const double* row = tab + k * kBoysCols;
+  const double c6 = -d * (1.0 / 6.0), c5 = -d * (1.0 / 5.0), c4 = -d * (1.0 / 4.0);
+  const double c3 = -d * (1.0 / 3.0), c2 = -d * 0.5, c1 = -d;
+  if (MMAX <= 2) {
+#pragma unroll
+    for (int m = 0; m <= MMAX; ++m) {
+      double s = __ldg(row + m + 6);
+      s = fma(s, c6, __ldg(row + m + 5));
+      s = fma(s, c5, __ldg(row + m + 4));
+      s = fma(s, c4, __ldg(row + m + 3));
+      s = fma(s, c3, __ldg(row + m + 2));
+      s = fma(s, c2, __ldg(row + m + 1));
+      F[m] = fma(s, c1, __ldg(row + m));
+    }
+  } else {
+    double s = __ldg(row + MMAX + 6);
+    s = fma(s, c6, __ldg(row + MMAX + 5));
+    s = fma(s, c5, __ldg(row + MMAX + 4));
+    s = fma(s, c4, __ldg(row + MMAX + 3));
+    s = fma(s, c3, __ldg(row + MMAX + 2));
+    s = fma(s, c2, __ldg(row + MMAX + 1));
+    s = fma(s, c1, __ldg(row + MMAX));
+    F[MMAX] = s;
+    const double eT = exp(-T);
+    const double twoT = 2.0 * T;
+#pragma unroll
+    for (int m = MMAX - 1; m >= 0; --m) {
+      s = fma(twoT, s, eT) * (1.0 / (2 * m + 1));
+      F[m] = s;
+    }
+  }
+}
+
+template <int MMAX>
+__device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, float* F) {
+  if (T > float(kBoysTmax)) {
+    const float rT = 1.0f / T;
+    float f = 0.886226925f * rsqrtf(T);
+    F[0] = f;
+#pragma unroll
+    for (int m = 0; m < MMAX; ++m) {
+      f = (2 * m + 1) * f * (0.5f * rT);  // e^{-T} < 5e-15 is below FP32 resolution
+      F[m + 1] = f;
+    }
+    return;
+  }
+  const int k = __float2int_rn(T * float(kBoysInvDT));
+  const float d = T - k * float(kBoysDT);
+  const float* row = tab + k * kBoysCols;
+  const float c3 = -d * (1.0f / 3.0f), c2 = -d * 0.5f, c1 = -d;
+  float s = __ldg(row + MMAX + 3);
+  s = fmaf(s, c3, __ldg(row + MMAX + 2));
+  s = fmaf(s, c2, __ldg(row + MMAX + 1));
+  s = fmaf(s, c1, __ldg(row + MMAX));
+  F[MMAX] = s;
+  if (MMAX > 0) {
+    const float eT = __expf(-T);
+    const float twoT = 2.0f * T;
+#pragma unroll
+    for (int m = MMAX - 1; m >= 0; --m) {
+      s = fmaf(twoT, s, eT) * (1.0f / (2 * m + 1));
+      F[m] = s;
+    }
+  }
+}
+
+struct RkQuartet {
+  int sh[4];
+  int bra_pp, ket_pp, nbpp, nkpp;
+  bool bsw, ksw;
+  double A[3], B[3], C[3], D[3];
+};
+
+__device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, bool bsw,
+                                        bool ksw, RkQuartet& q) {
+  const PairRec bp = a.pairs[bpair];
+  const PairRec kp = a.pairs[kpair];
+  q.sh[0] = bsw ? bp.s2 : bp.s1;
+  q.sh[1] = bsw ? bp.s1 : bp.s2;
+  q.sh[2] = ksw ? kp.s2 : kp.s1;
+  q.sh[3] = ksw ? kp.s1 : kp.s2;
+  q.bra_pp = bp.pp_off;
+  q.nbpp = bp.npp;
+  q.ket_pp = kp.pp_off;
+  q.nkpp = kp.npp;
+  q.bsw = bsw;
+  q.ksw = ksw;
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    q.A[x] = a.basis.O[3 * q.sh[0] + x];
+    q.B[x] = a.basis.O[3 * q.sh[1] + x];
+    q.C[x] = a.basis.O[3 * q.sh[2] + x];
+    q.D[x] = a.basis.O[3 * q.sh[3] + x];
+  }
+}
+
+// One primitive quartet into acc (FP64).  Returns false when screened out.
+template <class C>
+__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet& q, int ib, int ik,
+                                        double* acc) {
+  const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
+  const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
+  if (!(bp.ln_scr + kp.ln_scr > a.ln_prec)) return false;
+  const double zeta = bp.a1 + bp.a2, eta = kp.a1 + kp.a2;
+  const double gpq = zeta + eta;
+  const double rs = rsqrt(gpq);
+  const double oogpq = rs * rs;
+  const double pfac = bp.Kc * kp.Kc * rs;
+  if (fabs(pfac) < a.precision) return false;
+  const double PQx = bp.P[0] - kp.P[0], PQy = bp.P[1] - kp.P[1], PQz = bp.P[2] - kp.P[2];
+  const double rho = zeta * eta * oogpq;
+  const double T = rho * fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
+  double F[C::kMmax + 1];
+  rk_boys<C::kMmax>(a.boys, T, F);
+#pragma unroll
+  for (int m = 0; m <= C::kMmax; ++m) F[m] *= pfac;
+  rk::Geo<double> g;
+  const double ez = eta * oogpq, zz = zeta * oogpq;
+  g.PAx = bp.P[0] - q.A[0]; g.PAy = bp.P[1] - q.A[1]; g.PAz = bp.P[2] - q.A[2];
+  g.QCx = kp.P[0] - q.C[0]; g.QCy = kp.P[1] - q.C[1]; g.QCz = kp.P[2] - q.C[2];
+  g.WPx = -ez * PQx; g.WPy = -ez * PQy; g.WPz = -ez * PQz;
+  g.WQx = zz * PQx; g.WQy = zz * PQy; g.WQz = zz * PQz;
+  g.oo2z = 0.5 * bp.oog;
+  g.roz = ez;
+  g.oo2e = 0.5 * kp.oog;
+  g.roe = zz;
+  g.oo2ze = 0.5 * oogpq;
+  C::template vrr<double>(F, g, acc);
+  return true;
+}
+
+// One primitive quartet into acc (FP32).  AC = A - C of the quartet.
+template <class C>
+__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet& q, int ib, int ik,
+                                        float* acc, float ACx, float ACy, float ACz) {
+  const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
+  const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
+  if (!(bp.fln_scr + kp.fln_scr > float(a.ln_prec))) return false;
+  const float zeta = bp.fzeta, eta = kp.fzeta;
+  const float gpq = zeta + eta;
+  const float rs = rsqrtf(gpq);
+  const float oogpq = rs * rs;
+  const float pfac = bp.fKc * kp.fKc * rs;
+  if (fabsf(pfac) < float(a.precision)) return false;
+  const float* PA = q.bsw ? bp.fPA2 : bp.fPA1;
+  const float* QC = q.ksw ? kp.fPA2 : kp.fPA1;
+  const float PQx = PA[0] - QC[0] + ACx, PQy = PA[1] - QC[1] + ACy, PQz = PA[2] - QC[2] + ACz;
+  const float rho = zeta * eta * oogpq;
+  const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
+  float F[C::kMmax + 1];
+  rk_boys<C::kMmax>(a.boys32, T, F);
+#pragma unroll
+  for (int m = 0; m <= C::kMmax; ++m) F[m] *= pfac;
+  rk::Geo<float> g;
+  const float ez = eta * oogpq, zz = zeta * oogpq;
+  g.PAx = PA[0]; g.PAy = PA[1]; g.PAz = PA[2];
+  g.QCx = QC[0]; g.QCy = QC[1]; g.QCz = QC[2];
+  g.WPx = -ez * PQx; g.WPy = -ez * PQy; g.WPz = -ez * PQz;
+  g.WQx = zz * PQx; g.WQy = zz * PQy; g.WQz = zz * PQz;
+  g.oo2z = 0.5f * bp.foog;
+  g.roz = ez;
+  g.oo2e = 0.5f * kp.foog;
+  g.roe = zz;
+  g.oo2ze = 0.5f * oogpq;
+  C::template vrr<float>(F, g, acc);
+  return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T rk_shfl_xor(unsigned mask, T v, int o, int width);
+template <>
+__device__ __forceinline__ double rk_shfl_xor(unsigned mask, double v, int o, int width) {
+  return __shfl_xor_sync(mask, v, o, width);
+}
+template <>
+__device__ __forceinline__ float rk_shfl_xor(unsigned mask, float v, int o, int width) {
+  return __shfl_xor_sync(mask, v, o, width);
+}
+
+// D value in the kernel's precision (FP32 kernels read the FP32 copy).
+__device__ __forceinline__ double rk_D(const EriArgs& a, size_t i, double*) {
+  return __ldg(a.D + i);
+}
+__device__ __forceinline__ float rk_D(const EriArgs& a, size_t i, float*) {
+  return __ldg(a.Df + i);
+}
+
+template <typename T, int LA, int LB, int LC, int LD, int MODE>
+__global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
+  using C = rk::Cls<LA, LB, LC, LD>;
+  constexpr int N0 = C::kN0, N1 = C::kN1, N2 = C::kN2, N3 = C::kN3;
+  const int G = a.group;
+  const int lane = threadIdx.x & 31;
+  const int g = lane & (G - 1);
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ngroups = ((long long)gridDim.x * blockDim.x) / G;
+  const long long total = a.implicit ? a.bin.total : a.nitems;
+  int row = -1;
+  for (long long qi = gtid / G; qi < total; qi += ngroups) {
+    int bpair, kpair, flags, orig = 0;
+    long long outoff = 0;
+    if (a.implicit) {
+      if (row < 0) {
+        int lo = 0, hi = a.bin.nbra;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (a.bin.row_start[mid] <= qi) lo = mid; else hi = mid;
+        }
+        row = lo;
+      }
+      while (row + 1 < a.bin.nbra && a.bin.row_start[row + 1] <= qi) ++row;
+      const int j = int(qi - a.bin.row_start[row]) + a.bin.row_j0[row];
+      bpair = a.bin.bra_pairs[row];
+      kpair = a.bin.ket_pairs[j];
+      flags = (a.pair_swap[bpair] ? 1 : 0) | (a.pair_swap[kpair] ? 2 : 0);
+    } else {
+      const QuartetItem it = a.items[qi];
+      bpair = it.bra_pair;
+      kpair = it.ket_pair;
+      flags = it.flags;
+      outoff = it.out;
+      orig = it.pad;
+    }
+    RkQuartet q;
+    rk_load(a, bpair, kpair, flags & 1, (flags >> 1) & 1, q);
+    T acc[C::kNacc];
+#pragma unroll
+    for (int i = 0; i < C::kNacc; ++i) acc[i] = T(0);
+    const int nq = q.nbpp * q.nkpp;
+    int kept = 0;
+    const float ACx = float(q.A[0] - q.C[0]), ACy = float(q.A[1] - q.C[1]),
+                ACz = float(q.A[2] - q.C[2]);
+    for (int p = g; p < nq; p += G) {
+      const int ib = p / q.nkpp, ik = p - ib * q.nkpp;
+      bool ok;
+      if constexpr (sizeof(T) == 8) {
+        ok = rk_prim<C>(a, q, ib, ik, acc);
+      } else {
+        ok = rk_prim<C>(a, q, ib, ik, acc, ACx, ACy, ACz);
+      }
+      kept += ok ? 1 : 0;
+    }
+    if (G > 1) {
+      for (int o = G >> 1; o > 0; o >>= 1) {
+#pragma unroll
+        for (int i = 0; i < C::kNacc; ++i) acc[i] += rk_shfl_xor<T>(gmask, acc[i], o, G);
+        kept += __shfl_xor_sync(gmask, kept, o, G);
+      }
+    }
+    if (a.prim_count && g == 0) atomicAdd(a.prim_count, (unsigned long long)kept);
+    if (MODE == kModeStore && a.is_null && g == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
+    if (kept == 0) {
+      if (MODE == kModeSchwarz && g == 0) a.kschwarz[outoff] = 0.0;
+      continue;
+    }
+    const T AB[3] = {T(q.A[0] - q.B[0]), T(q.A[1] - q.B[1]), T(q.A[2] - q.B[2])};
+    const T CD[3] = {T(q.C[0] - q.D[0]), T(q.C[1] - q.D[1]), T(q.C[2] - q.D[2])};
+    T cart[C::kNcart];
+    C::template hrr<T>(acc, AB, CD, cart);
+    T v[C::kNsph];
+    C::template sph<T>(cart, v);
+    if (MODE == kModeSchwarz) {
+      double mx = 0;
+#pragma unroll
+      for (int e = 0; e < C::kNsph; ++e) mx = fmax(mx, fabs(double(v[e])));
+      if (g == 0) a.kschwarz[outoff] = sqrt(mx);
+    } else if (MODE == kModeStore) {
+      const int fl = flags >> 2;
+      const bool sbk = fl & 1, stb = (fl >> 1) & 1, stk = (fl >> 2) & 1;
+      int perm[4];
+      perm[0] = sbk ? (stk ? 3 : 2) : (stb ? 1 : 0);
+      perm[1] = sbk ? (stk ? 2 : 3) : (stb ? 0 : 1);
+      perm[2] = sbk ? (stb ? 1 : 0) : (stk ? 3 : 2);
+      perm[3] = sbk ? (stb ? 0 : 1) : (stk ? 2 : 3);
+      const int dims[4] = {N0, N1, N2, N3};
+      int tn[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) tn[perm[t]] = dims[t];
+      double* o = a.out + outoff;
+#pragma unroll
+      for (int e = 0; e < C::kNsph; ++e) {
+        if ((e & (G - 1)) != g) continue;
+        const int ci[4] = {e / (N1 * N2 * N3), (e / (N2 * N3)) % N1, (e / N3) % N2, e % N3};
+        int it[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) it[perm[t]] = ci[t];
+        o[((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3]] = double(v[e]);
+      }
+    } else if (MODE == kModeJK) {
+      const double deg = (q.sh[0] == q.sh[1] ? 1.0 : 2.0) * (q.sh[2] == q.sh[3] ? 1.0 : 2.0) *
+                         (bpair == kpair ? 1.0 : 2.0);
+      const int nbf = a.nbf;
+      const size_t o0 = a.basis.bf_off[q.sh[0]], o1 = a.basis.bf_off[q.sh[1]];
+      const size_t o2 = a.basis.bf_off[q.sh[2]], o3 = a.basis.bf_off[q.sh[3]];
+      T* tag = nullptr;
+#define V_(i, j, k, l) v[(((i) * N1 + (j)) * N2 + (k)) * N3 + (l)]
+      int slot = 0;
+      // J(a,b) += sum_cd D(c,d) v
+      {
+        T Dcd[N2 * N3];
+#pragma unroll
+        for (int k = 0; k < N2; ++k)
+#pragma unroll
+          for (int l = 0; l < N3; ++l) Dcd[k * N3 + l] = rk_D(a, (o2 + k) * nbf + o3 + l, tag);
+#pragma unroll
+        for (int i = 0; i < N0; ++i)
+#pragma unroll
+          for (int j = 0; j < N1; ++j, ++slot) {
+            T s = 0;
+#pragma unroll
+            for (int k = 0; k < N2; ++k)
+#pragma unroll
+              for (int l = 0; l < N3; ++l) s = fma(Dcd[k * N3 + l], V_(i, j, k, l), s);
+            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o0 + i) * nbf + o1 + j, deg * double(s));
+          }
+      }
+      // J(c,d) += sum_ab D(a,b) v
+      {
+        T Dab[N0 * N1];
+#pragma unroll
+        for (int i = 0; i < N0; ++i)
+#pragma unroll
+          for (int j = 0; j < N1; ++j) Dab[i * N1 + j] = rk_D(a, (o0 + i) * nbf + o1 + j, tag);
+#pragma unroll
+        for (int k = 0; k < N2; ++k)
+#pragma unroll
+          for (int l = 0; l < N3; ++l, ++slot) {
+            T s = 0;
+#pragma unroll
+            for (int i = 0; i < N0; ++i)
+#pragma unroll
+              for (int j = 0; j < N1; ++j) s = fma(Dab[i * N1 + j], V_(i, j, k, l), s);
+            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o2 + k) * nbf + o3 + l, deg * double(s));
+          }
+      }
+      // K(a,c) += sum_bd D(b,d) v ; K(b,d) += sum_ac D(a,c) v
+      {
+        T Dbd[N1 * N3], Dac[N0 * N2];
+#pragma unroll
+        for (int j = 0; j < N1; ++j)
+#pragma unroll
+          for (int l = 0; l < N3; ++l) Dbd[j * N3 + l] = rk_D(a, (o1 + j) * nbf + o3 + l, tag);
+#pragma unroll
+        for (int i = 0; i < N0; ++i)
+#pragma unroll
+          for (int k = 0; k < N2; ++k) Dac[i * N2 + k] = rk_D(a, (o0 + i) * nbf + o2 + k, tag);
+#pragma unroll
+        for (int i = 0; i < N0; ++i)
+#pragma unroll
+          for (int k = 0; k < N2; ++k, ++slot) {
+            T s = 0;
+#pragma unroll
+            for (int j = 0; j < N1; ++j)
+#pragma unroll
+              for (int l = 0; l < N3; ++l) s = fma(Dbd[j * N3 + l], V_(i, j, k, l), s);
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o0 + i) * nbf + o2 + k, deg * double(s));
+          }
+#pragma unroll
+        for (int j = 0; j < N1; ++j)
+#pragma unroll
+          for (int l = 0; l < N3; ++l, ++slot) {
+            T s = 0;
+#pragma unroll
+            for (int i = 0; i < N0; ++i)
+#pragma unroll
+              for (int k = 0; k < N2; ++k) s = fma(Dac[i * N2 + k], V_(i, j, k, l), s);
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o1 + j) * nbf + o3 + l, deg * double(s));
+          }
+      }
+      // K(a,d) += sum_bc D(b,c) v ; K(b,c) += sum_ad D(a,d) v
+      {
+        T Dbc[N1 * N2], Dad[N0 * N3];
+#pragma unroll
+        for (int j = 0; j < N1; ++j)
+#pragma unroll
+          for (int k = 0; k < N2; ++k) Dbc[j * N2 + k] = rk_D(a, (o1 + j) * nbf + o2 + k, tag);
+#pragma unroll
+        for (int i = 0; i < N0; ++i)
+#pragma unroll
+          for (int l = 0; l < N3; ++l) Dad[i * N3 + l] = rk_D(a, (o0 + i) * nbf + o3 + l, tag);
+#pragma unroll
+        for (int i = 0; i < N0; ++i)
+#pragma unroll
+          for (int l = 0; l < N3; ++l, ++slot) {
+            T s = 0;
+#pragma unroll
+            for (int j = 0; j < N1; ++j)
+#pragma unroll
+              for (int k = 0; k < N2; ++k) s = fma(Dbc[j * N2 + k], V_(i, j, k, l), s);
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o0 + i) * nbf + o3 + l, deg * double(s));
+          }
+#pragma unroll
+        for (int j = 0; j < N1; ++j)
+#pragma unroll
+          for (int k = 0; k < N2; ++k, ++slot) {
+            T s = 0;
+#pragma unroll
+            for (int i = 0; i < N0; ++i)
+#pragma unroll
+              for (int l = 0; l < N3; ++l) s = fma(Dad[i * N3 + l], V_(i, j, k, l), s);
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o1 + j) * nbf + o2 + k, deg * double(s));
+          }
+      }
+#undef V_
+    }
+  }
+}
+
+}  // namespace lgx
