@@ -153,6 +153,29 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ,
                          double* dK, double schwarz_thresh, int mode,
                          double mixed_thresh, lgx_jk_stats* stats);
 
+/* No counterpart in the reference.  lgx_jk_device for callers that must not
+ * allocate device memory while they run: code inside a region where
+ * cudaMalloc is not allowed or would stall (for example while another
+ * component, such as a framework's caching allocator, owns all device
+ * memory), or pipelines that budget device memory up front.  The call makes
+ * no cudaMalloc / cudaFree / allocating-library call: its J/K accumulators
+ * and the FP32 copy of D live in one file-scope __device__ array of the
+ * library, sized for nbf <= LGX_NOALLOC_MAX_NBF (768 functions: 11.25 MiB,
+ * held by every GPU that loads the library until the process exits); a
+ * larger basis returns LGX_ERR_TOO_LARGE.  The context's basis state (pair
+ * data, Schwarz factors, quartet bins, class programs) must already exist
+ * for the same schwarz_thresh / mode / mixed_thresh, i.e. after one
+ * lgx_jk_device or lgx_jk call; otherwise LGX_ERR_INVALID_ARG.  The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the one array and overwrites it (the accumulators are
+ * cleared at the start of each call), so calls that overlap on the GPU
+ * (two threads or contexts on one device at once) race. */
+#define LGX_NOALLOC_MAX_NBF 768
+lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
+                                 double* dK, double schwarz_thresh, int mode,
+                                 double mixed_thresh, lgx_jk_stats* stats);
+
 /* Nuclear gradients of E_J = 1/2 sum D.J and E_K = -1/4 sum D.K from
  * deriv_order = 1 integrals (compute_2body_fock_deriv<1>,
  * hartree-fock++.cc:1776-2000, per-atom digestion :1909-1973).

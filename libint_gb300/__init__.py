@@ -323,6 +323,18 @@ class Context:
         self._check(st, "lgx_jk_device")
         return stats
 
+    def jk_device_noalloc(self, dD, dJ, dK, schwarz_thresh=1e-12, mode=_lgx.LGX_FP64,
+                          mixed_thresh=1e-4):
+        """jk_device without device allocation during the call (see
+        lgx_jk_device_noalloc in include/lgx.h for the limits and the
+        preparation it needs)."""
+        stats = _lgx.LgxJkStats()
+        st = self._lib.lgx_jk_device_noalloc(self._h, ctypes.c_void_p(dD), ctypes.c_void_p(dJ),
+                                             ctypes.c_void_p(dK), float(schwarz_thresh),
+                                             int(mode), float(mixed_thresh), ctypes.byref(stats))
+        self._check(st, "lgx_jk_device_noalloc")
+        return stats
+
     def jk_grad(self, D, natoms=None, schwarz_thresh=1e-12):
         if natoms is None:
             natoms = int(max(self.basis.atom_of_shell)) + 1

@@ -21,6 +21,7 @@ LGX_ERR_NO_DEVICE = 7
 
 LGX_FP64 = 0
 LGX_MIXED = 1
+LGX_NOALLOC_MAX_NBF = 768
 LGX_SCREEN_ORIGINAL = 0
 LGX_SCREEN_CONSERVATIVE = 1
 
@@ -67,6 +68,9 @@ SIGNATURES = {
     "lgx_jk_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                      ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
+    "lgx_jk_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
     "lgx_jk_grad": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int,
                                    ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
     "lgx_shell_normalize": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),

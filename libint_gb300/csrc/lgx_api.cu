@@ -151,6 +151,7 @@ struct lgx_context {
   DBuf boys, boys32, sph, Df;
   std::map<int, std::unique_ptr<ProgDev>> progs;
   bool use_rk = true;  // register kernels for the small classes
+  bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
   BasisDev basis, small;
   DBuf gscratch, counter, errflag, primcount;
   DBuf items, out, isnull;
@@ -263,6 +264,9 @@ lgx_status get_prog(lgx_context* ctx, int la, int lb, int lc, int ld, int deriv,
     *out = it->second.get();
     return LGX_OK;
   }
+  if (ctx->noalloc)
+    return fail(ctx, LGX_ERR_INVALID_ARG,
+                "class program not prepared: call lgx_jk_device once with the same settings");
   auto pd = std::make_unique<ProgDev>();
   try {
     pd->host = build_class_program(la, lb, lc, ld, deriv);
@@ -456,7 +460,14 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
     const size_t per_block = size_t(L.wpb) * slot_bytes;
     const size_t cap = size_t(2) << 30;  // 2 GiB of per-warp slot scratch at most
     grid = std::min<long long>(grid, std::max<size_t>(1, cap / per_block));
-    CK(ctx->gscratch.ensure(size_t(grid) * per_block));
+    if (ctx->noalloc) {  // use the slot scratch a previous pass left, never grow it
+      if (ctx->gscratch.n < per_block)
+        return fail(ctx, LGX_ERR_INVALID_ARG,
+                    "slot scratch not prepared: call lgx_jk_device once with the same settings");
+      grid = std::min<long long>(grid, (long long)(ctx->gscratch.n / per_block));
+    } else {
+      CK(ctx->gscratch.ensure(size_t(grid) * per_block));
+    }
   }
   L.grid = int(grid);
   return LGX_OK;
@@ -814,8 +825,11 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
                     EriArgs base, lgx_jk_stats* stats) {
   BinCache& C = ctx->bins;
   const size_t nslots = 2 * C.bins.size() + 1;
-  CK(ctx->primcount.ensure(nslots * sizeof(unsigned long long)));
-  CK(cudaMemsetAsync(ctx->primcount.p, 0, nslots * sizeof(unsigned long long), ctx->stream));
+  const bool count = !ctx->noalloc || ctx->primcount.n >= nslots * sizeof(unsigned long long);
+  if (count) {
+    CK(ctx->primcount.ensure(nslots * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(ctx->primcount.p, 0, nslots * sizeof(unsigned long long), ctx->stream));
+  }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   long long integrals = 0, launches = 0;
   struct Rec { int bin, sp; bool fp32; };
@@ -836,7 +850,7 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       a.bin.row_j0 = bin.row_j0[sp].as<int>();
       a.bin.nbra = bin.nbra;
       a.bin.total = bin.total[sp];
-      a.prim_count = ctx->primcount.as<unsigned long long>() + 2 * bi + sp;
+      a.prim_count = count ? ctx->primcount.as<unsigned long long>() + 2 * bi + sp : nullptr;
       s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg);
       if (s != LGX_OK) return s;
       integrals += bin.integrals[sp];
@@ -850,9 +864,10 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
     CK(cudaEventSynchronize(ctx->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    std::vector<unsigned long long> pc(nslots);
-    CK(cudaMemcpy(pc.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
-                  cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> pc(nslots, 0);
+    if (count)
+      CK(cudaMemcpy(pc.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost));
     long long prims = 0;
     for (const Rec& r : recs) {
       const BinHost& bin = *C.bins[r.bin];
@@ -1128,6 +1143,99 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   if (s != LGX_OK) return s;
   CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
                         ctx->stream));
+  CK(cudaEventRecord(ctx->ev3, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (stats) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3));
+    stats->pass_ms = ms;
+    stats->launches += 1;
+  }
+  return check_errflag(ctx);
+}
+
+}  // extern "C"
+
+namespace {
+// Scratch of lgx_jk_device_noalloc: J and K accumulators (FP64) and the
+// FP32 copy of D for nbf <= LGX_NOALLOC_MAX_NBF, one array per device that
+// loads the library.  Host code only ever uses its device address, looked
+// up once per device with cudaGetSymbolAddress.
+constexpr size_t kNoAllocN = size_t(LGX_NOALLOC_MAX_NBF) * LGX_NOALLOC_MAX_NBF;
+constexpr size_t kNoAllocBytes = 2 * kNoAllocN * sizeof(double) + kNoAllocN * sizeof(float);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+std::map<int, unsigned char*> g_noalloc_addr;  // device -> address of the array
+
+lgx_status noalloc_scratch(lgx_context* ctx, unsigned char** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  auto it = g_noalloc_addr.find(ctx->device);
+  if (it != g_noalloc_addr.end()) {
+    *out = it->second;
+    return LGX_OK;
+  }
+  void* p = nullptr;
+  CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  g_noalloc_addr[ctx->device] = static_cast<unsigned char*>(p);
+  *out = static_cast<unsigned char*>(p);
+  return LGX_OK;
+}
+
+struct NoAllocGuard {
+  lgx_context* c;
+  explicit NoAllocGuard(lgx_context* ctx) : c(ctx) { c->noalloc = true; }
+  ~NoAllocGuard() { c->noalloc = false; }
+};
+}  // namespace
+
+extern "C" {
+
+lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ, double* dK,
+                                 double thresh, int mode, double mixed, lgx_jk_stats* stats) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!dD || !dJ || !dK) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
+  BasisDev& B = ctx->basis;
+  if (B.nbf > LGX_NOALLOC_MAX_NBF)
+    return fail(ctx, LGX_ERR_TOO_LARGE,
+                "lgx_jk_device_noalloc: nbf = " + std::to_string(B.nbf) +
+                    " exceeds LGX_NOALLOC_MAX_NBF = " + std::to_string(LGX_NOALLOC_MAX_NBF));
+  const double eps = std::numeric_limits<double>::epsilon();
+  const BinCache& C = ctx->bins;
+  const double mixed_key = mode == LGX_MIXED ? mixed : 0.0;
+  if (!B.schwarz_ok || !B.pairs_ok || B.pairs_lnprec != std::log(eps) || B.pairs_method != 0 ||
+      !C.valid || C.thresh != thresh || C.mode != mode || C.mixed != mixed_key)
+    return fail(ctx, LGX_ERR_INVALID_ARG,
+                "lgx_jk_device_noalloc: basis state not prepared for these settings; call "
+                "lgx_jk_device (or lgx_jk) once with the same threshold and mode first");
+  CK(cudaSetDevice(ctx->device));
+  unsigned char* scratch = nullptr;
+  lgx_status s = noalloc_scratch(ctx, &scratch);
+  if (s != LGX_OK) return s;
+  NoAllocGuard guard(ctx);
+  const size_t nn = size_t(B.nbf) * B.nbf;
+  double* Jacc = reinterpret_cast<double*>(scratch);
+  double* Kacc = Jacc + kNoAllocN;
+  float* Df = reinterpret_cast<float*>(Kacc + kNoAllocN);
+  CK(cudaEventRecord(ctx->ev2, ctx->stream));
+  CK(cudaMemsetAsync(Jacc, 0, nn * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(Kacc, 0, nn * sizeof(double), ctx->stream));
+  if (mode == LGX_MIXED) CK(launch_d2f(dD, Df, (long long)nn, ctx->stream));
+  EriArgs a{};
+  a.precision = eps;
+  a.ln_prec = std::log(eps);
+  a.screening = 0;
+  a.D = dD;
+  a.Df = Df;
+  a.Jacc = Jacc;
+  a.Kacc = Kacc;
+  a.nbf = B.nbf;
+  s = run_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, stats);
+  if (s != LGX_OK) return s;
+  CK(launch_jk_finalize(Jacc, Kacc, dJ, dK, B.nbf, ctx->stream));
   CK(cudaEventRecord(ctx->ev3, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (stats) {
