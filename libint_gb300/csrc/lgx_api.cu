@@ -834,6 +834,10 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
   long long integrals = 0, launches = 0;
   struct Rec { int bin, sp; bool fp32; };
   std::vector<Rec> recs;
+  // LGX_CLASS_PROFILE=1: per-launch device times, printed per class bin
+  // (the counterpart of libint's per-class Engine timers, engine.h:862-890)
+  static const bool prof = getenv("LGX_CLASS_PROFILE") && getenv("LGX_CLASS_PROFILE")[0] == '1';
+  std::vector<cudaEvent_t> pev;
   for (size_t bi = 0; bi < C.bins.size(); ++bi) {
     BinHost& bin = *C.bins[bi];
     ProgDev* P = nullptr;
@@ -851,6 +855,12 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       a.bin.nbra = bin.nbra;
       a.bin.total = bin.total[sp];
       a.prim_count = count ? ctx->primcount.as<unsigned long long>() + 2 * bi + sp : nullptr;
+      if (prof) {
+        cudaEvent_t e0;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventRecord(e0, ctx->stream));
+        pev.push_back(e0);
+      }
       s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg);
       if (s != LGX_OK) return s;
       integrals += bin.integrals[sp];
@@ -859,6 +869,25 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
     }
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (prof) {
+    CK(cudaEventSynchronize(ctx->ev1));
+    std::vector<unsigned long long> pcp(nslots, 0);
+    if (count)
+      CK(cudaMemcpy(pcp.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < recs.size(); ++i) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, pev[i], i + 1 < pev.size() ? pev[i + 1] : ctx->ev1));
+      const BinHost& bin = *C.bins[recs[i].bin];
+      ProgDev* P = nullptr;
+      get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
+      const bool rk = rk_eligible(ctx, B, *P, mode) && !(recs[i].fp32 && mode == kModeSchwarz);
+      fprintf(stderr, "lgx-class (%d%d|%d%d) %s %s quartets %lld prims %llu nq_avg %.1f  %.3f ms\n",
+              bin.la, bin.lb, bin.lc, bin.ld, recs[i].fp32 ? "fp32" : "fp64", rk ? "rk" : "prog",
+              (long long)bin.total[recs[i].sp], pcp[2 * recs[i].bin + recs[i].sp], bin.nq_avg, ms);
+      cudaEventDestroy(pev[i]);
+    }
+  }
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     CK(cudaEventSynchronize(ctx->ev1));

@@ -1,0 +1,151 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own
+code, compiled in place by oracle/ref/build_ref.sh into oracle/_ref/libref.so
+(libint2::Shell::renorm, SolidHarmonicsCoefficients::coeff,
+FmEval_Reference2, BasisSet, DerivMapGenerator and the brute-force ERI of
+src/bin/test_eri/eri.h).  Run in the development container, where the
+reference tree exists:
+
+    python tests/golden/make_golden.py
+
+Outputs (numpy .npz, committed):
+  boys.npz        F_m(T) from FmEval_Reference2 and FmEval_Reference<long double>
+  solid.npz       solid-harmonic coefficients, l <= 4
+  shells.npz      normalized coefficients of random shells (Shell::renorm)
+  basis.npz       BasisSet("cc-pVDZ"/"cc-pVTZ") for one water
+  derivmap.npz    first-derivative shell-set order and bra/ket-swap map
+  eri.npz         brute-force contracted shell sets, d0 and d1, many classes
+"""
+import ctypes
+import itertools
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+
+P = lambda a, t=ctypes.c_double: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+
+
+def main():
+    oracle.build_ref()
+    ref = oracle.ref_lib()
+    assert ref is not None, "reference build missing"
+    rng = np.random.default_rng(20240601)
+
+    # Boys
+    T = np.concatenate([np.linspace(0, 40, 801), [45, 60, 80, 117, 118, 150, 300, 1000]])
+    mmax = 16
+    F2 = np.zeros((len(T), mmax + 1))
+    Fld = np.zeros((len(T), mmax + 1))
+    for i, t in enumerate(T):
+        ref.ref_boys_reference2(float(t), mmax, P(F2[i]))
+        if t < 117:
+            ref.ref_boys_reference_ld(float(t), mmax, P(Fld[i]))
+        else:
+            Fld[i] = F2[i]
+    np.savez_compressed(os.path.join(HERE, "boys.npz"), T=T, F_ref2=F2, F_refld=Fld)
+
+    # solid harmonics
+    rows = []
+    for l in range(5):
+        for m in range(-l, l + 1):
+            for lx in range(l, -1, -1):
+                for ly in range(l - lx, -1, -1):
+                    rows.append((l, m, lx, ly, l - lx - ly,
+                                 ref.ref_solid_coeff(l, m, lx, ly, l - lx - ly)))
+    rows = np.array(rows)
+    np.savez_compressed(os.path.join(HERE, "solid.npz"), idx=rows[:, :5].astype(np.int32),
+                        coeff=rows[:, 5])
+
+    # shell normalization
+    L, A, Cin, Cout = [], [], [], []
+    for k in range(40):
+        l = k % 5
+        n = 1 + k % 4
+        a = np.sort(rng.uniform(0.05, 50.0, n))[::-1].copy()
+        c = rng.uniform(-1, 1, n)
+        co = np.zeros(n)
+        ml = np.zeros(n)
+        ref.ref_shell_normalize(l, 0, n, P(a), P(c), P(co), P(ml))
+        L.append(l); A.append(a); Cin.append(c); Cout.append(co)
+    np.savez_compressed(os.path.join(HERE, "shells.npz"), l=np.array(L, np.int32),
+                        alpha=np.array(A, dtype=object), cin=np.array(Cin, dtype=object),
+                        cout=np.array(Cout, dtype=object), allow_pickle=True)
+
+    # BasisSet for one water (bohr)
+    Z = np.array([8, 1, 1], np.int32)
+    xyz = np.array([0.0, -0.143, 0.0, 1.638, 1.136, 0.0, -1.638, 1.136, 0.0])
+    out = {"Z": Z, "xyz": xyz}
+    for name in ("cc-pVDZ", "cc-pVTZ"):
+        ns = ref.ref_basis(name.encode(), 3, P(Z, ctypes.c_int), P(xyz), None, None, None,
+                           None, None, None, 0)
+        l = np.zeros(ns, np.int32); pure = np.zeros(ns, np.int32); npr = np.zeros(ns, np.int32)
+        O = np.zeros(3 * ns); al = np.zeros(400); co = np.zeros(400)
+        ref.ref_basis(name.encode(), 3, P(Z, ctypes.c_int), P(xyz), P(l, ctypes.c_int),
+                      P(pure, ctypes.c_int), P(npr, ctypes.c_int), P(O), P(al), P(co), 400)
+        m = int(npr.sum())
+        key = name.lower().replace("-", "")
+        out[key + "_l"] = l; out[key + "_pure"] = pure; out[key + "_nprim"] = npr
+        out[key + "_O"] = O; out[key + "_alpha"] = al[:m]; out[key + "_coeff"] = co[:m]
+    np.savez_compressed(os.path.join(HERE, "basis.npz"), **out)
+
+    # derivative order and map
+    order = np.zeros(12, np.int32)
+    ref.ref_deriv_order1(P(order, ctypes.c_int))
+    dmap = np.zeros((2, 2, 2, 12), np.int32)
+    for a, b, c, s in itertools.product(range(2), range(2), range(2), range(12)):
+        dmap[a, b, c, s] = ref.ref_deriv_map1(a, b, c, s)
+    np.savez_compressed(os.path.join(HERE, "derivmap.npz"), order=order, map=dmap)
+
+    # brute-force shell sets
+    cases = []
+    for ls in itertools.product(range(4), repeat=4):
+        cases.append((ls, 0))
+    for ls in itertools.product(range(3), repeat=4):
+        if sum(ls) <= 5:
+            cases.append((ls, 1))
+    recs = {"l": [], "pure": [], "nprim": [], "alpha": [], "coeff": [], "O": [], "deriv": [],
+            "values": [], "offset": []}
+    off = 0
+    vals = []
+    for ls, d in cases:
+        shells = []
+        for k, l in enumerate(ls):
+            n = 1 if (l == 3 or sum(ls) > 7) else (2 if l > 0 else 3)
+            a = np.sort(rng.uniform(0.15, 5.0, n))[::-1].copy()
+            c = rng.uniform(0.2, 1.0, n)
+            cn, _ = oracle.shell_normalize(l, a, c)
+            pure = 1 if l > 1 else 0
+            shells.append((l, pure, a, cn, rng.uniform(-1.2, 1.2, 3)))
+        r = oracle.ref_eri_shellset(ref, shells, d)
+        v = np.concatenate([x.reshape(-1) for x in r])
+        recs["l"].append(ls); recs["pure"].append([s[1] for s in shells])
+        recs["nprim"].append([len(s[2]) for s in shells])
+        recs["alpha"].append(np.concatenate([s[2] for s in shells]))
+        recs["coeff"].append(np.concatenate([s[3] for s in shells]))
+        recs["O"].append(np.concatenate([s[4] for s in shells]))
+        recs["deriv"].append(d)
+        recs["offset"].append(off)
+        vals.append(v)
+        off += v.size
+    maxp = max(len(a) for a in recs["alpha"])
+    alpha = np.zeros((len(cases), maxp)); coeff = np.zeros((len(cases), maxp))
+    for i in range(len(cases)):
+        alpha[i, :len(recs["alpha"][i])] = recs["alpha"][i]
+        coeff[i, :len(recs["coeff"][i])] = recs["coeff"][i]
+    np.savez_compressed(os.path.join(HERE, "eri.npz"), l=np.array(recs["l"], np.int32),
+                        pure=np.array(recs["pure"], np.int32),
+                        nprim=np.array(recs["nprim"], np.int32), alpha=alpha, coeff=coeff,
+                        O=np.array(recs["O"]), deriv=np.array(recs["deriv"], np.int32),
+                        offset=np.array(recs["offset"], np.int64),
+                        values=np.concatenate(vals))
+    print("cases", len(cases), "values", off)
+
+
+if __name__ == "__main__":
+    main()

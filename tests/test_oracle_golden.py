@@ -1,0 +1,61 @@
+"""The CPU oracle against golden fixtures produced by the reference's own
+code (brute-force ERIs of src/bin/test_eri/eri.h, FmEval_Reference2,
+Shell::renorm, SolidHarmonicsCoefficients, DerivMapGenerator).  Thresholds
+follow tests/unit/test-2body.cc:304-322: absolute 5e-14 or relative 1e-9,
+tightened to a plain 1e-12 absolute (the parity bar of this project)."""
+import numpy as np
+
+from golden_util import eri_cases, load
+
+
+def test_boys_vs_reference(oracle_mod):
+    g = load("boys.npz")
+    worst = 0.0
+    for T, ref in zip(g["T"], g["F_refld"]):
+        F = oracle_mod.boys(float(T), len(ref) - 1)
+        worst = max(worst, float(np.max(np.abs(F - ref))))
+    assert worst < 1e-14, worst
+
+
+def test_solid_harmonics_vs_reference(oracle_mod):
+    g = load("solid.npz")
+    for (l, m, lx, ly, lz), c in zip(g["idx"], g["coeff"]):
+        assert abs(oracle_mod.solid_coeff(int(l), int(m), int(lx), int(ly), int(lz)) - c) < 1e-13
+
+
+def test_shell_normalization_vs_reference(oracle_mod):
+    g = load("shells.npz")
+    for l, a, cin, cout in zip(g["l"], g["alpha"], g["cin"], g["cout"]):
+        c, _ = oracle_mod.shell_normalize(int(l), a, cin)
+        np.testing.assert_allclose(c, cout, rtol=1e-13, atol=0)
+
+
+def test_eri_shellsets_vs_reference_bruteforce(oracle_mod):
+    worst = 0.0
+    for l, pure, nprim, alpha, coeff, O, deriv, vals in eri_cases():
+        ob = oracle_mod.OracleBasis(l, pure, nprim, O, alpha, coeff)
+        r = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, deriv, precision=0.0)
+        got = np.concatenate([x.reshape(-1) for x in r])
+        err = float(np.max(np.abs(got - vals)))
+        worst = max(worst, err)
+        assert err < 1e-12, (tuple(l), deriv, err)
+    print("worst", worst)
+
+
+def test_derivative_order_and_map(oracle_mod):
+    g = load("derivmap.npz")
+    # sets ordered A_x, A_y, A_z, B_x, ..., D_z
+    assert list(g["order"]) == list(range(12))
+    # the remap used by the oracle/kernels: canonical centre k -> target
+    # centre perm[k] (engine.impl.h:1181-1211 swaps)
+    for sbk in range(2):
+        for stb in range(2):
+            for stk in range(2):
+                perm = [
+                    (3 if stk else 2) if sbk else (1 if stb else 0),
+                    (2 if stk else 3) if sbk else (0 if stb else 1),
+                    (1 if stb else 0) if sbk else (3 if stk else 2),
+                    (0 if stb else 1) if sbk else (2 if stk else 3),
+                ]
+                for s in range(12):
+                    assert g["map"][sbk, stb, stk, s] == perm[s // 3] * 3 + s % 3
