@@ -1,0 +1,259 @@
+// libint2::Engine (Operator::coulomb, BraKet::xx_xx, deriv_order 0/1) as a
+// drop-in over liblgx (include/lgx.h).
+//
+// Names and signatures follow the reference's engine.h:444-1064 for this
+// path: Engine(Operator, max_nprim, max_l, deriv_order, precision, params,
+// braket, screening); compute(s1,s2,s3,s4); compute2<op,braket,deriv>(...);
+// results(), nshellsets(), set_precision(), precision(), set(...);
+// exceptions lmax_exceeded / using_default_initialized.  compute() returns
+// results(): nshellsets() pointers to row-major shell sets in the caller's
+// shell order, valid until the next compute on this Engine; results()[0] is
+// nullptr when every primitive quartet was screened out
+// (engine.impl.h:1781-1784).  The arithmetic runs on the GPU context
+// created by libint2::initialize().
+#ifndef LGX_LIBINT2_ENGINE_H
+#define LGX_LIBINT2_ENGINE_H
+
+#include <array>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../lgx.h"
+#include "shell.h"
+
+namespace libint2 {
+
+/// Operator enum of the reference (engine.h:98-184); only coulomb is served.
+enum class Operator {
+  overlap = 0,
+  kinetic,
+  nuclear,
+  erf_nuclear,
+  erfc_nuclear,
+  emultipole1,
+  emultipole2,
+  emultipole3,
+  sphemultipole,
+  opVop,
+  delta,
+  coulomb,
+  cgtg,
+  cgtg_x_coulomb,
+  delcgtg2,
+  r12,
+  erf_coulomb,
+  erfc_coulomb,
+  stg,
+  stg_x_coulomb,
+  invalid = -1,
+  first_2body_oper = delta,
+  last_2body_oper = stg_x_coulomb
+};
+
+/// BraKet enum (engine.h:188-206); only xx_xx is served.
+enum class BraKet { x_x = 0, xx_xx, xs_xx, xx_xs, xs_xs, invalid = -1 };
+
+enum class CartesianShellNormalization { standard, uniform };
+
+constexpr size_t num_geometrical_derivatives(size_t ncenter, size_t deriv_order) {
+  return deriv_order > 0 ? (num_geometrical_derivatives(ncenter, deriv_order - 1) *
+                            (3 * ncenter + deriv_order - 1)) /
+                               deriv_order
+                         : 1;
+}
+
+namespace detail {
+struct Runtime {
+  std::mutex mu;
+  lgx_context* ctx = nullptr;
+  int device = 0;
+};
+inline Runtime& runtime() {
+  static Runtime r;
+  return r;
+}
+}  // namespace detail
+
+/// libint2::initialize() (initialize.h:76-95): creates the GPU context.
+inline void initialize(bool /*verbose*/ = false) {
+  auto& r = detail::runtime();
+  std::lock_guard<std::mutex> lk(r.mu);
+  if (!r.ctx) {
+    if (lgx_create(&r.ctx, r.device) != LGX_OK)
+      throw std::runtime_error("libint2::initialize: no usable GB300 / sm_100+ CUDA device");
+  }
+}
+inline bool initialized() { return detail::runtime().ctx != nullptr; }
+/// libint2::finalize(): releases the GPU context.
+inline void finalize() {
+  auto& r = detail::runtime();
+  std::lock_guard<std::mutex> lk(r.mu);
+  if (r.ctx) lgx_destroy(r.ctx);
+  r.ctx = nullptr;
+}
+
+class Engine {
+ public:
+  typedef double value_type;
+  typedef double scalar_type;
+  typedef std::vector<const value_type*> target_ptr_vec;
+  static constexpr auto max_ntargets = 12;
+
+  /// thrown when max_l exceeds LGX_MAX_L (engine.h:893-905)
+  struct lmax_exceeded : public std::logic_error {
+    lmax_exceeded(const char* task_name, size_t lmax_limit, size_t lmax_requested)
+        : std::logic_error("Engine::lmax_exceeded"),
+          task_name_(task_name),
+          lmax_limit_(lmax_limit),
+          lmax_requested_(lmax_requested) {}
+    const char* task_name() const { return task_name_.c_str(); }
+    size_t lmax_limit() const { return lmax_limit_; }
+    size_t lmax_requested() const { return lmax_requested_; }
+   private:
+    std::string task_name_;
+    size_t lmax_limit_, lmax_requested_;
+  };
+  /// thrown when using a default-initialized Engine (engine.h:907-913)
+  struct using_default_initialized : public std::logic_error {
+    using_default_initialized()
+        : std::logic_error("Engine is default-initialized: use the full constructor") {}
+  };
+
+  Engine() = default;
+  Engine(Operator oper, size_t max_nprim, int max_l, int deriv_order = 0,
+         scalar_type precision = std::numeric_limits<scalar_type>::epsilon(),
+         std::nullptr_t /*params*/ = nullptr, BraKet braket = BraKet::invalid,
+         ScreeningMethod screening = default_screening_method())
+      : oper_(oper),
+        braket_(braket == BraKet::invalid ? BraKet::xx_xx : braket),
+        max_nprim_(max_nprim),
+        lmax_(max_l),
+        deriv_order_(deriv_order),
+        screening_(screening) {
+    if (oper_ != Operator::coulomb || braket_ != BraKet::xx_xx)
+      throw std::invalid_argument(
+          "libint2::Engine (GB300): only Operator::coulomb with BraKet::xx_xx is implemented");
+    if (max_l < 0 || max_l > LGX_MAX_L) throw lmax_exceeded("eri", LGX_MAX_L, max_l);
+    if (deriv_order < 0 || deriv_order > LGX_MAX_DERIV)
+      throw std::invalid_argument("libint2::Engine (GB300): deriv_order must be 0 or 1");
+    set_precision(precision);
+    if (!initialized()) initialize();
+    targets_.assign(nshellsets(), nullptr);
+    initialized_ = true;
+  }
+
+  Operator oper() const { return oper_; }
+  BraKet braket() const { return braket_; }
+  int deriv_order() const { return deriv_order_; }
+  unsigned int nshellsets() const {
+    return unsigned(num_geometrical_derivatives(4, size_t(deriv_order_)));
+  }
+  const target_ptr_vec& results() const { return targets_; }
+
+  Engine& set_precision(scalar_type prec) {
+    if (prec <= 0.) {
+      precision_ = 0.;
+      ln_precision_ = std::numeric_limits<scalar_type>::lowest();
+    } else {
+      precision_ = prec;
+      ln_precision_ = std::log(prec);
+    }
+    return *this;
+  }
+  scalar_type precision() const { return precision_; }
+  Engine& set(ScreeningMethod m) {
+    screening_ = m;
+    return *this;
+  }
+  Engine& set(CartesianShellNormalization n) {
+    if (n != CartesianShellNormalization::standard)
+      throw std::invalid_argument("libint2::Engine (GB300): only standard normalization");
+    return *this;
+  }
+  ScreeningMethod screening_method() const { return screening_; }
+  Engine& set_max_nprim(size_t n) {
+    max_nprim_ = n;
+    return *this;
+  }
+  Engine& set_max_l(int L) {
+    if (L > LGX_MAX_L) throw lmax_exceeded("eri", LGX_MAX_L, L);
+    lmax_ = L;
+    return *this;
+  }
+
+  /// Engine::compute (engine.impl.h:140-175)
+  const target_ptr_vec& compute(const Shell& s1, const Shell& s2, const Shell& s3,
+                                const Shell& s4) {
+    return compute_impl(s1, s2, s3, s4);
+  }
+  /// Engine::compute2<op, braket, deriv> (engine.h:787-791); the optional
+  /// ShellPair data is not needed by the GPU path.
+  template <Operator op, BraKet bk, size_t deriv>
+  const target_ptr_vec& compute2(const Shell& s1, const Shell& s2, const Shell& s3,
+                                 const Shell& s4, const ShellPair* = nullptr,
+                                 const ShellPair* = nullptr) {
+    static_assert(op == Operator::coulomb && bk == BraKet::xx_xx,
+                  "only coulomb / xx_xx is implemented on the GPU path");
+    if (int(deriv) != deriv_order_)
+      throw std::invalid_argument("Engine::compute2: deriv_order mismatch");
+    return compute_impl(s1, s2, s3, s4);
+  }
+
+ private:
+  Operator oper_ = Operator::invalid;
+  BraKet braket_ = BraKet::invalid;
+  size_t max_nprim_ = 0;
+  int lmax_ = -1;
+  int deriv_order_ = 0;
+  scalar_type precision_ = 0, ln_precision_ = 0;
+  ScreeningMethod screening_ = ScreeningMethod::Original;
+  bool initialized_ = false;
+  std::vector<value_type> buf_;
+  target_ptr_vec targets_;
+
+  const target_ptr_vec& compute_impl(const Shell& s1, const Shell& s2, const Shell& s3,
+                                     const Shell& s4) {
+    if (!initialized_) throw using_default_initialized();
+    const Shell* sh[4] = {&s1, &s2, &s3, &s4};
+    lgx_shell d[4];
+    size_t nv = 1;
+    for (int k = 0; k < 4; ++k) {
+      if (sh[k]->ncontr() != 1)
+        throw std::invalid_argument("generally-contracted shells are not yet supported");
+      const int l = sh[k]->contr[0].l;
+      if (l > lmax_) throw lmax_exceeded("eri", size_t(lmax_), size_t(l));
+      d[k].l = l;
+      d[k].pure = sh[k]->contr[0].pure ? 1 : 0;
+      d[k].nprim = int(sh[k]->nprim());
+      d[k].pad_ = 0;
+      for (int x = 0; x < 3; ++x) d[k].origin[x] = sh[k]->O[x];
+      d[k].alpha = sh[k]->alpha.data();
+      d[k].coeff = sh[k]->contr[0].coeff.data();
+      nv *= sh[k]->size();
+    }
+    const unsigned ns = nshellsets();
+    buf_.resize(nv * ns);
+    int nsets = 0, nvalues = 0, is_null = 0;
+    const int method =
+        screening_ == ScreeningMethod::Conservative ? LGX_SCREEN_CONSERVATIVE : LGX_SCREEN_ORIGINAL;
+    auto& rt = detail::runtime();
+    const lgx_status st = lgx_compute_shellset(rt.ctx, d, deriv_order_, precision_, method,
+                                               buf_.data(), buf_.size(), &nsets, &nvalues,
+                                               &is_null);
+    if (st == LGX_ERR_LMAX_EXCEEDED) throw lmax_exceeded("eri", LGX_MAX_L, size_t(lmax_));
+    if (st != LGX_OK)
+      throw std::runtime_error(std::string("libint2::Engine::compute: ") + lgx_last_error(rt.ctx));
+    targets_.assign(ns, nullptr);
+    if (is_null) return targets_;
+    for (unsigned s = 0; s < ns; ++s) targets_[s] = buf_.data() + size_t(s) * nv;
+    return targets_;
+  }
+};
+
+}  // namespace libint2
+
+#endif

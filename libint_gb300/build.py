@@ -18,8 +18,7 @@ BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liblgx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu", "lgx_rk_f64_jk.cu", "lgx_rk_f64_store.cu",
-                "lgx_rk_f32.cu"]
+CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu"]
 CXX_SOURCES = ["lgx_program.cpp", "lgx_host.cpp"]
 
 
@@ -30,14 +29,16 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblgx")
 
 
-def _generate() -> None:
-    """Regenerates the unrolled per-class code (no-op when unchanged)."""
+def _generate() -> list:
+    """Regenerates the unrolled per-class code (files are rewritten only when
+    their content changes); returns the generated CUDA units (csrc/gen)."""
     sys.path.insert(0, os.path.join(PKG_DIR, "codegen"))
     try:
         import gen_rk
-        gen_rk.main()
+        units = gen_rk.main()
     finally:
         sys.path.pop(0)
+    return [os.path.join("gen", u) for u in units]
 
 
 def _deps_mtime() -> float:
@@ -52,15 +53,15 @@ def _deps_mtime() -> float:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    _generate()
+    cuda_sources = CUDA_SOURCES + _generate()
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) >= _deps_mtime()):
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
-    for src in CUDA_SOURCES:
-        obj = os.path.join(BUILD_DIR, src + ".o")
+    for src in cuda_sources:
+        obj = os.path.join(BUILD_DIR, src.replace("/", "_") + ".o")
         jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17",
                      "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
                      "-c", os.path.join(CSRC, src), "-o", obj])
@@ -69,17 +70,30 @@ def build(force: bool = False, verbose: bool = False) -> str:
         jobs.append(["g++", "-std=c++17", "-O3", "-fPIC", "-c",
                      os.path.join(CSRC, src), "-o", obj])
 
+    # skip objects newer than their source and every header
+    hdr = 0.0
+    for d in (CSRC, os.path.join(CSRC, "gen"), os.path.join(ROOT, "include")):
+        for f in os.listdir(d):
+            if f.endswith((".h", ".cuh", ".hpp")):
+                hdr = max(hdr, os.path.getmtime(os.path.join(d, f)))
+    if not force:
+        jobs = [j for j in jobs if not (os.path.exists(j[-1]) and os.path.getmtime(j[-1]) >=
+                                        max(hdr, os.path.getmtime(j[-3])))]
+
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
         return r.stdout + r.stderr
 
-    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+    # biggest units first so the parallel build ends evenly
+    jobs.sort(key=lambda j: -os.path.getsize(j[-3]))
+    workers = max(2, min(max(len(jobs), 1), os.cpu_count() or 4))
+    with ThreadPoolExecutor(max_workers=workers) as ex:
         logs = list(ex.map(run, jobs))
     if verbose:
         print("".join(logs))
-    objs = [os.path.join(BUILD_DIR, s + ".o") for s in CUDA_SOURCES + CXX_SOURCES]
+    objs = [os.path.join(BUILD_DIR, s.replace("/", "_") + ".o") for s in cuda_sources + CXX_SOURCES]
     tmp = LIB_PATH + ".tmp"
     run([nvcc, *ARCH, "-shared", "-o", tmp, *objs])
     os.replace(tmp, LIB_PATH)

@@ -27,8 +27,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DEFAULT = os.path.join(os.path.dirname(HERE), "csrc", "gen", "rk_classes.cuh")
 
 # classes compiled into register kernels: total angular momentum <= RK_MAX_L
-RK_MAX_L = 4
+# for the J/K digestion kernels, <= RK_MAX_L_STORE for store / Schwarz
+RK_MAX_L = 6
+RK_MAX_L_STORE = 4
 LMAX = 3
+# (precision, mode) variants and the class limit of each
+VARIANTS = [("double", "kModeJK", RK_MAX_L), ("float", "kModeJK", RK_MAX_L),
+            ("double", "kModeStore", RK_MAX_L_STORE), ("double", "kModeSchwarz", RK_MAX_L_STORE),
+            ("float", "kModeStore", RK_MAX_L_STORE)]
+N_UNITS = 24  # instantiation translation units (compiled in parallel)
 
 
 def comps(l):
@@ -49,13 +56,14 @@ def ncart(l):
     return (l + 1) * (l + 2) // 2
 
 
-def rk_classes():
+def rk_classes(lmax_total=None):
+    lmax_total = RK_MAX_L if lmax_total is None else lmax_total
     out = []
     for la in range(LMAX + 1):
         for lb in range(la + 1):
             for lc in range(LMAX + 1):
                 for ld in range(lc + 1):
-                    if la + lb <= lc + ld and la + lb + lc + ld <= RK_MAX_L:
+                    if la + lb <= lc + ld and la + lb + lc + ld <= lmax_total:
                         out.append((la, lb, lc, ld))
     return out
 
@@ -285,6 +293,82 @@ def gen_class(la, lb, lc, ld):
     return "\n".join(s)
 
 
+def _write_if_changed(path, text):
+    if os.path.exists(path) and open(path).read() == text:
+        return
+    with open(path, "w") as f:
+        f.write(text)
+
+
+def _cost(c):
+    la, lb, lc, ld = c
+    return (la + lb + lc + ld + 1) ** 4
+
+
+def write_units(gen_dir):
+    """Instantiation units: each defines the launchers of a share of the
+    (precision, mode, class) kernels; rk_dispatch.cu maps run-time
+    (precision, mode, class) to them.  Returns the unit file names."""
+    items = []
+    for prec, mode, lmax in VARIANTS:
+        for c in rk_classes(lmax):
+            items.append((prec, mode, c))
+    items.sort(key=lambda it: -_cost(it[2]))
+    units = [[] for _ in range(N_UNITS)]
+    load = [0] * N_UNITS
+    for it in items:  # greedy balance by estimated code size
+        k = load.index(min(load))
+        units[k].append(it)
+        load[k] += _cost(it[2])
+    names = []
+    decls = []
+    for k, u in enumerate(units):
+        name = "rk_unit_%02d.cu" % k
+        names.append(name)
+        lines = ["// GENERATED by libint_gb300/codegen/gen_rk.py -- do not edit.",
+                 '#include "../lgx_rk.cuh"', "", "namespace lgx {"]
+        for prec, mode, c in u:
+            fn = "rk_launch_%s_%s_%d%d%d%d" % (prec[0], mode[5:].lower(), *c)
+            decls.append((prec, mode, c, fn))
+            lines.append("cudaError_t %s(const EriArgs& a, long long work, int nsm, "
+                         "cudaStream_t st) {" % fn)
+            lines.append("  return rk_launch_one<%s, %d, %d, %d, %d, %s>(a, work, nsm, st);" %
+                         (prec, *c, mode))
+            lines.append("}")
+        lines.append("}  // namespace lgx")
+        _write_if_changed(os.path.join(gen_dir, name), "\n".join(lines) + "\n")
+    d = ["// GENERATED by libint_gb300/codegen/gen_rk.py -- do not edit.",
+         "// Run-time dispatch of the register kernels.", '#include "../lgx_rk.cuh"', "",
+         "namespace lgx {"]
+    for prec, mode, c, fn in decls:
+        d.append("cudaError_t %s(const EriArgs& a, long long work, int nsm, cudaStream_t st);" % fn)
+    d.append("")
+    d.append("// Launches the register kernel of (precision, mode, class); returns")
+    d.append("// cudaErrorNotSupported when that kernel is not compiled.")
+    d.append("cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, "
+             "const EriArgs& a, long long work, int nsm, cudaStream_t st) {")
+    d.append("  const int key = (((fp32 ? 1 : 0) * 8 + mode) * 4096) + ((la * 8 + lb) * 8 + lc) * 8 + ld;")
+    d.append("  switch (key) {")
+    for prec, mode, c, fn in sorted(decls, key=lambda x: x[3]):
+        mode_id = {"kModeStore": 0, "kModeSchwarz": 1, "kModeJK": 2}[mode]
+        key = (((1 if prec == "float" else 0) * 8 + mode_id) * 4096) + ((c[0] * 8 + c[1]) * 8 + c[2]) * 8 + c[3]
+        d.append("    case %d: return %s(a, work, nsm, st);" % (key, fn))
+    d.append("  }")
+    d.append("  return cudaErrorNotSupported;")
+    d.append("}")
+    d.append("")
+    d.append("bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld) {")
+    d.append("  const int L = la + lb + lc + ld;")
+    d.append("  if (mode == kModeJK) return L <= %d;" % RK_MAX_L)
+    d.append("  if (mode == kModeStore) return L <= %d;" % RK_MAX_L_STORE)
+    d.append("  if (mode == kModeSchwarz) return !fp32 && L <= %d;" % RK_MAX_L_STORE)
+    d.append("  return false;")
+    d.append("}")
+    d.append("}  // namespace lgx")
+    _write_if_changed(os.path.join(gen_dir, "rk_dispatch.cu"), "\n".join(d) + "\n")
+    return names + ["rk_dispatch.cu"]
+
+
 def main(out=OUT_DEFAULT):
     os.makedirs(os.path.dirname(out), exist_ok=True)
     parts = ["// GENERATED by libint_gb300/codegen/gen_rk.py -- do not edit.",
@@ -296,18 +380,12 @@ def main(out=OUT_DEFAULT):
     for c in classes:
         parts.append(gen_class(*c))
         parts.append("")
-    parts.append("#define LGX_RK_CLASS_LIST(X) \\")
-    parts.append(" \\\n".join("  X(%d, %d, %d, %d)" % c for c in classes))
-    parts.append("")
     parts.append("}  // namespace rk")
     parts.append("}  // namespace lgx")
     text = "\n".join(parts) + "\n"
-    if os.path.exists(out) and open(out).read() == text:
-        return out
-    with open(out, "w") as f:
-        f.write(text)
-    return out
+    _write_if_changed(out, text)
+    return write_units(os.path.dirname(out))
 
 
 if __name__ == "__main__":
-    print(main(sys.argv[1] if len(sys.argv) > 1 else OUT_DEFAULT))
+    print("\n".join(main(sys.argv[1] if len(sys.argv) > 1 else OUT_DEFAULT)))

@@ -29,15 +29,9 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
 size_t stage_bytes_per_warp();
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
-#define LGX_DECL_RK(NAME)                                                              \
-  cudaError_t NAME(int la, int lb, int lc, int ld, const EriArgs& a, long long work,    \
-                   int nsm, cudaStream_t st);
-LGX_DECL_RK(rk_launch_f64_jk)
-LGX_DECL_RK(rk_launch_f64_store)
-LGX_DECL_RK(rk_launch_f64_schwarz)
-LGX_DECL_RK(rk_launch_f32_jk)
-LGX_DECL_RK(rk_launch_f32_store)
-#undef LGX_DECL_RK
+cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
+                      long long work, int nsm, cudaStream_t st);
+bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
 }  // namespace lgx
 
 using namespace lgx;
@@ -125,8 +119,8 @@ struct BinHost {
   int bra_class, ket_class;
   long long total[2];   // [0] FP64 space, [1] FP32 space
   long long integrals[2];
-  DBuf row_start[2], row_j0[2];
-  int nbra;
+  DBuf seg_start[2], seg_bra[2], seg_j0[2];
+  int nseg[2];
 };
 
 struct BinCache {
@@ -473,13 +467,13 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
   return LGX_OK;
 }
 
-// Register kernels exist for classes with la+lb+lc+ld <= 4 (deriv 0) and
-// shells with the standard pure flags; everything else runs on the
-// warp-cooperative program kernel.
-bool rk_eligible(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode) {
+// Register kernels exist for the generated classes (deriv 0; see
+// codegen/gen_rk.py for the limits per mode) with the standard pure flags;
+// everything else runs on the warp-cooperative program kernel.
+bool rk_eligible(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode,
+                 bool fp32) {
   if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0) return false;
-  if (P.host.la + P.host.lb + P.host.lc + P.host.ld > 4) return false;
-  return mode == kModeJK || mode == kModeStore || mode == kModeSchwarz;
+  return rk_available(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld);
 }
 
 int choose_group(double nq_avg) {
@@ -498,24 +492,15 @@ lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, boo
   a.boys32 = ctx->boys32.as<float>();
   a.sph = ctx->sph.as<double>();
   a.error_flag = ctx->errflag.as<int>();
-  a.group = choose_group(nq_avg);
-  const int la = P.host.la, lb = P.host.lb, lc = P.host.lc, ld = P.host.ld;
-  cudaError_t e;
-  if (!fp32) {
-    e = mode == kModeJK ? rk_launch_f64_jk(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream)
-        : mode == kModeStore ? rk_launch_f64_store(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream)
-                             : rk_launch_f64_schwarz(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream);
-  } else {
-    e = mode == kModeJK ? rk_launch_f32_jk(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream)
-                        : rk_launch_f32_store(la, lb, lc, ld, a, nwork, ctx->nsm, ctx->stream);
-  }
-  CK(e);
+  a.group = a.implicit ? 1 : choose_group(nq_avg);
+  CK(rk_launch(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, nwork, ctx->nsm,
+               ctx->stream));
   return LGX_OK;
 }
 
 lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
                    EriArgs a, long long nwork, double nq_avg = 1.0) {
-  if (rk_eligible(ctx, B, P, mode) && !(fp32 && mode == kModeSchwarz))
+  if (rk_eligible(ctx, B, P, mode, fp32))
     return run_rk(ctx, B, P, mode, fp32, a, nwork, nq_avg);
   Launch L;
   lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, L);
@@ -698,6 +683,7 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
   const long long npairs = (long long)B.hpairs.size();
   double Kmax = 0;
   for (double k : B.Kpair) Kmax = std::max(Kmax, k);
+  // significant pairs per pair class, ordered by (contraction depth, K desc)
   std::vector<std::vector<int>> lists(10);
   for (long long p = 0; p < npairs; ++p) {
     if (B.Kpair[p] * Kmax < thresh) continue;
@@ -705,9 +691,18 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
     const int lhi = std::max(B.l[s1], B.l[s2]), llo = std::min(B.l[s1], B.l[s2]);
     lists[pair_class(lhi, llo)].push_back(int(p));
   }
-  for (auto& v : lists)
-    std::stable_sort(v.begin(), v.end(),
-                     [&](int a, int b) { return B.Kpair[a] > B.Kpair[b]; });
+  std::vector<std::vector<int>> groups(10);  // group boundaries (depth runs)
+  for (int c = 0; c < 10; ++c) {
+    auto& v = lists[c];
+    std::stable_sort(v.begin(), v.end(), [&](int a, int b) {
+      if (B.hpairs[a].npp != B.hpairs[b].npp) return B.hpairs[a].npp < B.hpairs[b].npp;
+      return B.Kpair[a] > B.Kpair[b];
+    });
+    groups[c].push_back(0);
+    for (size_t i = 1; i < v.size(); ++i)
+      if (B.hpairs[v[i]].npp != B.hpairs[v[i - 1]].npp) groups[c].push_back(int(i));
+    groups[c].push_back(int(v.size()));
+  }
   C.class_off.assign(11, 0);
   std::vector<int> flat;
   for (int c = 0; c < 10; ++c) {
@@ -725,6 +720,10 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
       cls_l[pair_class(lhi, llo)][0] = lhi;
       cls_l[pair_class(lhi, llo)][1] = llo;
     }
+  auto nf_pair = [&](int p) {
+    return (long long)nfunc(B.l[B.hpairs[p].s1], B.pure[B.hpairs[p].s1]) *
+           nfunc(B.l[B.hpairs[p].s2], B.pure[B.hpairs[p].s2]);
+  };
   C.quartets[0] = C.quartets[1] = 0;
   for (int x = 0; x < 10; ++x)
     for (int y = 0; y < 10; ++y) {
@@ -738,55 +737,64 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
       bin->lc = cls_l[y][0]; bin->ld = cls_l[y][1];
       bin->bra_class = x;
       bin->ket_class = y;
-      bin->nbra = int(bra.size());
-      std::vector<long long> rs[2];
-      std::vector<int> j0[2];
-      for (int sp = 0; sp < 2; ++sp) {
-        rs[sp].assign(bra.size() + 1, 0);
-        j0[sp].assign(bra.size(), 0);
-      }
-      // number of kets j (sorted desc) with K_i*K_j >= t
-      auto count_ge = [&](double Ki, double t) -> long long {
+      // kets j in [k0, k1) (one depth group, K desc) with K_i*K_j >= t
+      auto count_ge = [&](double Ki, double t, int k0, int k1) -> int {
         if (Ki <= 0) return 0;
         const double need = t / Ki;
-        long long lo = 0, hi = (long long)ket.size();
+        int lo = k0, hi = k1;
         while (lo < hi) {
-          const long long mid = (lo + hi) / 2;
+          const int mid = (lo + hi) / 2;
           if (B.Kpair[ket[mid]] >= need) lo = mid + 1; else hi = mid;
         }
-        return lo;
+        return lo - k0;
       };
-      for (size_t i = 0; i < bra.size(); ++i) {
-        const double Ki = B.Kpair[bra[i]];
-        long long n = count_ge(Ki, thresh);
-        if (x == y) n = std::min<long long>(n, (long long)i + 1);
-        long long m = n;
-        if (mode == LGX_MIXED) m = std::min(n, count_ge(Ki, mixed));
-        rs[0][i + 1] = rs[0][i] + m;
-        rs[1][i + 1] = rs[1][i] + (n - m);
-        j0[0][i] = 0;
-        j0[1][i] = int(m);
-      }
-      auto nf_pair = [&](int p) {
-        return (long long)nfunc(B.l[B.hpairs[p].s1], B.pure[B.hpairs[p].s1]) *
-               nfunc(B.l[B.hpairs[p].s2], B.pure[B.hpairs[p].s2]);
-      };
+      std::vector<long long> st[2];
+      std::vector<int> sb[2], sj[2];
+      for (int sp = 0; sp < 2; ++sp) st[sp].push_back(0);
+      double nq_sum = 0, nq_w = 0;
+      const auto& gb = groups[x];
+      const auto& gk = groups[y];
+      for (size_t bgi = 0; bgi + 1 < gb.size(); ++bgi)
+        for (size_t kgi = 0; kgi + 1 < gk.size(); ++kgi) {
+          if (x == y && kgi > bgi) continue;  // unique quartets: ket index <= bra index
+          const int k0 = gk[kgi], k1 = gk[kgi + 1];
+          for (int i = gb[bgi]; i < gb[bgi + 1]; ++i) {
+            const double Ki = B.Kpair[bra[i]];
+            int n = count_ge(Ki, thresh, k0, k1);
+            if (x == y && kgi == bgi) n = std::min(n, i - k0 + 1);
+            if (n <= 0) continue;
+            int m = n;
+            if (mode == LGX_MIXED) m = std::min(n, count_ge(Ki, mixed, k0, k1));
+            if (m > 0) {
+              st[0].push_back(st[0].back() + m);
+              sb[0].push_back(i);
+              sj[0].push_back(k0);
+            }
+            if (n - m > 0) {
+              st[1].push_back(st[1].back() + (n - m));
+              sb[1].push_back(i);
+              sj[1].push_back(k0 + m);
+            }
+            nq_sum += double(n) * B.hpairs[bra[i]].npp * B.hpairs[ket[k0]].npp;
+            nq_w += n;
+          }
+        }
+      bin->nq_avg = nq_w > 0 ? nq_sum / nq_w : 1.0;
       const long long nfq = nf_pair(bra[0]) * nf_pair(ket[0]);
-      {
-        double sb = 0, sk = 0;
-        for (int p : bra) sb += B.hpairs[p].npp;
-        for (int p : ket) sk += B.hpairs[p].npp;
-        bin->nq_avg = (sb / bra.size()) * (sk / ket.size());
-      }
       for (int sp = 0; sp < 2; ++sp) {
-        bin->total[sp] = rs[sp].back();
+        bin->nseg[sp] = int(sb[sp].size());
+        bin->total[sp] = st[sp].back();
         bin->integrals[sp] = bin->total[sp] * nfq;
         C.quartets[sp] += bin->total[sp];
-        CK(bin->row_start[sp].ensure(rs[sp].size() * sizeof(long long)));
-        CK(bin->row_j0[sp].ensure(j0[sp].size() * sizeof(int)));
-        CK(cudaMemcpyAsync(bin->row_start[sp].p, rs[sp].data(), rs[sp].size() * sizeof(long long),
+        if (bin->nseg[sp] == 0) continue;
+        CK(bin->seg_start[sp].ensure(st[sp].size() * sizeof(long long)));
+        CK(bin->seg_bra[sp].ensure(sb[sp].size() * sizeof(int)));
+        CK(bin->seg_j0[sp].ensure(sj[sp].size() * sizeof(int)));
+        CK(cudaMemcpyAsync(bin->seg_start[sp].p, st[sp].data(), st[sp].size() * sizeof(long long),
                            cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaMemcpyAsync(bin->row_j0[sp].p, j0[sp].data(), j0[sp].size() * sizeof(int),
+        CK(cudaMemcpyAsync(bin->seg_bra[sp].p, sb[sp].data(), sb[sp].size() * sizeof(int),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(bin->seg_j0[sp].p, sj[sp].data(), sj[sp].size() * sizeof(int),
                            cudaMemcpyHostToDevice, ctx->stream));
       }
       C.bins.push_back(std::move(bin));
@@ -850,9 +858,10 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       a.implicit = 1;
       a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
       a.bin.ket_pairs = C.class_lists.as<int>() + C.class_off[bin.ket_class];
-      a.bin.row_start = bin.row_start[sp].as<long long>();
-      a.bin.row_j0 = bin.row_j0[sp].as<int>();
-      a.bin.nbra = bin.nbra;
+      a.bin.seg_start = bin.seg_start[sp].as<long long>();
+      a.bin.seg_bra = bin.seg_bra[sp].as<int>();
+      a.bin.seg_j0 = bin.seg_j0[sp].as<int>();
+      a.bin.nseg = bin.nseg[sp];
       a.bin.total = bin.total[sp];
       a.prim_count = count ? ctx->primcount.as<unsigned long long>() + 2 * bi + sp : nullptr;
       if (prof) {
@@ -881,7 +890,7 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       const BinHost& bin = *C.bins[recs[i].bin];
       ProgDev* P = nullptr;
       get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
-      const bool rk = rk_eligible(ctx, B, *P, mode) && !(recs[i].fp32 && mode == kModeSchwarz);
+      const bool rk = rk_eligible(ctx, B, *P, mode, recs[i].fp32);
       fprintf(stderr, "lgx-class (%d%d|%d%d) %s %s quartets %lld prims %llu nq_avg %.1f  %.3f ms\n",
               bin.la, bin.lb, bin.lc, bin.ld, recs[i].fp32 ? "fp32" : "fp64", rk ? "rk" : "prog",
               (long long)bin.total[recs[i].sp], pcp[2 * recs[i].bin + recs[i].sp], bin.nq_avg, ms);

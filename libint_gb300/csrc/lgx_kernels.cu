@@ -423,22 +423,15 @@ eri_warp_kernel(EriArgs a) {
     }
     const long long end = min(total, start + (long long)a.chunk);
     // implicit decode state
-    int row = 0;
-    if (a.implicit) {
-      int lo = 0, hi = a.bin.nbra;  // last row with row_start <= start
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (a.bin.row_start[mid] <= start) lo = mid; else hi = mid;
-      }
-      row = lo;
-    }
+    int seg = 0;
+    if (a.implicit) seg = bin_segment(a.bin, start);
     for (long long q = start; q < end; ++q) {
       int bpair, kpair, flags = 0, orig = 0;
       long long outoff = 0;
       if (a.implicit) {
-        while (row + 1 < a.bin.nbra && a.bin.row_start[row + 1] <= q) ++row;
-        const int j = int(q - a.bin.row_start[row]) + a.bin.row_j0[row];
-        bpair = a.bin.bra_pairs[row];
+        while (seg + 1 < a.bin.nseg && a.bin.seg_start[seg + 1] <= q) ++seg;
+        const int j = int(q - a.bin.seg_start[seg]) + a.bin.seg_j0[seg];
+        bpair = a.bin.bra_pairs[a.bin.seg_bra[seg]];
         kpair = a.bin.ket_pairs[j];
         flags = (a.pair_swap[bpair] ? 1 : 0) | (a.pair_swap[kpair] ? 2 : 0);
       } else {

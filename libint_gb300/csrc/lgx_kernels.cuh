@@ -21,16 +21,31 @@ struct QuartetItem {
   long long out;           // output offset (doubles) or K index (Schwarz)
 };
 
-// Implicit work (one class bin of the screened J/K quartet space).
+// Implicit work: one class bin of the screened J/K quartet space as a list
+// of segments.  A segment is one bra pair with a contiguous run of ket
+// pairs of one contraction-depth group; segments are ordered by (bra depth
+// group, ket depth group, bra pair) so consecutive quartets share their
+// primitive counts.
 struct BinWork {
-  const int* bra_pairs;     // pair ids of the bra class, sorted by K desc
-  const int* ket_pairs;     // pair ids of the ket class, sorted by K desc
-  const long long* row_start;  // [nbra+1] prefix sums of per-row counts
-  const int* row_j0;        // first ket index of each row in this space
-  int nbra;
+  const int* bra_pairs;        // pair ids of the bra class (depth, K desc)
+  const int* ket_pairs;        // pair ids of the ket class (depth, K desc)
+  const long long* seg_start;  // [nseg+1] prefix sums of segment lengths
+  const int* seg_bra;          // bra index (into bra_pairs) of each segment
+  const int* seg_j0;           // first ket index (into ket_pairs)
+  int nseg;
   int pad;
   long long total;
 };
+
+// Segment containing quartet q (binary search over seg_start).
+__device__ __forceinline__ int bin_segment(const BinWork& b, long long q) {
+  int lo = 0, hi = b.nseg;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (b.seg_start[mid] <= q) lo = mid; else hi = mid;
+  }
+  return lo;
+}
 
 struct EriArgs {
   DevBasis basis;

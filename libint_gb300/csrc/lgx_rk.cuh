@@ -237,25 +237,21 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
   const int lane = threadIdx.x & 31;
   const int g = lane & (G - 1);
   const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
-  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long ngroups = ((long long)gridDim.x * blockDim.x) / G;
+  const int per_warp = 32 / G;  // quartets per warp chunk
+  const long long warp_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const long long total = a.implicit ? a.bin.total : a.nitems;
-  int row = -1;
-  for (long long qi = gtid / G; qi < total; qi += ngroups) {
+  // Warp chunks of per_warp consecutive quartets, strided over the grid:
+  // consecutive quartets share a bin segment (same bra pair, same depth).
+  for (long long c = warp_id; c * per_warp < total; c += nwarps) {
+    const long long qi = c * per_warp + (lane / G);
+    if (qi >= total) continue;
     int bpair, kpair, flags, orig = 0;
     long long outoff = 0;
     if (a.implicit) {
-      if (row < 0) {
-        int lo = 0, hi = a.bin.nbra;
-        while (hi - lo > 1) {
-          const int mid = (lo + hi) >> 1;
-          if (a.bin.row_start[mid] <= qi) lo = mid; else hi = mid;
-        }
-        row = lo;
-      }
-      while (row + 1 < a.bin.nbra && a.bin.row_start[row + 1] <= qi) ++row;
-      const int j = int(qi - a.bin.row_start[row]) + a.bin.row_j0[row];
-      bpair = a.bin.bra_pairs[row];
+      const int seg = bin_segment(a.bin, qi);
+      const int j = int(qi - a.bin.seg_start[seg]) + a.bin.seg_j0[seg];
+      bpair = a.bin.bra_pairs[a.bin.seg_bra[seg]];
       kpair = a.bin.ket_pairs[j];
       flags = (a.pair_swap[bpair] ? 1 : 0) | (a.pair_swap[kpair] ? 2 : 0);
     } else {
@@ -450,5 +446,24 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
     }
   }
 }
+
+// Launch of one register kernel: occupancy-sized grid, capped by the work.
+template <typename T, int LA, int LB, int LC, int LD, int MODE>
+cudaError_t rk_launch_one(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  const int block = 128;
+  auto k = rk_kernel<T, LA, LB, LC, LD, MODE>;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, block, 0) != cudaSuccess || occ < 1)
+    occ = 1;
+  long long grid = (long long)nsm * occ;
+  const long long need = (work * a.group + block - 1) / block;
+  if (need < grid) grid = need < 1 ? 1 : need;
+  k<<<(unsigned)grid, block, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
+                      long long work, int nsm, cudaStream_t st);
+bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
 
 }  // namespace lgx

@@ -1,0 +1,70 @@
+// Test driver for the C++ drop-in headers (include/libint2.hpp): written the
+// way a libint2 caller writes it (initialize, BasisSet, Engine::compute,
+// compute2<...,1>, results(), lmax_exceeded, finalize), plus the batched
+// JKBuilder.  Writes every shell set it computes to a binary file that the
+// pytest wrapper compares with the oracle.
+#include <libint2.hpp>
+
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <vector>
+
+int main(int argc, char** argv) {
+  if (argc < 2) return 2;
+  std::ofstream out(argv[1], std::ios::binary);
+  auto put = [&](double v) { out.write(reinterpret_cast<const char*>(&v), sizeof v); };
+  libint2::initialize();
+  std::vector<libint2::Atom> atoms = {{8, 0.0, -0.143, 0.0}, {1, 1.638, 1.136, 0.0},
+                                      {1, -1.638, 1.136, 0.0}, {8, 5.0, 0.2, 0.1},
+                                      {1, 6.6, 1.4, 0.0}, {1, 3.4, 1.2, 0.3}};
+  libint2::BasisSet obs("cc-pVDZ", atoms);
+  put(double(obs.size()));
+  libint2::Engine engine(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 0);
+  const auto& buf = engine.results();
+  const size_t ns = 8;  // first 8 shells: s, s, s, p, p, d on O and s, s on H
+  for (size_t a = 0; a < ns; ++a)
+    for (size_t b = 0; b < ns; ++b)
+      for (size_t c = 0; c < ns; ++c)
+        for (size_t d = 0; d < ns; ++d) {
+          engine.compute(obs[a], obs[b], obs[c], obs[d]);
+          const size_t n = obs[a].size() * obs[b].size() * obs[c].size() * obs[d].size();
+          if (buf[0] == nullptr) {
+            put(0.0);
+            continue;
+          }
+          put(1.0);
+          for (size_t i = 0; i < n; ++i) put(buf[0][i]);
+        }
+  // first derivatives through compute2<coulomb, xx_xx, 1>
+  libint2::Engine d1(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 1);
+  const size_t q1[][4] = {{5, 3, 8, 0}, {3, 5, 5, 9}, {0, 14, 5, 3}};
+  for (const auto& q : q1) {
+    const auto& r = d1.compute2<libint2::Operator::coulomb, libint2::BraKet::xx_xx, 1>(
+        obs[q[0]], obs[q[1]], obs[q[2]], obs[q[3]]);
+    const size_t n = obs[q[0]].size() * obs[q[1]].size() * obs[q[2]].size() * obs[q[3]].size();
+    for (unsigned s = 0; s < d1.nshellsets(); ++s)
+      for (size_t i = 0; i < n; ++i) put(r[s][i]);
+  }
+  // lmax_exceeded is thrown for max_l beyond the build
+  bool thrown = false;
+  try {
+    libint2::Engine e(libint2::Operator::coulomb, 4, 5, 0);
+  } catch (const libint2::Engine::lmax_exceeded&) {
+    thrown = true;
+  }
+  put(thrown ? 1.0 : 0.0);
+  // batched J/K
+  libint2::gb300::JKBuilder jk(obs);
+  const int nbf = jk.nbf();
+  std::vector<double> D(size_t(nbf) * nbf), J, K;
+  for (int i = 0; i < nbf; ++i)
+    for (int j = 0; j < nbf; ++j) D[size_t(i) * nbf + j] = std::exp(-0.3 * std::abs(i - j));
+  jk.compute(D, J, K, 0.0);
+  for (double v : J) put(v);
+  for (double v : K) put(v);
+  libint2::finalize();
+  std::cout << "ok" << std::endl;
+  return 0;
+}
