@@ -35,6 +35,7 @@ WORKLOADS = {
     "h2o32_cc-pvdz": ((4, 4, 2), "cc-pVDZ", 1e-12, "(H2O)32 cc-pVDZ 4x4x2 grid, Schwarz 1e-12"),
     "h2o16_cc-pvdz": ((4, 2, 2), "cc-pVDZ", 1e-12, "(H2O)16 cc-pVDZ 4x2x2 grid, Schwarz 1e-12"),
     "h2o4_cc-pvdz": ((2, 2, 1), "cc-pVDZ", 0.0, "(H2O)4 cc-pVDZ 2x2x1 grid, no screening"),
+    "h2o8_cc-pvtz": ((2, 2, 2), "cc-pVTZ", 1e-12, "(H2O)8 cc-pVTZ 2x2x2 grid, Schwarz 1e-12"),
 }
 MIXED_THRESH = 1e-4
 SEED = 2024
@@ -336,7 +337,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lgx", choices=["lgx", "reference"])
-    ap.add_argument("--workload", default="h2o64_cc-pvtz", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="h2o32_cc-pvdz", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-budget", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
