@@ -26,7 +26,7 @@ cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npair
                               double ln_prec, int method, cudaStream_t st);
 cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J,
                                double* K, int nbf, cudaStream_t st);
-size_t stage_bytes_per_warp();
+size_t stage_bytes_per_warp(bool fp32);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
 cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
@@ -95,7 +95,7 @@ struct BasisDev {
   int nshell = 0, nprim_total = 0, nbf = 0, natoms = 0;
   std::vector<int> l, pure, nprim, prim_off, bf_off, atom;
   std::vector<double> O, alpha, coeff;
-  DBuf ints, dbls;
+  DBuf ints, dbls, flts;
   DevBasis dev{};
   // pairs
   std::vector<PairRec> hpairs;
@@ -142,7 +142,7 @@ struct lgx_context {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   std::string err;
-  DBuf boys, boys32, sph, Df;
+  DBuf boys, boys_tay, boys32, sph_off, sph_c, sph_cd, sph_cf, Df;
   std::map<int, std::unique_ptr<ProgDev>> progs;
   bool use_rk = true;  // register kernels for the small classes
   bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
@@ -379,6 +379,19 @@ lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t
   B.dev.O = db;
   B.dev.alpha = db + 3 * nshell;
   B.dev.coeff = db + 3 * nshell + np;
+  {
+    std::vector<float> hf(6 * size_t(nshell));
+    for (int i = 0; i < 3 * nshell; ++i) {
+      const float hi = float(B.O[i]);
+      hf[i] = hi;
+      hf[3 * nshell + i] = float(B.O[i] - double(hi));
+    }
+    CK(B.flts.ensure(hf.size() * sizeof(float)));
+    CK(cudaMemcpyAsync(B.flts.p, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    B.dev.Ohi = B.flts.as<float>();
+    B.dev.Olo = B.flts.as<float>() + 3 * nshell;
+  }
   B.pairs_ok = false;
   B.schwarz_ok = false;
   // pair table layout (all s1 >= s2)
@@ -441,7 +454,7 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
   L.wpb = 4;
   L.stride = (P.host.total_slots() + 1) & ~1;
   const size_t slot_bytes = size_t(L.stride) * elt;
-  const size_t stage = stage_bytes_per_warp();
+  const size_t stage = stage_bytes_per_warp(fp32);
   const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
   L.global = slot_bytes > 40 * 1024 || L.wpb * (stage + slot_bytes) > smem_cap;
   L.smem = L.wpb * (stage + (L.global ? 0 : slot_bytes));
@@ -470,6 +483,24 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
 // Register kernels exist for the generated classes (deriv 0; see
 // codegen/gen_rk.py for the limits per mode) with the standard pure flags;
 // everything else runs on the warp-cooperative program kernel.
+// Context and basis pointers every kernel launch needs.
+void fill_common(const lgx_context* ctx, const BasisDev& B, EriArgs& a) {
+  a.basis = B.dev;
+  a.pairs = B.pairs.as<PairRec>();
+  a.pprims = B.pprims.as<PrimPairRec>();
+  a.pair_swap = B.pair_swap.as<unsigned char>();
+  a.boys = ctx->boys.as<double>();
+  a.boys_tay = ctx->boys_tay.as<double>();
+  a.boys32 = ctx->boys32.as<float>();
+  a.sph_off = ctx->sph_off.as<int>();
+  a.sph_c = ctx->sph_c.as<int>();
+  a.sph_cd = ctx->sph_cd.as<double>();
+  a.sph_cf = ctx->sph_cf.as<float>();
+  a.error_flag = ctx->errflag.as<int>();
+  a.fprecision = float(a.precision);
+  a.fln_prec = float(std::max(a.ln_prec, -1.0e30));
+}
+
 bool rk_eligible(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode,
                  bool fp32) {
   if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0) return false;
@@ -484,14 +515,7 @@ int choose_group(double nq_avg) {
 
 lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
                   EriArgs a, long long nwork, double nq_avg) {
-  a.basis = B.dev;
-  a.pairs = B.pairs.as<PairRec>();
-  a.pprims = B.pprims.as<PrimPairRec>();
-  a.pair_swap = B.pair_swap.as<unsigned char>();
-  a.boys = ctx->boys.as<double>();
-  a.boys32 = ctx->boys32.as<float>();
-  a.sph = ctx->sph.as<double>();
-  a.error_flag = ctx->errflag.as<int>();
+  fill_common(ctx, B, a);
   a.group = a.implicit ? 1 : choose_group(nq_avg);
   CK(rk_launch(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, nwork, ctx->nsm,
                ctx->stream));
@@ -505,15 +529,9 @@ lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bo
   Launch L;
   lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, L);
   if (s != LGX_OK) return s;
-  a.basis = B.dev;
-  a.pairs = B.pairs.as<PairRec>();
-  a.pprims = B.pprims.as<PrimPairRec>();
-  a.pair_swap = B.pair_swap.as<unsigned char>();
+  fill_common(ctx, B, a);
   a.prog = P.dev;
-  a.boys = ctx->boys.as<double>();
-  a.sph = ctx->sph.as<double>();
   a.counter = ctx->counter.as<unsigned long long>();
-  a.error_flag = ctx->errflag.as<int>();
   a.slot_stride = L.stride;
   a.global_slots = L.global ? 1 : 0;
   a.gscratch = ctx->gscratch.p;
@@ -970,15 +988,58 @@ lgx_status lgx_create(lgx_context** out, int device) {
     CK(cudaEventCreate(&c->ev2));
     CK(cudaEventCreate(&c->ev3));
     const auto boys = make_boys_table();
+    const auto sph = make_sph_table();
     CK(c->boys.ensure(boys.size() * sizeof(double)));
     CK(cudaMemcpy(c->boys.p, boys.data(), boys.size() * sizeof(double), cudaMemcpyHostToDevice));
+    {
+      // pre-divided Taylor coefficients F_{m+i}(T_k)/i!
+      std::vector<double> tay(size_t(kBoysRows) * (kBoysMaxM + 1) * kBoysTaylorStride, 0.0);
+      for (int k = 0; k < kBoysRows; ++k)
+        for (int m = 0; m <= kBoysMaxM; ++m) {
+          double f = 1;
+          for (int i = 0; i < 7; ++i) {
+            if (i > 0) f *= i;
+            tay[(size_t(k) * (kBoysMaxM + 1) + m) * kBoysTaylorStride + i] =
+                boys[size_t(k) * kBoysCols + m + i] / f;
+          }
+        }
+      CK(c->boys_tay.ensure(tay.size() * sizeof(double)));
+      CK(cudaMemcpy(c->boys_tay.p, tay.data(), tay.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    {
+      // sparse solid-harmonic rows
+      std::vector<int> off(4 * 9, 0), cidx;
+      std::vector<double> cd;
+      std::vector<float> cf;
+      for (int l = 0; l <= 3; ++l) {
+        const int nc = ncart(l);
+        for (int p = 0; p <= 2 * l; ++p) {
+          off[l * 9 + p] = int(cidx.size());
+          for (int c2 = 0; c2 < nc; ++c2) {
+            const double v = sph[sph_off(l) + p * nc + c2];
+            if (v != 0.0) {
+              cidx.push_back(c2);
+              cd.push_back(v);
+              cf.push_back(float(v));
+            }
+          }
+        }
+        off[l * 9 + 2 * l + 1] = int(cidx.size());
+      }
+      CK(c->sph_off.ensure(off.size() * sizeof(int)));
+      CK(c->sph_c.ensure(cidx.size() * sizeof(int)));
+      CK(c->sph_cd.ensure(cd.size() * sizeof(double)));
+      CK(c->sph_cf.ensure(cf.size() * sizeof(float)));
+      CK(cudaMemcpy(c->sph_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(c->sph_c.p, cidx.data(), cidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(c->sph_cd.p, cd.data(), cd.size() * sizeof(double), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(c->sph_cf.p, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
     std::vector<float> boysf(boys.begin(), boys.end());
     CK(c->boys32.ensure(boysf.size() * sizeof(float)));
     CK(cudaMemcpy(c->boys32.p, boysf.data(), boysf.size() * sizeof(float), cudaMemcpyHostToDevice));
     if (const char* e = getenv("LGX_DISABLE_RK")) c->use_rk = (e[0] == '0');
-    const auto sph = make_sph_table();
-    CK(c->sph.ensure(sph.size() * sizeof(double)));
-    CK(cudaMemcpy(c->sph.p, sph.data(), sph.size() * sizeof(double), cudaMemcpyHostToDevice));
+
     CK(set_inv_odd_table());
     CK(c->counter.ensure(64));
     CK(c->errflag.ensure(64));

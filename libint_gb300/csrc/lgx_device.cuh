@@ -23,48 +23,10 @@ constexpr int kBoysMaxM = 16;                         // largest mmax served
 constexpr int kBoysCols = kBoysMaxM + kBoysTerms;     // 23 columns
 constexpr int kBoysRows = int(kBoysTmax * 32.0) + 2;  // 1058 grid points
 
-// Device pointer to the [kBoysRows][kBoysCols] table (set per context).
-struct BoysTable {
-  const double* F;
-};
-
-__device__ __forceinline__ void boys_eval(const double* __restrict__ tab,
-                                          double T, int mmax,
-                                          double* __restrict__ F,
-                                          int stride) {
-  if (T > kBoysTmax) {
-    const double eT = exp(-T);
-    const double rT = 1.0 / T;
-    double f = 0.88622692545275801365 * sqrt(rT);
-    F[0] = f;
-    const double oo2T = 0.5 * rT;
-    for (int m = 0; m < mmax; ++m) {
-      f = ((2 * m + 1) * f - eT) * oo2T;
-      F[(m + 1) * stride] = f;
-    }
-    return;
-  }
-  const int k = __double2int_rn(T * kBoysInvDT);
-  const double d = T - k * kBoysDT;
-  const double* row = tab + k * kBoysCols + mmax;
-  // sum_{i<7} F_{mmax+i}(T_k) (-d)^i / i!   (Horner)
-  double s = __ldg(row + 6);
-  s = fma(s, -d * (1.0 / 6.0), __ldg(row + 5));
-  s = fma(s, -d * (1.0 / 5.0), __ldg(row + 4));
-  s = fma(s, -d * (1.0 / 4.0), __ldg(row + 3));
-  s = fma(s, -d * (1.0 / 3.0), __ldg(row + 2));
-  s = fma(s, -d * (1.0 / 2.0), __ldg(row + 1));
-  s = fma(s, -d, __ldg(row + 0));
-  F[mmax * stride] = s;
-  if (mmax > 0) {
-    const double eT = exp(-T);
-    const double twoT = 2.0 * T;
-    for (int m = mmax - 1; m >= 0; --m) {
-      s = fma(twoT, s, eT) * (1.0 / (2 * m + 1));
-      F[m * stride] = s;
-    }
-  }
-}
+// Pre-divided Taylor table: [kBoysRows][kBoysMaxM+1][8] with
+// entry i = F_{m+i}(T_k) / i! (i < 7), so that
+// F_m(T_k + d) = sum_i entry_i (-d)^i by Horner without extra products.
+constexpr int kBoysTaylorStride = 8;
 
 // ------------------------------------------------------------ basis data
 struct DevBasis {
@@ -78,7 +40,30 @@ struct DevBasis {
   const double* O;      // [3*nshell]
   const double* alpha;  // flattened
   const double* coeff;  // flattened, normalization embedded
+  const float* Ohi;     // [3*nshell] float(O)
+  const float* Olo;     // [3*nshell] float(O - Ohi): Ohi + Olo = O to ~1e-15
 };
+
+// float -> double with integer operations only (no FP64-pipe instruction):
+// exact for normal floats; zero and subnormal inputs (|x| < 1.2e-38) give 0.
+__device__ __forceinline__ double f2d_int(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (e == 0u) return __longlong_as_double((long long)sign);
+  const unsigned long long exp64 = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e - 127u + 1023u);
+  const unsigned long long mant = (unsigned long long)(u & 0x7fffffu) << 29;
+  return __longlong_as_double((long long)(sign | (exp64 << 52) | mant));
+}
+
+// double(n) for a small non-negative integer n < 2^20 with integer
+// operations only.
+__device__ __forceinline__ double i2d_int(int n) {
+  if (n <= 0) return 0.0;
+  const int e = 31 - __clz(n);
+  const unsigned hi = ((unsigned)(1023 + e) << 20) | ((unsigned)(n - (1 << e)) << (20 - e));
+  return __hiloint2double((int)hi, 0);
+}
 
 // One primitive pair of a shell pair (s1, s2) as stored (s1 = first shell),
 // with FP64 fields for the FP64 kernels and FP32 copies (centre-relative
@@ -87,14 +72,15 @@ struct __align__(16) PrimPairRec {
   double P[3];
   double Kc;      // sqrt(2) pi^{5/4} exp(-rho AB^2)/gamma * c1 * c2
   double oog;     // 1/(alpha1 + alpha2)
-  double ln_scr;  // ln of the pair screening factor (shell.h:1041-1059)
-  double nonsph;  // Conservative screening factor
+  double zeta;    // alpha1 + alpha2
   double a1, a2;  // exponents of s1 and s2
+  double ln_scr;  // ln of the pair screening factor (shell.h:1041-1059)
   float fKc, fzeta, foog, fln_scr;
   float fPA1[3];  // P - O(s1)
   float fPA2[3];  // P - O(s2)
   float fa1, fa2;
-  float pad[2];
+  float fnonsph;  // Conservative screening factor
+  float pad;
 };
 static_assert(sizeof(PrimPairRec) == 128, "PrimPairRec layout");
 

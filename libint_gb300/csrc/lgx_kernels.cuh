@@ -53,11 +53,19 @@ struct EriArgs {
   const PrimPairRec* pprims;
   const unsigned char* pair_swap;  // per pair: 1 if its canonical bra1 is s2
   DevProg prog;
-  const double* boys;
-  const float* boys32;   // FP32 copy of the Boys table
-  const double* sph;
-  // screening
+  const double* boys;     // [kBoysRows][kBoysCols] F_m(T_k)
+  const double* boys_tay; // pre-divided Taylor table (kBoysTaylorStride)
+  const float* boys32;    // FP32 copy of the Boys table
+  // Cartesian -> solid harmonics, sparse: nonzeros of row (l, p) are
+  // [sph_off[l*9+p], sph_off[l*9+p+1]) with Cartesian index sph_c[] and
+  // coefficient sph_cd[] (FP64) / sph_cf[] (FP32)
+  const int* sph_off;
+  const int* sph_c;
+  const double* sph_cd;
+  const float* sph_cf;
+  // screening (FP32 copies for the FP32 kernels)
   double precision, ln_prec;
+  float fprecision, fln_prec;
   int screening;  // 0 Original, 1 Conservative
   // work
   const QuartetItem* items;
@@ -85,7 +93,7 @@ struct EriArgs {
   // watchdog: a bounded number of work chunks per warp
   long long max_chunks;
   int* error_flag;
-  // statistics
+  // statistics: primitive quartets computed (one atomic per thread)
   unsigned long long* prim_count;
 };
 

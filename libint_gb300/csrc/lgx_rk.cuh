@@ -16,17 +16,16 @@
 
 namespace lgx {
 
-__device__ __forceinline__ double rk_exp(double x) { return exp(x); }
-__device__ __forceinline__ float rk_exp(float x) { return __expf(x); }
-__device__ __forceinline__ double rk_rsqrt(double x) { return rsqrt(x); }
-__device__ __forceinline__ float rk_rsqrt(float x) { return rsqrtf(x); }
+// T -> double for the FP64 accumulators (integer-only for float)
+__device__ __forceinline__ double rk_f64(double x) { return x; }
+__device__ __forceinline__ double rk_f64(float x) { return f2d_int(x); }
 
 // Boys F_0..F_MMAX(T) (times nothing).  FP64: 7-term Taylor about the grid
 // point (every m directly when MMAX <= 2, else the top m plus the downward
 // recursion); FP32: 4-term Taylor on the same grid.  T > kBoysTmax:
 // asymptotic F_0 and upward recursion.
 template <int MMAX>
-__device__ __forceinline__ void rk_boys(const double* __restrict__ tab, double T, double* F) {
+__device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T, double* F) {
   if (T > kBoysTmax) {
     const double rT = 1.0 / T;
     const double oo2T = 0.5 * rT;
@@ -40,30 +39,26 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tab, double T
     }
     return;
   }
-  const int k = __double2int_rn(T * kBoysInvDT);
-  const double d = T - k * kBoysDT;
-  const double* row = tab + k * kBoysCols;
-  const double c6 = -d * (1.0 / 6.0), c5 = -d * (1.0 / 5.0), c4 = -d * (1.0 / 4.0);
-  const double c3 = -d * (1.0 / 3.0), c2 = -d * 0.5, c1 = -d;
+  // nearest grid point: adding 1.5*2^52 rounds T*32 to an integer held in
+  // the low mantissa bits (read back with an integer move)
+  const double t32 = fma(T, kBoysInvDT, 6755399441055744.0);
+  const int k = __double2loint(t32);
+  const double md = fma(t32 - 6755399441055744.0, kBoysDT, -T);  // = -(T - T_k)
+  const double* row = tay + (k * (kBoysMaxM + 1)) * kBoysTaylorStride;
   if (MMAX <= 2) {
 #pragma unroll
     for (int m = 0; m <= MMAX; ++m) {
-      double s = __ldg(row + m + 6);
-      s = fma(s, c6, __ldg(row + m + 5));
-      s = fma(s, c5, __ldg(row + m + 4));
-      s = fma(s, c4, __ldg(row + m + 3));
-      s = fma(s, c3, __ldg(row + m + 2));
-      s = fma(s, c2, __ldg(row + m + 1));
-      F[m] = fma(s, c1, __ldg(row + m));
+      const double* c = row + m * kBoysTaylorStride;
+      double s = __ldg(c + 6);
+#pragma unroll
+      for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
+      F[m] = s;
     }
   } else {
-    double s = __ldg(row + MMAX + 6);
-    s = fma(s, c6, __ldg(row + MMAX + 5));
-    s = fma(s, c5, __ldg(row + MMAX + 4));
-    s = fma(s, c4, __ldg(row + MMAX + 3));
-    s = fma(s, c3, __ldg(row + MMAX + 2));
-    s = fma(s, c2, __ldg(row + MMAX + 1));
-    s = fma(s, c1, __ldg(row + MMAX));
+    const double* c = row + MMAX * kBoysTaylorStride;
+    double s = __ldg(c + 6);
+#pragma unroll
+    for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
     F[MMAX] = s;
     const double eT = exp(-T);
     const double twoT = 2.0 * T;
@@ -108,15 +103,18 @@ __device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, 
   }
 }
 
+template <typename T>
 struct RkQuartet {
   int sh[4];
   int bra_pp, ket_pp, nbpp, nkpp;
   bool bsw, ksw;
-  double A[3], B[3], C[3], D[3];
+  double A[3], C[3];  // FP64 kernels only
+  T AB[3], CD[3], AC[3];
 };
 
+template <typename T>
 __device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, bool bsw,
-                                        bool ksw, RkQuartet& q) {
+                                        bool ksw, RkQuartet<T>& q) {
   const PairRec bp = a.pairs[bpair];
   const PairRec kp = a.pairs[kpair];
   q.sh[0] = bsw ? bp.s2 : bp.s1;
@@ -129,33 +127,55 @@ __device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, 
   q.nkpp = kp.npp;
   q.bsw = bsw;
   q.ksw = ksw;
+  if constexpr (sizeof(T) == 8) {
 #pragma unroll
-  for (int x = 0; x < 3; ++x) {
-    q.A[x] = a.basis.O[3 * q.sh[0] + x];
-    q.B[x] = a.basis.O[3 * q.sh[1] + x];
-    q.C[x] = a.basis.O[3 * q.sh[2] + x];
-    q.D[x] = a.basis.O[3 * q.sh[3] + x];
+    for (int x = 0; x < 3; ++x) {
+      const double A = a.basis.O[3 * q.sh[0] + x], B = a.basis.O[3 * q.sh[1] + x];
+      const double C = a.basis.O[3 * q.sh[2] + x], D = a.basis.O[3 * q.sh[3] + x];
+      q.A[x] = A;
+      q.C[x] = C;
+      q.AB[x] = A - B;
+      q.CD[x] = C - D;
+      q.AC[x] = A - C;
+    }
+  } else {
+    // FP32: differences of the hi/lo float centres keep FP32 relative
+    // precision without an FP64 instruction
+    const float* hi = a.basis.Ohi;
+    const float* lo = a.basis.Olo;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      const int i0 = 3 * q.sh[0] + x, i1 = 3 * q.sh[1] + x, i2 = 3 * q.sh[2] + x,
+                i3 = 3 * q.sh[3] + x;
+      q.AB[x] = (hi[i0] - hi[i1]) + (lo[i0] - lo[i1]);
+      q.CD[x] = (hi[i2] - hi[i3]) + (lo[i2] - lo[i3]);
+      q.AC[x] = (hi[i0] - hi[i2]) + (lo[i0] - lo[i2]);
+    }
   }
 }
 
 // One primitive quartet into acc (FP64).  Returns false when screened out.
+// The ln-screen runs on the FP32 copies (it only decides whether a
+// primitive quartet below ~1e-16 contributes) and the pfac screen compares
+// the IEEE bit patterns, so neither costs an FP64 instruction.
 template <class C>
-__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet& q, int ib, int ik,
-                                        double* acc) {
+__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double>& q, int ib,
+                                        int ik, double* acc) {
   const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
-  if (!(bp.ln_scr + kp.ln_scr > a.ln_prec)) return false;
-  const double zeta = bp.a1 + bp.a2, eta = kp.a1 + kp.a2;
+  if (!(bp.fln_scr + kp.fln_scr > a.fln_prec)) return false;
+  const double zeta = bp.zeta, eta = kp.zeta;
   const double gpq = zeta + eta;
   const double rs = rsqrt(gpq);
-  const double oogpq = rs * rs;
   const double pfac = bp.Kc * kp.Kc * rs;
-  if (fabs(pfac) < a.precision) return false;
+  if ((__double_as_longlong(pfac) & 0x7fffffffffffffffll) < __double_as_longlong(a.precision))
+    return false;
+  const double oogpq = rs * rs;
   const double PQx = bp.P[0] - kp.P[0], PQy = bp.P[1] - kp.P[1], PQz = bp.P[2] - kp.P[2];
   const double rho = zeta * eta * oogpq;
   const double T = rho * fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
   double F[C::kMmax + 1];
-  rk_boys<C::kMmax>(a.boys, T, F);
+  rk_boys<C::kMmax>(a.boys_tay, T, F);
 #pragma unroll
   for (int m = 0; m <= C::kMmax; ++m) F[m] *= pfac;
   rk::Geo<double> g;
@@ -175,20 +195,21 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet& q, in
 
 // One primitive quartet into acc (FP32).  AC = A - C of the quartet.
 template <class C>
-__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet& q, int ib, int ik,
-                                        float* acc, float ACx, float ACy, float ACz) {
+__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>& q, int ib,
+                                        int ik, float* acc) {
   const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
-  if (!(bp.fln_scr + kp.fln_scr > float(a.ln_prec))) return false;
+  if (!(bp.fln_scr + kp.fln_scr > a.fln_prec)) return false;
   const float zeta = bp.fzeta, eta = kp.fzeta;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
   const float pfac = bp.fKc * kp.fKc * rs;
-  if (fabsf(pfac) < float(a.precision)) return false;
+  if (fabsf(pfac) < a.fprecision) return false;
   const float* PA = q.bsw ? bp.fPA2 : bp.fPA1;
   const float* QC = q.ksw ? kp.fPA2 : kp.fPA1;
-  const float PQx = PA[0] - QC[0] + ACx, PQy = PA[1] - QC[1] + ACy, PQz = PA[2] - QC[2] + ACz;
+  const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
+              PQz = PA[2] - QC[2] + q.AC[2];
   const float rho = zeta * eta * oogpq;
   const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
   float F[C::kMmax + 1];
@@ -241,6 +262,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
   const long long warp_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const long long total = a.implicit ? a.bin.total : a.nitems;
+  unsigned long long my_prims = 0;
   // Warp chunks of per_warp consecutive quartets, strided over the grid:
   // consecutive quartets share a bin segment (same bra pair, same depth).
   for (long long c = warp_id; c * per_warp < total; c += nwarps) {
@@ -262,24 +284,16 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
       outoff = it.out;
       orig = it.pad;
     }
-    RkQuartet q;
-    rk_load(a, bpair, kpair, flags & 1, (flags >> 1) & 1, q);
+    RkQuartet<T> q;
+    rk_load<T>(a, bpair, kpair, flags & 1, (flags >> 1) & 1, q);
     T acc[C::kNacc];
 #pragma unroll
     for (int i = 0; i < C::kNacc; ++i) acc[i] = T(0);
     const int nq = q.nbpp * q.nkpp;
     int kept = 0;
-    const float ACx = float(q.A[0] - q.C[0]), ACy = float(q.A[1] - q.C[1]),
-                ACz = float(q.A[2] - q.C[2]);
     for (int p = g; p < nq; p += G) {
       const int ib = p / q.nkpp, ik = p - ib * q.nkpp;
-      bool ok;
-      if constexpr (sizeof(T) == 8) {
-        ok = rk_prim<C>(a, q, ib, ik, acc);
-      } else {
-        ok = rk_prim<C>(a, q, ib, ik, acc, ACx, ACy, ACz);
-      }
-      kept += ok ? 1 : 0;
+      kept += rk_prim<C>(a, q, ib, ik, acc) ? 1 : 0;
     }
     if (G > 1) {
       for (int o = G >> 1; o > 0; o >>= 1) {
@@ -288,22 +302,20 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
         kept += __shfl_xor_sync(gmask, kept, o, G);
       }
     }
-    if (a.prim_count && g == 0) atomicAdd(a.prim_count, (unsigned long long)kept);
+    if (g == 0) my_prims += (unsigned long long)kept;
     if (MODE == kModeStore && a.is_null && g == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
     if (kept == 0) {
       if (MODE == kModeSchwarz && g == 0) a.kschwarz[outoff] = 0.0;
       continue;
     }
-    const T AB[3] = {T(q.A[0] - q.B[0]), T(q.A[1] - q.B[1]), T(q.A[2] - q.B[2])};
-    const T CD[3] = {T(q.C[0] - q.D[0]), T(q.C[1] - q.D[1]), T(q.C[2] - q.D[2])};
     T cart[C::kNcart];
-    C::template hrr<T>(acc, AB, CD, cart);
+    C::template hrr<T>(acc, q.AB, q.CD, cart);
     T v[C::kNsph];
     C::template sph<T>(cart, v);
     if (MODE == kModeSchwarz) {
       double mx = 0;
 #pragma unroll
-      for (int e = 0; e < C::kNsph; ++e) mx = fmax(mx, fabs(double(v[e])));
+      for (int e = 0; e < C::kNsph; ++e) mx = fmax(mx, fabs(rk_f64(v[e])));
       if (g == 0) a.kschwarz[outoff] = sqrt(mx);
     } else if (MODE == kModeStore) {
       const int fl = flags >> 2;
@@ -325,11 +337,11 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
         int it[4];
 #pragma unroll
         for (int t = 0; t < 4; ++t) it[perm[t]] = ci[t];
-        o[((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3]] = double(v[e]);
+        o[((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3]] = rk_f64(v[e]);
       }
     } else if (MODE == kModeJK) {
-      const double deg = (q.sh[0] == q.sh[1] ? 1.0 : 2.0) * (q.sh[2] == q.sh[3] ? 1.0 : 2.0) *
-                         (bpair == kpair ? 1.0 : 2.0);
+      const T deg = T((q.sh[0] == q.sh[1] ? 1 : 2) * (q.sh[2] == q.sh[3] ? 1 : 2) *
+                      (bpair == kpair ? 1 : 2));
       const int nbf = a.nbf;
       const size_t o0 = a.basis.bf_off[q.sh[0]], o1 = a.basis.bf_off[q.sh[1]];
       const size_t o2 = a.basis.bf_off[q.sh[2]], o3 = a.basis.bf_off[q.sh[3]];
@@ -352,7 +364,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             for (int k = 0; k < N2; ++k)
 #pragma unroll
               for (int l = 0; l < N3; ++l) s = fma(Dcd[k * N3 + l], V_(i, j, k, l), s);
-            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o0 + i) * nbf + o1 + j, deg * double(s));
+            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o0 + i) * nbf + o1 + j, rk_f64(deg * s));
           }
       }
       // J(c,d) += sum_ab D(a,b) v
@@ -371,7 +383,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             for (int i = 0; i < N0; ++i)
 #pragma unroll
               for (int j = 0; j < N1; ++j) s = fma(Dab[i * N1 + j], V_(i, j, k, l), s);
-            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o2 + k) * nbf + o3 + l, deg * double(s));
+            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o2 + k) * nbf + o3 + l, rk_f64(deg * s));
           }
       }
       // K(a,c) += sum_bd D(b,d) v ; K(b,d) += sum_ac D(a,c) v
@@ -394,7 +406,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             for (int j = 0; j < N1; ++j)
 #pragma unroll
               for (int l = 0; l < N3; ++l) s = fma(Dbd[j * N3 + l], V_(i, j, k, l), s);
-            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o0 + i) * nbf + o2 + k, deg * double(s));
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o0 + i) * nbf + o2 + k, rk_f64(deg * s));
           }
 #pragma unroll
         for (int j = 0; j < N1; ++j)
@@ -405,7 +417,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             for (int i = 0; i < N0; ++i)
 #pragma unroll
               for (int k = 0; k < N2; ++k) s = fma(Dac[i * N2 + k], V_(i, j, k, l), s);
-            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o1 + j) * nbf + o3 + l, deg * double(s));
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o1 + j) * nbf + o3 + l, rk_f64(deg * s));
           }
       }
       // K(a,d) += sum_bc D(b,c) v ; K(b,c) += sum_ad D(a,d) v
@@ -428,7 +440,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             for (int j = 0; j < N1; ++j)
 #pragma unroll
               for (int k = 0; k < N2; ++k) s = fma(Dbc[j * N2 + k], V_(i, j, k, l), s);
-            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o0 + i) * nbf + o3 + l, deg * double(s));
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o0 + i) * nbf + o3 + l, rk_f64(deg * s));
           }
 #pragma unroll
         for (int j = 0; j < N1; ++j)
@@ -439,12 +451,13 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             for (int i = 0; i < N0; ++i)
 #pragma unroll
               for (int l = 0; l < N3; ++l) s = fma(Dad[i * N3 + l], V_(i, j, k, l), s);
-            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o1 + j) * nbf + o2 + k, deg * double(s));
+            if ((slot & (G - 1)) == g) atomicAdd(a.Kacc + (o1 + j) * nbf + o2 + k, rk_f64(deg * s));
           }
       }
 #undef V_
     }
   }
+  if (a.prim_count && my_prims) atomicAdd(a.prim_count, my_prims);
 }
 
 // Launch of one register kernel: occupancy-sized grid, capped by the work.
