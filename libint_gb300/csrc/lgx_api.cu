@@ -26,7 +26,7 @@ cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npair
                               double ln_prec, int method, cudaStream_t st);
 cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J,
                                double* K, int nbf, cudaStream_t st);
-size_t stage_bytes_per_warp(bool fp32);
+size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
 cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
@@ -442,24 +442,43 @@ lgx_status ensure_pairs(lgx_context* ctx, BasisDev& B, double ln_prec, int metho
 
 // ------------------------------------------------------ launch helpers
 struct Launch {
-  int grid, block, wpb, stride;
+  int grid, block, wpb, stride, rows;
   size_t smem;
   bool global;
 };
 
+// Program-kernel launch shape: staging rows (primitive quartets prepared per
+// batch; a few suffice for the nearly uncontracted high-L classes and leave
+// shared memory to more resident warps) and warps per block, chosen for the
+// most resident warps per SM; rows_hint > 0 forces the row count.
 lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
-                       long long nwork, Launch& L) {
+                       long long nwork, double nq_avg, int rows_hint, Launch& L) {
   const size_t elt = fp32 ? 4 : 8;
-  L.block = 128;
-  L.wpb = 4;
   L.stride = (P.host.total_slots() + 1) & ~1;
   const size_t slot_bytes = size_t(L.stride) * elt;
-  const size_t stage = stage_bytes_per_warp(fp32);
+  L.rows = rows_hint > 0 ? rows_hint : (nq_avg > 12 ? 32 : (nq_avg > 6 ? 16 : 8));
+  const size_t stage = stage_bytes_per_warp(fp32, L.rows);
   const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
-  L.global = slot_bytes > 40 * 1024 || L.wpb * (stage + slot_bytes) > smem_cap;
-  L.smem = L.wpb * (stage + (L.global ? 0 : slot_bytes));
-  int bps = eri_blocks_per_sm(mode, fp32, L.block, L.smem);
-  if (bps < 1) bps = 1;
+  L.global = slot_bytes > 40 * 1024;
+  int best_warps = -1, bps = 1;
+  for (int wpb : {4, 2, 1}) {
+    const size_t smem = wpb * (stage + (L.global ? 0 : slot_bytes));
+    if (smem > smem_cap) continue;
+    const int b = std::max(1, eri_blocks_per_sm(mode, fp32, 32 * wpb, smem));
+    if (b * wpb > best_warps) {
+      best_warps = b * wpb;
+      bps = b;
+      L.wpb = wpb;
+      L.smem = smem;
+    }
+  }
+  if (best_warps < 0) {  // not even one warp's slots fit: global slots
+    L.global = true;
+    L.wpb = 4;
+    L.smem = L.wpb * stage;
+    bps = std::max(1, eri_blocks_per_sm(mode, fp32, 32 * L.wpb, L.smem));
+  }
+  L.block = 32 * L.wpb;
   long long grid = (long long)ctx->nsm * bps;
   const long long need = (nwork + L.wpb - 1) / L.wpb;
   grid = std::max<long long>(1, std::min(grid, need));
@@ -527,12 +546,13 @@ lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bo
   if (rk_eligible(ctx, B, P, mode, fp32))
     return run_rk(ctx, B, P, mode, fp32, a, nwork, nq_avg);
   Launch L;
-  lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, L);
+  lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, nq_avg, 0, L);
   if (s != LGX_OK) return s;
   fill_common(ctx, B, a);
   a.prog = P.dev;
   a.counter = ctx->counter.as<unsigned long long>();
   a.slot_stride = L.stride;
+  a.stage_rows = L.rows;
   a.global_slots = L.global ? 1 : 0;
   a.gscratch = ctx->gscratch.p;
   const long long nwarps = (long long)L.grid * L.wpb;
@@ -909,9 +929,16 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       ProgDev* P = nullptr;
       get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
       const bool rk = rk_eligible(ctx, B, *P, mode, recs[i].fp32);
-      fprintf(stderr, "lgx-class (%d%d|%d%d) %s %s quartets %lld prims %llu nq_avg %.1f  %.3f ms\n",
+      const int pure[4] = {bin.la > 1, bin.lb > 1, bin.lc > 1, bin.ld > 1};
+      const double np = double(pcp[2 * recs[i].bin + recs[i].sp]);
+      const double gflop = 1e-9 * (np * double(P->host.vrr_flops) +
+                                   double(bin.total[recs[i].sp]) *
+                                       (double(P->host.post_flops) +
+                                        (deriv ? 12 : 1) * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure)));
+      fprintf(stderr, "lgx-class (%d%d|%d%d) %s %s quartets %lld prims %.0f nq_avg %.1f  %.3f ms"
+              "  %.1f GFLOP %.3f TFLOP/s\n",
               bin.la, bin.lb, bin.lc, bin.ld, recs[i].fp32 ? "fp32" : "fp64", rk ? "rk" : "prog",
-              (long long)bin.total[recs[i].sp], pcp[2 * recs[i].bin + recs[i].sp], bin.nq_avg, ms);
+              (long long)bin.total[recs[i].sp], np, bin.nq_avg, ms, gflop, gflop / ms);
       cudaEventDestroy(pev[i]);
     }
   }

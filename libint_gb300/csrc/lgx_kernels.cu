@@ -30,6 +30,9 @@ constexpr int kStF = 0;           // F_m * pfac, m <= 15
 constexpr int kStPA = 16, kStWP = 19, kStQC = 22, kStWQ = 25;
 constexpr int kStOo2z = 28, kStRoz = 29, kStOo2e = 30, kStRoe = 31, kStOo2ze = 32;
 constexpr int kStW = 33;          // 2 alpha_A, 2 alpha_B, 2 alpha_D
+// Per-warp table of the integer-weighted recurrence factors of the current
+// primitive quartet: k/(2 zeta), k/(2 eta), k/(2(zeta+eta)) for k = 0..7.
+constexpr int kKtab = 24;
 
 __constant__ double c_inv_odd[40];  // 1/(2m+1)
 
@@ -258,15 +261,17 @@ template <typename T>
 __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __restrict__ slots,
                                 T* __restrict__ stage, int lane) {
   const DevProg& P = a.prog;
+  const int R = a.stage_rows;
+  T* ktab = stage + R * kStage;
   for (int i = lane; i < P.nacc; i += 32) slots[i] = T(0);
   const int nq = g.nbpp * g.nkpp;
   int kept = 0;
   const double npbraket = double(nq);
-  for (int base = 0; base < nq; base += 32) {
+  for (int base = 0; base < nq; base += R) {
     const int idx = base + lane;
     T row[kStage];
     bool keep = false;
-    if (idx < nq) keep = prologue(a, g, idx, npbraket, row);
+    if (lane < R && idx < nq) keep = prologue(a, g, idx, npbraket, row);
     const unsigned ballot = __ballot_sync(0xffffffffu, keep);
     if (keep) {
       T* st = stage + __popc(ballot & ((1u << lane) - 1u)) * kStage;
@@ -288,6 +293,8 @@ __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __
       const T oo2ze = st[kStOo2ze];
       const T w1 = st[kStW], w2 = st[kStW + 1], w3 = st[kStW + 2];
       for (int m = lane; m <= P.mmax; m += 32) slots[P.leaf_slot0 + m] = st[kStF + m];
+      if (lane < kKtab)
+        ktab[lane] = small_int<T>(lane & 7) * (lane < 8 ? oo2z : (lane < 16 ? oo2e : oo2ze));
       __syncwarp();
       for (int k = 0; k < P.nlev; ++k) {
         if (k > 0) {
@@ -299,22 +306,20 @@ __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __
             const int dir = (fl >> 1) & 3;
             const int n1 = (fl >> 3) & 31;
             const int ne = (fl >> 8) & 31;
-            T c1, c2, c3, c4;
+            T c1, c2, c4;
             if ((fl & 1u) == 0) {
               c1 = sel3(dir, PAx, PAy, PAz);
               c2 = sel3(dir, WPx, WPy, WPz);
-              c3 = oo2z;
               c4 = roz;
             } else {
               c1 = sel3(dir, QCx, QCy, QCz);
               c2 = sel3(dir, WQx, WQy, WQz);
-              c3 = oo2e;
               c4 = roe;
             }
             T val = c1 * slots[u.y];
             val = fma(c2, slots[u.z], val);
-            if (n1) val = fma(small_int<T>(n1) * c3, fma(-c4, slots[v.x], slots[u.w]), val);
-            if (ne) val = fma(small_int<T>(ne) * oo2ze, slots[v.y], val);
+            if (n1) val = fma(ktab[((fl & 1u) << 3) + n1], fma(-c4, slots[v.x], slots[u.w]), val);
+            if (ne) val = fma(ktab[16 + ne], slots[v.y], val);
             slots[u.x] = val;
           }
           __syncwarp();
@@ -518,13 +523,14 @@ __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const DevProg& P = a.prog;
-  T* stage = reinterpret_cast<T*>(smem_d) + wib * (32 * kStage);
+  const int stage_per_warp = (a.stage_rows * kStage + kKtab + 3) & ~3;
+  T* stage = reinterpret_cast<T*>(smem_d) + wib * stage_per_warp;
   T* slots;
   if (a.global_slots) {
     const size_t gw = size_t(blockIdx.x) * wpb + wib;
     slots = reinterpret_cast<T*>(a.gscratch) + gw * size_t(a.slot_stride);
   } else {
-    T* base = reinterpret_cast<T*>(smem_d) + wpb * (32 * kStage);
+    T* base = reinterpret_cast<T*>(smem_d) + wpb * stage_per_warp;
     slots = base + size_t(wib) * a.slot_stride;
   }
   const long long total = a.implicit ? a.bin.total : a.nitems;
@@ -793,9 +799,10 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
   return cudaGetLastError();
 }
 
-// Bytes of per-warp staging for the program kernel in FP64 or FP32.
-size_t stage_bytes_per_warp(bool fp32) {
-  return size_t(32) * kStage * (fp32 ? sizeof(float) : sizeof(double));
+// Bytes of per-warp staging (rows primitive quartets + the factor table)
+// for the program kernel in FP64 or FP32.
+size_t stage_bytes_per_warp(bool fp32, int rows) {
+  return size_t((rows * kStage + kKtab + 3) & ~3) * (fp32 ? sizeof(float) : sizeof(double));
 }
 
 __global__ void d2f_kernel(const double* src, float* dst, long long n) {

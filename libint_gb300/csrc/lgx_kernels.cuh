@@ -77,6 +77,7 @@ struct EriArgs {
   unsigned long long* counter;
   // slots
   int slot_stride;     // slots per warp (elements of T)
+  int stage_rows;      // program kernel: primitive quartets staged per batch (8, 16 or 32)
   int global_slots;    // 1: slots live in gscratch
   void* gscratch;      // [nwarps_total][slot_stride] of T
   // outputs

@@ -320,6 +320,8 @@ ClassProgramHost build_class_program(int la, int lb, int lc, int ld, int deriv) 
       for (int id : bylev[k]) {
         const VNode& n = nodes[id];
         auto sl = [&](int s) { return s >= 0 ? slot32(nodes[s].slot) : 0u; };
+        // the kernel's factor table holds k/(2 zeta) etc. for k = 0..7
+        if (n.n1 > 7 || n.ne > 7) throw std::runtime_error("lgx: recurrence factor out of range");
         P.vrr_ops.push_back(slot32(n.slot));
         for (int t = 0; t < 5; ++t) P.vrr_ops.push_back(sl(n.src[t]));
         P.vrr_ops.push_back(uint32_t(n.kind) | (uint32_t(n.dir) << 1) |
