@@ -35,7 +35,8 @@ def _generate() -> list:
     sys.path.insert(0, os.path.join(PKG_DIR, "codegen"))
     try:
         import gen_rk
-        units = gen_rk.main()
+        import gen_post
+        units = gen_rk.main() + gen_post.main()
     finally:
         sys.path.pop(0)
     return [os.path.join("gen", u) for u in units]

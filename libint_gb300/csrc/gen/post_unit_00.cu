@@ -1,0 +1,35 @@
+// GENERATED by libint_gb300/codegen/gen_post.py -- do not edit.
+#include "post_classes.cuh"
+
+namespace lgx {
+cudaError_t post_launch_d_3333(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 3, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_3333(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 3, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_3033(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 0, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_3033(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 0, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_2132(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 1, 3, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_2132(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 1, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_d_3122(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 1, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_3122(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 1, 2, 2>>(block, smem);
+}
+cudaError_t post_launch_d_2122(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 1, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_2122(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 1, 2, 2>>(block, smem);
+}
+}  // namespace lgx

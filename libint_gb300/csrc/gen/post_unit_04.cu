@@ -1,0 +1,47 @@
+// GENERATED by libint_gb300/codegen/gen_post.py -- do not edit.
+#include "post_classes.cuh"
+
+namespace lgx {
+cudaError_t post_launch_d_2233(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 2, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_2233(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 2, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_3232(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 2, 3, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_3232(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 2, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_d_1133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<1, 1, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_1133(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<1, 1, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_2231(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 2, 3, 1>>(a, grid, block, smem, st);
+}
+int post_occ_d_2231(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 2, 3, 1>>(block, smem);
+}
+cudaError_t post_launch_d_1033(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<1, 0, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_1033(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<1, 0, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_2032(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 0, 3, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_2032(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 0, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_d_3031(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 0, 3, 1>>(a, grid, block, smem, st);
+}
+int post_occ_d_3031(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 0, 3, 1>>(block, smem);
+}
+}  // namespace lgx

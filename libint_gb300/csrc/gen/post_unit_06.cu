@@ -1,0 +1,41 @@
+// GENERATED by libint_gb300/codegen/gen_post.py -- do not edit.
+#include "post_classes.cuh"
+
+namespace lgx {
+cudaError_t post_launch_d_3133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 1, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_3133(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 1, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_2133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 1, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_d_2133(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 1, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_d_3132(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 1, 3, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_3132(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 1, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_d_2222(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 2, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_2222(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 2, 2, 2>>(block, smem);
+}
+cudaError_t post_launch_d_3131(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 1, 3, 1>>(a, grid, block, smem, st);
+}
+int post_occ_d_3131(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 1, 3, 1>>(block, smem);
+}
+cudaError_t post_launch_d_3022(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 0, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_3022(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 0, 2, 2>>(block, smem);
+}
+}  // namespace lgx

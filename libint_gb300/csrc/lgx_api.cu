@@ -18,7 +18,6 @@
 #include "lgx_program.h"
 
 namespace lgx {
-cudaError_t set_inv_odd_table();
 cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int block,
                        size_t smem, cudaStream_t st);
 cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npairs,
@@ -32,6 +31,10 @@ cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t 
 cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
                       long long work, int nsm, cudaStream_t st);
 bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
+cudaError_t post_launch(bool fp32, int la, int lb, int lc, int ld, const EriArgs& a, int grid,
+                        int block, size_t smem, cudaStream_t st);
+int post_blocks_per_sm(bool fp32, int la, int lb, int lc, int ld, int block, size_t smem);
+bool post_info(int la, int lb, int lc, int ld, int* nacc, int* slots);
 }  // namespace lgx
 
 using namespace lgx;
@@ -135,6 +138,15 @@ struct BinCache {
 
 }  // namespace
 
+// Launch variant of one class bin: the register kernel with G lanes per
+// quartet, or the program kernel with interpreted or generated post stage
+// and R staging rows.
+struct Variant {
+  int kind = 0;   // 0 register kernel, 1 program kernel, 2 program kernel + generated post
+  int group = 1;  // register kernel: lanes per quartet
+  int rows = 0;   // program kernel: staging rows (0: from the contraction depth)
+};
+
 struct lgx_context {
   int device = 0;
   int nsm = 0;
@@ -142,9 +154,15 @@ struct lgx_context {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   std::string err;
-  DBuf boys, boys_tay, boys32, sph_off, sph_c, sph_cd, sph_cf, Df;
+  DBuf boys, boys_tay, boys32, sph_off, sph_c, sph_cd, sph_cf, Df, inv_odd;
   std::map<int, std::unique_ptr<ProgDev>> progs;
   bool use_rk = true;  // register kernels for the small classes
+  bool use_post = true;  // generated post stages for the large J/K classes
+  bool tune = true;      // per-class launch-shape tuning on the first pass
+  long long tune_min = 4096;  // bins with fewer quartets keep the default variant
+  // tuned launch variant per (class, deriv, mode, precision)
+  std::map<int, struct Variant> tuned;
+  DBuf tuneJ, tuneK;
   bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
   BasisDev basis, small;
   DBuf gscratch, counter, errflag, primcount;
@@ -282,14 +300,35 @@ lgx_status get_prog(lgx_context* ctx, int la, int lb, int lc, int ld, int deriv,
   const size_t o_phlev = blob.size();
   for (int v : H.phase_lev) blob.push_back(uint32_t(v));
   pad16();
+  // 16-bit slot indices when every slot fits (halves the op stream)
+  const bool compact = H.total_slots() < 65536;
   const size_t o_vops = blob.size();
-  blob.insert(blob.end(), H.vrr_ops.begin(), H.vrr_ops.end());
+  if (compact) {
+    for (size_t i = 0; i < H.vrr_ops.size(); i += 8) {
+      const uint32_t* w = &H.vrr_ops[i];
+      blob.push_back(w[0] | (w[1] << 16));
+      blob.push_back(w[2] | (w[3] << 16));
+      blob.push_back(w[4] | (w[5] << 16));
+      blob.push_back(w[6]);
+    }
+  } else {
+    blob.insert(blob.end(), H.vrr_ops.begin(), H.vrr_ops.end());
+  }
   pad16();
   const size_t o_aops = blob.size();
   blob.insert(blob.end(), H.acc_ops.begin(), H.acc_ops.end());
   pad16();
   const size_t o_pops = blob.size();
-  blob.insert(blob.end(), H.post_ops.begin(), H.post_ops.end());
+  if (compact) {
+    for (size_t i = 0; i < H.post_ops.size(); i += 4) {
+      const uint32_t* w = &H.post_ops[i];
+      if (w[3] > 0xFFFFu) return fail(ctx, LGX_ERR_INVALID_ARG, "post op word out of range");
+      blob.push_back(w[0] | (w[1] << 16));
+      blob.push_back(w[2] | (w[3] << 16));
+    }
+  } else {
+    blob.insert(blob.end(), H.post_ops.begin(), H.post_ops.end());
+  }
   pad16();
   CK(pd->buf.ensure(blob.size() * 4));
   CK(cudaMemcpyAsync(pd->buf.p, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice,
@@ -307,9 +346,11 @@ lgx_status get_prog(lgx_context* ctx, int la, int lb, int lc, int ld, int deriv,
   D.acc_lev = reinterpret_cast<const int*>(base + o_alev);
   D.post_lev = reinterpret_cast<const int*>(base + o_plev);
   D.phase_lev = reinterpret_cast<const int*>(base + o_phlev);
+  D.compact = compact ? 1 : 0;
   D.vrr_ops = reinterpret_cast<const uint4*>(base + o_vops);
   D.acc_ops = reinterpret_cast<const uint2*>(base + o_aops);
   D.post_ops = reinterpret_cast<const uint4*>(base + o_pops);
+  D.post_ops_c = reinterpret_cast<const uint2*>(base + o_pops);
   *out = pd.get();
   ctx->progs.emplace(key, std::move(pd));
   return LGX_OK;
@@ -452,9 +493,20 @@ struct Launch {
 // shared memory to more resident warps) and warps per block, chosen for the
 // most resident warps per SM; rows_hint > 0 forces the row count.
 lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
-                       long long nwork, double nq_avg, int rows_hint, Launch& L) {
+                       long long nwork, double nq_avg, int rows_hint, bool gen, Launch& L) {
   const size_t elt = fp32 ? 4 : 8;
   L.stride = (P.host.total_slots() + 1) & ~1;
+  if (gen) {  // accumulators + VRR work, or accumulators + generated post regions
+    int nacc = 0, slots = 0;
+    post_info(P.host.la, P.host.lb, P.host.lc, P.host.ld, &nacc, &slots);
+    if (nacc != P.host.nacc)
+      return fail(ctx, LGX_ERR_INVALID_ARG, "generated post stage does not match the class program");
+    L.stride = (std::max(P.host.nacc + P.host.vrr_work, slots) + 1) & ~1;
+  }
+  auto occupancy = [&](int block, size_t smem) {
+    return gen ? post_blocks_per_sm(fp32, P.host.la, P.host.lb, P.host.lc, P.host.ld, block, smem)
+               : eri_blocks_per_sm(mode, fp32, block, smem);
+  };
   const size_t slot_bytes = size_t(L.stride) * elt;
   L.rows = rows_hint > 0 ? rows_hint : (nq_avg > 12 ? 32 : (nq_avg > 6 ? 16 : 8));
   const size_t stage = stage_bytes_per_warp(fp32, L.rows);
@@ -464,7 +516,7 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
   for (int wpb : {4, 2, 1}) {
     const size_t smem = wpb * (stage + (L.global ? 0 : slot_bytes));
     if (smem > smem_cap) continue;
-    const int b = std::max(1, eri_blocks_per_sm(mode, fp32, 32 * wpb, smem));
+    const int b = std::max(1, occupancy(32 * wpb, smem));
     if (b * wpb > best_warps) {
       best_warps = b * wpb;
       bps = b;
@@ -476,7 +528,7 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
     L.global = true;
     L.wpb = 4;
     L.smem = L.wpb * stage;
-    bps = std::max(1, eri_blocks_per_sm(mode, fp32, 32 * L.wpb, L.smem));
+    bps = std::max(1, occupancy(32 * L.wpb, L.smem));
   }
   L.block = 32 * L.wpb;
   long long grid = (long long)ctx->nsm * bps;
@@ -511,6 +563,7 @@ void fill_common(const lgx_context* ctx, const BasisDev& B, EriArgs& a) {
   a.boys = ctx->boys.as<double>();
   a.boys_tay = ctx->boys_tay.as<double>();
   a.boys32 = ctx->boys32.as<float>();
+  a.inv_odd = ctx->inv_odd.as<double>();
   a.sph_off = ctx->sph_off.as<int>();
   a.sph_c = ctx->sph_c.as<int>();
   a.sph_cd = ctx->sph_cd.as<double>();
@@ -532,21 +585,42 @@ int choose_group(double nq_avg) {
   return g;
 }
 
+bool post_gen_ok(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode) {
+  int nacc = 0, slots = 0;
+  return ctx->use_post && mode == kModeJK && B.std_pure && P.host.deriv == 0 &&
+         post_info(P.host.la, P.host.lb, P.host.lc, P.host.ld, &nacc, &slots);
+}
+
+// Default variant of a class bin (before or without tuning).
+Variant default_variant(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode,
+                        bool fp32, bool implicit, double nq_avg) {
+  Variant v;
+  if (rk_eligible(ctx, B, P, mode, fp32)) {
+    v.kind = 0;
+    v.group = implicit ? 1 : choose_group(nq_avg);
+  } else {
+    v.kind = post_gen_ok(ctx, B, P, mode) ? 2 : 1;
+  }
+  return v;
+}
+
 lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
-                  EriArgs a, long long nwork, double nq_avg) {
+                  EriArgs a, long long nwork, int group) {
   fill_common(ctx, B, a);
-  a.group = a.implicit ? 1 : choose_group(nq_avg);
+  a.group = group;
   CK(rk_launch(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, nwork, ctx->nsm,
                ctx->stream));
   return LGX_OK;
 }
 
 lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
-                   EriArgs a, long long nwork, double nq_avg = 1.0) {
-  if (rk_eligible(ctx, B, P, mode, fp32))
-    return run_rk(ctx, B, P, mode, fp32, a, nwork, nq_avg);
+                   EriArgs a, long long nwork, double nq_avg = 1.0,
+                   const Variant* var = nullptr) {
+  const Variant v = var ? *var : default_variant(ctx, B, P, mode, fp32, a.implicit, nq_avg);
+  if (v.kind == 0) return run_rk(ctx, B, P, mode, fp32, a, nwork, v.group);
+  const bool gen = v.kind == 2;
   Launch L;
-  lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, nq_avg, 0, L);
+  lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, nq_avg, v.rows, gen, L);
   if (s != LGX_OK) return s;
   fill_common(ctx, B, a);
   a.prog = P.dev;
@@ -559,7 +633,11 @@ lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bo
   a.chunk = int(std::max<long long>(1, std::min<long long>(32, nwork / (nwarps * 8))));
   a.max_chunks = nwork / a.chunk + 2;
   CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream));
-  CK(launch_eri(a, mode, fp32, L.grid, L.block, L.smem, ctx->stream));
+  if (gen)
+    CK(post_launch(fp32, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, L.grid, L.block, L.smem,
+                   ctx->stream));
+  else
+    CK(launch_eri(a, mode, fp32, L.grid, L.block, L.smem, ctx->stream));
   return LGX_OK;
 }
 
@@ -867,6 +945,100 @@ double sph_flops(int la, int lb, int lc, int ld, const int* pure) {
   return f;
 }
 
+int tune_key(const BinHost& bin, int deriv, int mode, bool fp32) {
+  return ((class_index(bin.la, bin.lb, bin.lc, bin.ld) * 2 + deriv) * 4 + mode) * 2 + (fp32 ? 1 : 0);
+}
+
+// Work description of precision space sp of a class bin.
+void bin_args(const BinCache& C, const BinHost& bin, int sp, EriArgs& a) {
+  a.implicit = 1;
+  a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
+  a.bin.ket_pairs = C.class_lists.as<int>() + C.class_off[bin.ket_class];
+  a.bin.seg_start = bin.seg_start[sp].as<long long>();
+  a.bin.seg_bra = bin.seg_bra[sp].as<int>();
+  a.bin.seg_j0 = bin.seg_j0[sp].as<int>();
+  a.bin.nseg = bin.nseg[sp];
+  a.bin.total = bin.total[sp];
+}
+
+// Per-class launch-shape autotuner: for every (class, precision) of the
+// pass without a tuned variant, times the candidate variants (register
+// kernel lanes per quartet; program kernel with interpreted or generated
+// post stage and its staging rows) on a leading sample of the bin's
+// quartets, into scratch accumulators, and keeps the fastest.  Runs once per
+// basis; later passes reuse the choice.
+lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
+                     EriArgs base) {
+  if (!ctx->tune || ctx->noalloc) return LGX_OK;
+  const BinCache& C = ctx->bins;
+  const size_t nn = std::max(size_t(B.nbf) * B.nbf, size_t(3 * B.natoms + 64));
+  bool scratch = false;
+  for (size_t bi = 0; bi < C.bins.size(); ++bi) {
+    const BinHost& bin = *C.bins[bi];
+    ProgDev* P = nullptr;
+    lgx_status s = get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
+    if (s != LGX_OK) return s;
+    for (int sp = 0; sp < 2; ++sp) {
+      if (bin.total[sp] == 0) continue;
+      const bool fp32 = (sp == 1) && allow_fp32;
+      const int key = tune_key(bin, deriv, mode, fp32);
+      if (ctx->tuned.count(key)) continue;
+      std::vector<Variant> cand;
+      const Variant d = default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
+      cand.push_back(d);
+      if (d.kind == 0) {
+        for (int g = 2; g <= 8 && g <= 2 * bin.nq_avg; g *= 2) cand.push_back({0, g, 0});
+      } else {
+        for (int kind = 1; kind <= d.kind; ++kind) {
+          cand.push_back({kind, 1, 8});
+          if (bin.nq_avg > 4) cand.push_back({kind, 1, 32});
+        }
+      }
+      const long long cap = d.kind == 0 ? (1LL << 22) : (1LL << 17);
+      const long long sample = std::min<long long>(bin.total[sp], cap);
+      if (cand.size() < 2 || sample < ctx->tune_min) {
+        ctx->tuned[key] = d;
+        continue;
+      }
+      if (!scratch) {
+        CK(ctx->tuneJ.ensure(nn * sizeof(double)));
+        CK(ctx->tuneK.ensure(nn * sizeof(double)));
+        scratch = true;
+      }
+      EriArgs a = base;
+      bin_args(C, bin, sp, a);
+      a.bin.total = sample;
+      a.prim_count = nullptr;
+      if (mode == kModeJK) {
+        a.Jacc = ctx->tuneJ.as<double>();
+        a.Kacc = ctx->tuneK.as<double>();
+      } else {
+        a.gJ = ctx->tuneJ.as<double>();
+        a.gK = ctx->tuneK.as<double>();
+      }
+      float best = 0;
+      Variant bestv = d;
+      for (size_t ci = 0; ci < cand.size(); ++ci) {
+        float ms = 0;
+        for (int rep = 0; rep < 2; ++rep) {  // the second run is timed
+          CK(cudaEventRecord(ctx->ev0, ctx->stream));
+          s = run_eri(ctx, B, *P, mode, fp32, a, sample, bin.nq_avg, &cand[ci]);
+          if (s != LGX_OK) return s;
+          CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        }
+        CK(cudaEventSynchronize(ctx->ev1));
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        if (ci == 0 || ms < best) {
+          best = ms;
+          bestv = cand[ci];
+        }
+      }
+      ctx->tuned[key] = bestv;
+    }
+  }
+  return check_errflag(ctx);
+}
+
 lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
                     EriArgs base, lgx_jk_stats* stats) {
   BinCache& C = ctx->bins;
@@ -878,7 +1050,7 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
   }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   long long integrals = 0, launches = 0;
-  struct Rec { int bin, sp; bool fp32; };
+  struct Rec { int bin, sp; bool fp32; Variant v; };
   std::vector<Rec> recs;
   // LGX_CLASS_PROFILE=1: per-launch device times, printed per class bin
   // (the counterpart of libint's per-class Engine timers, engine.h:862-890)
@@ -893,26 +1065,23 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       if (bin.total[sp] == 0) continue;
       const bool fp32 = (sp == 1) && allow_fp32;
       EriArgs a = base;
-      a.implicit = 1;
-      a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
-      a.bin.ket_pairs = C.class_lists.as<int>() + C.class_off[bin.ket_class];
-      a.bin.seg_start = bin.seg_start[sp].as<long long>();
-      a.bin.seg_bra = bin.seg_bra[sp].as<int>();
-      a.bin.seg_j0 = bin.seg_j0[sp].as<int>();
-      a.bin.nseg = bin.nseg[sp];
-      a.bin.total = bin.total[sp];
+      bin_args(C, bin, sp, a);
       a.prim_count = count ? ctx->primcount.as<unsigned long long>() + 2 * bi + sp : nullptr;
+      const auto tv = ctx->tuned.find(tune_key(bin, deriv, mode, fp32));
+      const Variant v = tv != ctx->tuned.end()
+                            ? tv->second
+                            : default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
       if (prof) {
         cudaEvent_t e0;
         CK(cudaEventCreate(&e0));
         CK(cudaEventRecord(e0, ctx->stream));
         pev.push_back(e0);
       }
-      s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg);
+      s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg, &v);
       if (s != LGX_OK) return s;
       integrals += bin.integrals[sp];
       ++launches;
-      recs.push_back({int(bi), sp, fp32});
+      recs.push_back({int(bi), sp, fp32, v});
     }
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -928,7 +1097,10 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
       const BinHost& bin = *C.bins[recs[i].bin];
       ProgDev* P = nullptr;
       get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
-      const bool rk = rk_eligible(ctx, B, *P, mode, recs[i].fp32);
+      const Variant& v = recs[i].v;
+      char kind[32];
+      if (v.kind == 0) snprintf(kind, sizeof(kind), "rk/G%d", v.group);
+      else snprintf(kind, sizeof(kind), "%s/R%d", v.kind == 2 ? "gen" : "prog", v.rows);
       const int pure[4] = {bin.la > 1, bin.lb > 1, bin.lc > 1, bin.ld > 1};
       const double np = double(pcp[2 * recs[i].bin + recs[i].sp]);
       const double gflop = 1e-9 * (np * double(P->host.vrr_flops) +
@@ -937,7 +1109,7 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
                                         (deriv ? 12 : 1) * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure)));
       fprintf(stderr, "lgx-class (%d%d|%d%d) %s %s quartets %lld prims %.0f nq_avg %.1f  %.3f ms"
               "  %.1f GFLOP %.3f TFLOP/s\n",
-              bin.la, bin.lb, bin.lc, bin.ld, recs[i].fp32 ? "fp32" : "fp64", rk ? "rk" : "prog",
+              bin.la, bin.lb, bin.lc, bin.ld, recs[i].fp32 ? "fp32" : "fp64", kind,
               (long long)bin.total[recs[i].sp], np, bin.nq_avg, ms, gflop, gflop / ms);
       cudaEventDestroy(pev[i]);
     }
@@ -1066,8 +1238,16 @@ lgx_status lgx_create(lgx_context** out, int device) {
     CK(c->boys32.ensure(boysf.size() * sizeof(float)));
     CK(cudaMemcpy(c->boys32.p, boysf.data(), boysf.size() * sizeof(float), cudaMemcpyHostToDevice));
     if (const char* e = getenv("LGX_DISABLE_RK")) c->use_rk = (e[0] == '0');
+    if (const char* e = getenv("LGX_DISABLE_POST")) c->use_post = (e[0] == '0');
+    if (const char* e = getenv("LGX_TUNE")) c->tune = (e[0] != '0');
+    if (const char* e = getenv("LGX_TUNE_MIN")) c->tune_min = std::max(1LL, atoll(e));
 
-    CK(set_inv_odd_table());
+    {
+      double h[40];
+      for (int m = 0; m < 40; ++m) h[m] = 1.0 / (2 * m + 1);
+      CK(c->inv_odd.ensure(sizeof(h)));
+      CK(cudaMemcpy(c->inv_odd.p, h, sizeof(h), cudaMemcpyHostToDevice));
+    }
     CK(c->counter.ensure(64));
     CK(c->errflag.ensure(64));
     CK(c->primcount.ensure(64));
@@ -1155,6 +1335,7 @@ lgx_status lgx_set_basis(lgx_context* ctx, int nshell, const int32_t* l, const i
   std::lock_guard<std::mutex> lk(ctx->mu);
   CK(cudaSetDevice(ctx->device));
   ctx->bins.valid = false;
+  ctx->tuned.clear();
   return upload_basis(ctx, ctx->basis, nshell, l, pure, nprim, atom, origins, alpha, coeff);
 }
 
@@ -1249,13 +1430,7 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   const size_t nn = size_t(B.nbf) * B.nbf;
   CK(ctx->Jacc.ensure(nn * sizeof(double)));
   CK(ctx->Kacc.ensure(nn * sizeof(double)));
-  CK(cudaEventRecord(ctx->ev2, ctx->stream));
-  CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
-  CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
-  if (mode == LGX_MIXED) {
-    CK(ctx->Df.ensure(nn * sizeof(float)));
-    CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
-  }
+  if (mode == LGX_MIXED) CK(ctx->Df.ensure(nn * sizeof(float)));
   EriArgs a{};
   a.precision = eps;
   a.ln_prec = std::log(eps);
@@ -1265,6 +1440,13 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   a.Jacc = ctx->Jacc.as<double>();
   a.Kacc = ctx->Kacc.as<double>();
   a.nbf = B.nbf;
+  if (mode == LGX_MIXED) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
+  s = tune_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a);
+  if (s != LGX_OK) return s;
+  CK(cudaEventRecord(ctx->ev2, ctx->stream));
+  CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
+  if (mode == LGX_MIXED) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
   s = run_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, stats);
   if (s != LGX_OK) return s;
   CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
@@ -1427,6 +1609,8 @@ lgx_status lgx_jk_grad(lgx_context* ctx, const double* D, double* gJ, double* gK
   a.gJ = ctx->gJ.as<double>();
   a.gK = ctx->gK.as<double>();
   a.nbf = B.nbf;
+  s = tune_bins(ctx, B, kModeGrad, 1, false, a);
+  if (s != LGX_OK) return s;
   s = run_bins(ctx, B, kModeGrad, 1, false, a, stats);
   if (s != LGX_OK) return s;
   CK(cudaMemcpyAsync(gJ, ctx->gJ.p, 3 * natoms * sizeof(double), cudaMemcpyDeviceToHost,

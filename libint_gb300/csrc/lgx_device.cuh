@@ -98,11 +98,16 @@ struct DevProg {
   int nlev, npost_lev;
   const int* vrr_lev;
   const int* acc_lev;
-  const uint4* vrr_ops;  // 2 uint4 per op
+  // compact != 0 (every slot index < 65536): a VRR op is one uint4
+  // {dst | s1<<16, s2 | s3<<16, s4 | s5<<16, flags} and a post op one uint2
+  // {dst | s1<<16, s2 | word<<16}; otherwise two uint4 / one uint4 per op.
+  int compact;
+  const uint4* vrr_ops;
   const uint2* acc_ops;
   const int* post_lev;
   const int* phase_lev;
   const uint4* post_ops;
+  const uint2* post_ops_c;
 };
 
 // Spherical-harmonic coefficient tables, dense [l][2l+1][ncart(l)], l <= 3.

@@ -56,6 +56,7 @@ struct EriArgs {
   const double* boys;     // [kBoysRows][kBoysCols] F_m(T_k)
   const double* boys_tay; // pre-divided Taylor table (kBoysTaylorStride)
   const float* boys32;    // FP32 copy of the Boys table
+  const double* inv_odd;  // 1/(2m+1), m < 40
   // Cartesian -> solid harmonics, sparse: nonzeros of row (l, p) are
   // [sph_off[l*9+p], sph_off[l*9+p+1]) with Cartesian index sph_c[] and
   // coefficient sph_cd[] (FP64) / sph_cf[] (FP32)

@@ -457,6 +457,7 @@ ClassProgramHost build_class_program(int la, int lb, int lc, int ld, int deriv) 
   }
   const int post_work = (temps0 - nacc) + std::max(post_high, P.ncart4);
   P.nwork = std::max(vrr_work, post_work);
+  P.vrr_work = vrr_work;
   slot32(P.nacc + P.nwork);
   return P;
 }

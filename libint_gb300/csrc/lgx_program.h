@@ -48,6 +48,7 @@ struct ClassProgramHost {
   int la, lb, lc, ld, deriv, mmax, nweights;
   int nacc;          // accumulator slots [0, nacc)
   int nwork;         // work slots [nacc, nacc + nwork)
+  int vrr_work;      // of which the VRR stage uses [nacc, nacc + vrr_work)
   int leaf_slot0;    // F_m * pfac written to leaf_slot0 + m
   int nphases;       // post phases: 1 (deriv 0) or 3 (centres A, B, D)
   int sets_per_phase;// Cartesian sets produced per phase: 1 or 3 (x, y, z)

@@ -172,3 +172,40 @@ def test_gradient_vs_oracle_and_fd(lgx, oracle_mod, water2):
         assert abs(fdJ - gJ[at, x]) < 1e-6, (fdJ, gJ[at, x])
         assert abs(fdK - gK[at, x]) < 1e-6, (fdK, gK[at, x])
     ctx.close()
+
+
+@pytest.fixture(scope="module")
+def water_tz(lgx, oracle_mod):
+    atoms = lgx.water_cluster(1, 1, 1, seed=4)
+    bs = lgx.BasisSet("cc-pVTZ", atoms)
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    D = lgx.random_density(bs.nbf, 5, seed=5)
+    return atoms, bs, ob, D
+
+
+@pytest.mark.parametrize("variant", ["tuned", "interpreted_post"])
+def test_jk_tz_vs_oracle(lgx, oracle_mod, water_tz, monkeypatch, variant):
+    # cc-pVTZ reaches the f classes: (ff|ff) and the other L > 6 classes run
+    # on the program kernel, with the generated post stages unless disabled
+    if variant == "interpreted_post":
+        monkeypatch.setenv("LGX_DISABLE_POST", "1")
+    else:  # tune every class bin, however small
+        monkeypatch.setenv("LGX_TUNE_MIN", "1")
+    _, bs, ob, D = water_tz
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    J, K, st = ctx.jk(D, schwarz_thresh=1e-12)
+    Kq = oracle_mod.schwarz(ob)
+    Jr, Kr, nq = oracle_mod.jk(ob, D, Kq, 1e-12)
+    assert st.quartets_fp64 == nq
+    assert np.max(np.abs(J - Jr)) < 1e-11
+    assert np.max(np.abs(K - Kr)) < 1e-11
+    # a second pass reuses the tuned variants and gives the same result
+    J2, K2, _ = ctx.jk(D, schwarz_thresh=1e-12)
+    assert np.max(np.abs(J2 - J)) < 1e-12 and np.max(np.abs(K2 - K)) < 1e-12
+    Jm, Km, stm = ctx.jk(D, 1e-12, mode=1, mixed_thresh=1e-4)
+    assert stm.quartets_fp32 > 0
+    e64 = lgx.jk_energies(D, J, K)
+    em = lgx.jk_energies(D, Jm, Km)
+    assert abs(e64[0] - em[0]) <= 1e-8 and abs(e64[1] - em[1]) <= 1e-8
+    ctx.close()
