@@ -209,3 +209,24 @@ def test_jk_tz_vs_oracle(lgx, oracle_mod, water_tz, monkeypatch, variant):
     em = lgx.jk_energies(D, Jm, Km)
     assert abs(e64[0] - em[0]) <= 1e-8 and abs(e64[1] - em[1]) <= 1e-8
     ctx.close()
+
+
+def test_jk_graph_replay_matches_eager(lgx, water2, monkeypatch):
+    # the second pass with the same settings replays the captured CUDA graph;
+    # it must see the new density and match a pass without graphs
+    _, bs, _, D = water2
+    D2 = lgx.random_density(bs.nbf, 10, seed=7)
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    for mode in (0, 1):
+        ctx.jk(D, 1e-12, mode=mode)                   # eager, then captured
+        J2, K2, st = ctx.jk(D2, 1e-12, mode=mode)     # graph replay
+        assert st.pass_ms > 0 and st.integrals > 0
+        monkeypatch.setenv("LGX_GRAPHS", "0")
+        ref = lgx.Context(0)
+        ref.set_basis(bs)
+        Jr, Kr, _ = ref.jk(D2, 1e-12, mode=mode)
+        ref.close()
+        monkeypatch.delenv("LGX_GRAPHS")
+        assert np.max(np.abs(J2 - Jr)) < 1e-12 and np.max(np.abs(K2 - Kr)) < 1e-12
+    ctx.close()
