@@ -31,6 +31,8 @@ cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t 
 cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
                       long long work, int nsm, cudaStream_t st);
 bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
+cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
+                              PrimPairJK32* out, cudaStream_t st);
 cudaError_t post_launch(bool fp32, int la, int lb, int lc, int ld, const EriArgs& a, int grid,
                         int block, size_t smem, cudaStream_t st);
 int post_blocks_per_sm(bool fp32, int la, int lb, int lc, int ld, int block, size_t smem);
@@ -106,6 +108,7 @@ struct BasisDev {
   long long npp = 0;
   DBuf pairs, pprims, pp_pair, pair_swap;
   bool pairs_ok = false;
+  unsigned long long pairs_version = 0;  // bumped whenever pprims is rewritten
   double pairs_lnprec = 0;
   int pairs_method = -1;
   // Schwarz
@@ -132,6 +135,10 @@ struct BinCache {
   int mode = -1;
   DBuf class_lists;                 // pair ids of every pair class, sorted
   std::vector<long long> class_off; // offsets of each class in class_lists
+  // FP32 records per list position (PrimPairJK32 layout) and their source
+  DBuf rec_idx, rec_src, recs;
+  long long nrec = 0;
+  unsigned long long rec_version = ~0ull;  // pairs_version the records hold
   std::vector<std::unique_ptr<BinHost>> bins;
   long long quartets[2] = {0, 0};
 };
@@ -502,12 +509,23 @@ lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t
   return LGX_OK;
 }
 
+// FP32 J/K records of the current bins from the current primitive pairs.
+lgx_status ensure_jk_records(lgx_context* ctx, BasisDev& B) {
+  BinCache& C = ctx->bins;
+  if (C.rec_version == B.pairs_version) return LGX_OK;
+  CK(launch_jk_records(B.pprims.as<PrimPairRec>(), C.rec_src.as<int>(), C.nrec,
+                       C.recs.as<PrimPairJK32>(), ctx->stream));
+  C.rec_version = B.pairs_version;
+  return LGX_OK;
+}
+
 lgx_status ensure_pairs(lgx_context* ctx, BasisDev& B, double ln_prec, int method) {
   if (B.pairs_ok && B.pairs_lnprec == ln_prec && B.pairs_method == method) return LGX_OK;
   CK(launch_shellpairs(B.dev, B.pairs.as<PairRec>(), int(B.hpairs.size()),
                        B.pprims.as<PrimPairRec>(), B.pp_pair.as<int>(), B.npp, ln_prec,
                        method, ctx->stream));
   B.pairs_ok = true;
+  ++B.pairs_version;
   B.pairs_lnprec = ln_prec;
   B.pairs_method = method;
   return LGX_OK;
@@ -863,6 +881,43 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
   if (!flat.empty())
     CK(cudaMemcpyAsync(C.class_lists.p, flat.data(), flat.size() * sizeof(int),
                        cudaMemcpyHostToDevice, ctx->stream));
+  {
+    // FP32 record layout: per class, per depth group [g0, g1) of npp n, the
+    // record of (position i, primitive pair ip) at base + ip * (g1 - g0) + (i - g0)
+    std::vector<int2> idx(std::max<size_t>(1, flat.size()));
+    std::vector<int> src;
+    for (int c = 0; c < 10; ++c) {
+      const auto& v = lists[c];
+      const auto& g = groups[c];
+      for (size_t gi = 0; gi + 1 < g.size(); ++gi) {
+        const int g0 = g[gi], g1 = g[gi + 1];
+        if (g1 <= g0) continue;
+        const int n = B.hpairs[v[g0]].npp;
+        const long long base = (long long)src.size();
+        if (base + (long long)n * (g1 - g0) > std::numeric_limits<int>::max())
+          return fail(ctx, LGX_ERR_TOO_LARGE, "too many primitive-pair records");
+        src.resize(base + (size_t)n * (g1 - g0));
+        for (int i = g0; i < g1; ++i) {
+          const int pr = v[i];
+          idx[C.class_off[c] + i] = make_int2(int(base + (i - g0)), g1 - g0);
+          const unsigned sw = B.hswap[pr] ? 0x80000000u : 0u;
+          for (int ip = 0; ip < n; ++ip)
+            src[base + (size_t)ip * (g1 - g0) + (i - g0)] =
+                int(unsigned(B.hpairs[pr].pp_off + ip) | sw);
+        }
+      }
+    }
+    C.nrec = (long long)src.size();
+    CK(C.rec_idx.ensure(idx.size() * sizeof(int2)));
+    CK(C.rec_src.ensure(std::max<size_t>(1, src.size()) * sizeof(int)));
+    CK(C.recs.ensure(std::max<size_t>(1, src.size()) * sizeof(PrimPairJK32)));
+    CK(cudaMemcpyAsync(C.rec_idx.p, idx.data(), idx.size() * sizeof(int2),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    if (!src.empty())
+      CK(cudaMemcpyAsync(C.rec_src.p, src.data(), src.size() * sizeof(int),
+                         cudaMemcpyHostToDevice, ctx->stream));
+    C.rec_version = ~0ull;
+  }
   int cls_l[10][2];
   for (int lhi = 0; lhi <= 3; ++lhi)
     for (int llo = 0; llo <= lhi; ++llo) {
@@ -986,6 +1041,9 @@ int tune_key(const BinHost& bin, int deriv, int mode, bool fp32) {
 // Work description of precision space sp of a class bin.
 void bin_args(const BinCache& C, const BinHost& bin, int sp, EriArgs& a) {
   a.implicit = 1;
+  a.jk32 = C.recs.as<PrimPairJK32>();
+  a.bin.bra_rec = C.rec_idx.as<int2>() + C.class_off[bin.bra_class];
+  a.bin.ket_rec = C.rec_idx.as<int2>() + C.class_off[bin.ket_class];
   a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
   a.bin.ket_pairs = C.class_lists.as<int>() + C.class_off[bin.ket_class];
   a.bin.seg_start = bin.seg_start[sp].as<long long>();
@@ -1499,6 +1557,8 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   const double eps = std::numeric_limits<double>::epsilon();
   s = ensure_pairs(ctx, B, std::log(eps), 0);
   if (s != LGX_OK) return s;
+  s = ensure_jk_records(ctx, B);
+  if (s != LGX_OK) return s;
   const size_t nn = size_t(B.nbf) * B.nbf;
   CK(ctx->Jacc.ensure(nn * sizeof(double)));
   CK(ctx->Kacc.ensure(nn * sizeof(double)));
@@ -1648,6 +1708,8 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   lgx_status s = noalloc_scratch(ctx, &scratch);
   if (s != LGX_OK) return s;
   NoAllocGuard guard(ctx);
+  s = ensure_jk_records(ctx, B);
+  if (s != LGX_OK) return s;
   const size_t nn = size_t(B.nbf) * B.nbf;
   double* Jacc = reinterpret_cast<double*>(scratch);
   double* Kacc = Jacc + kNoAllocN;
@@ -1718,6 +1780,8 @@ lgx_status lgx_jk_grad(lgx_context* ctx, const double* D, double* gJ, double* gK
   if (s != LGX_OK) return s;
   const double eps = std::numeric_limits<double>::epsilon();
   s = ensure_pairs(ctx, B, std::log(eps), 0);
+  if (s != LGX_OK) return s;
+  s = ensure_jk_records(ctx, B);
   if (s != LGX_OK) return s;
   const size_t nn = size_t(B.nbf) * B.nbf;
   CK(ctx->Dd.ensure(nn * sizeof(double)));

@@ -84,6 +84,17 @@ struct __align__(16) PrimPairRec {
 };
 static_assert(sizeof(PrimPairRec) == 128, "PrimPairRec layout");
 
+// FP32 primitive-pair record of the J/K bins (two float4): {K c1 c2,
+// zeta, 1/zeta, ln screening factor} and {P - O(first canonical centre),
+// Conservative factor}.  The records of one pair class are laid out
+// [depth group][primitive pair][position in the group], so the lanes that
+// take consecutive ket pairs of a segment read consecutive addresses.
+struct __align__(16) PrimPairJK32 {
+  float4 k;
+  float4 pa;
+};
+static_assert(sizeof(PrimPairJK32) == 32, "PrimPairJK32 layout");
+
 // A shell pair with its primitive-pair range (pair list, shell.h:1079-1329).
 struct PairRec {
   int s1, s2;       // shell indices as stored

@@ -73,6 +73,30 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, P
   pp[t] = r;
 }
 
+// FP32 J/K records: record r takes primitive pair src[r] & 0x7fffffff,
+// oriented on its second centre when the sign bit is set.
+__global__ void jk_records_kernel(const PrimPairRec* __restrict__ pp, const int* __restrict__ src,
+                                  long long n, PrimPairJK32* __restrict__ out) {
+  const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const unsigned v = unsigned(src[r]);
+  const PrimPairRec& q = pp[v & 0x7fffffffu];
+  const bool sw = (v >> 31) != 0;
+  PrimPairJK32 o;
+  o.k = make_float4(q.fKc, q.fzeta, q.foog, q.fln_scr);
+  o.pa = sw ? make_float4(q.fPA2[0], q.fPA2[1], q.fPA2[2], q.fnonsph)
+            : make_float4(q.fPA1[0], q.fPA1[1], q.fPA1[2], q.fnonsph);
+  out[r] = o;
+}
+
+cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
+                              PrimPairJK32* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int block = 256;
+  jk_records_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(pp, src, n, out);
+  return cudaGetLastError();
+}
+
 // J = (Jacc + Jacc^T)/4, K = (Kacc + Kacc^T)/8 (hartree-fock++.cc:1766 with
 // the G = 2J - K split).
 __global__ void jk_finalize_kernel(const double* Jacc, const double* Kacc, double* J, double* K,

@@ -35,6 +35,9 @@ struct BinWork {
   int nseg;
   int pad;
   long long total;
+  // FP32 records (EriArgs::jk32) of list position i: jk32[rec[i].x + ip * rec[i].y]
+  const int2* bra_rec;
+  const int2* ket_rec;
 };
 
 // Segment containing quartet q (binary search over seg_start).
@@ -51,6 +54,7 @@ struct EriArgs {
   DevBasis basis;
   const PairRec* pairs;
   const PrimPairRec* pprims;
+  const PrimPairJK32* jk32;  // J/K bins: coalesced FP32 records (may be null)
   const unsigned char* pair_swap;  // per pair: 1 if its canonical bra1 is s2
   DevProg prog;
   const double* boys;     // [kBoysRows][kBoysCols] F_m(T_k)

@@ -193,21 +193,43 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double
   return true;
 }
 
+// FP32 primitive pair in the quartet's orientation: {K c1 c2, zeta,
+// 1/zeta, ln screen} and P minus its first canonical centre.
+struct PrimF32 {
+  float4 k;
+  float4 pa;
+};
+
+// From the coalesced J/K records (one 32-byte record, two vector loads).
+__device__ __forceinline__ PrimF32 rk_rec32(const PrimPairJK32* r) {
+  PrimF32 p;
+  p.k = __ldg(&r->k);
+  p.pa = __ldg(&r->pa);
+  return p;
+}
+
+// From the general primitive-pair table (explicit quartet lists).
+__device__ __forceinline__ PrimF32 rk_pp32(const PrimPairRec& r, bool sw) {
+  PrimF32 p;
+  p.k = make_float4(r.fKc, r.fzeta, r.foog, r.fln_scr);
+  const float* PA = sw ? r.fPA2 : r.fPA1;
+  p.pa = make_float4(PA[0], PA[1], PA[2], r.fnonsph);
+  return p;
+}
+
 // One primitive quartet into acc (FP32).  AC = A - C of the quartet.
 template <class C>
-__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>& q, int ib,
-                                        int ik, float* acc) {
-  const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
-  const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
-  if (!(bp.fln_scr + kp.fln_scr > a.fln_prec)) return false;
-  const float zeta = bp.fzeta, eta = kp.fzeta;
+__device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>& q,
+                                        const PrimF32& bp, const PrimF32& kp, float* acc) {
+  if (!(bp.k.w + kp.k.w > a.fln_prec)) return false;
+  const float zeta = bp.k.y, eta = kp.k.y;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
-  const float pfac = bp.fKc * kp.fKc * rs;
+  const float pfac = bp.k.x * kp.k.x * rs;
   if (fabsf(pfac) < a.fprecision) return false;
-  const float* PA = q.bsw ? bp.fPA2 : bp.fPA1;
-  const float* QC = q.ksw ? kp.fPA2 : kp.fPA1;
+  const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
+  const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
               PQz = PA[2] - QC[2] + q.AC[2];
   const float rho = zeta * eta * oogpq;
@@ -222,9 +244,9 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
   g.QCx = QC[0]; g.QCy = QC[1]; g.QCz = QC[2];
   g.WPx = -ez * PQx; g.WPy = -ez * PQy; g.WPz = -ez * PQz;
   g.WQx = zz * PQx; g.WQy = zz * PQy; g.WQz = zz * PQz;
-  g.oo2z = 0.5f * bp.foog;
+  g.oo2z = 0.5f * bp.k.z;
   g.roz = ez;
-  g.oo2e = 0.5f * kp.foog;
+  g.oo2e = 0.5f * kp.k.z;
   g.roe = zz;
   g.oo2ze = 0.5f * oogpq;
   C::template vrr<float>(F, g, acc);
@@ -270,11 +292,17 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
     if (qi >= total) continue;
     int bpair, kpair, flags, orig = 0;
     long long outoff = 0;
+    int2 brec = make_int2(0, 0), krec = make_int2(0, 0);
     if (a.implicit) {
       const int seg = bin_segment(a.bin, qi);
       const int j = int(qi - a.bin.seg_start[seg]) + a.bin.seg_j0[seg];
-      bpair = a.bin.bra_pairs[a.bin.seg_bra[seg]];
+      const int bpos = a.bin.seg_bra[seg];
+      bpair = a.bin.bra_pairs[bpos];
       kpair = a.bin.ket_pairs[j];
+      if (sizeof(T) == 4 && a.jk32) {
+        brec = __ldg(a.bin.bra_rec + bpos);
+        krec = __ldg(a.bin.ket_rec + j);
+      }
       flags = (a.pair_swap[bpair] ? 1 : 0) | (a.pair_swap[kpair] ? 2 : 0);
     } else {
       const QuartetItem it = a.items[qi];
@@ -291,9 +319,27 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
     for (int i = 0; i < C::kNacc; ++i) acc[i] = T(0);
     const int nq = q.nbpp * q.nkpp;
     int kept = 0;
+    // primitive quartets g, g+G, ... as (bra, ket) primitive pairs, stepped
+    // without a division per step
+    int ib = g / q.nkpp, ik = g - ib * q.nkpp;
+    const int gb = G / q.nkpp, gk = G - gb * q.nkpp;
     for (int p = g; p < nq; p += G) {
-      const int ib = p / q.nkpp, ik = p - ib * q.nkpp;
-      kept += rk_prim<C>(a, q, ib, ik, acc) ? 1 : 0;
+      if constexpr (sizeof(T) == 4) {
+        const bool rec = a.implicit && a.jk32;
+        const PrimF32 bp = rec ? rk_rec32(a.jk32 + brec.x + ib * brec.y)
+                               : rk_pp32(a.pprims[q.bra_pp + ib], q.bsw);
+        const PrimF32 kp = rec ? rk_rec32(a.jk32 + krec.x + ik * krec.y)
+                               : rk_pp32(a.pprims[q.ket_pp + ik], q.ksw);
+        kept += rk_prim<C>(a, q, bp, kp, acc) ? 1 : 0;
+      } else {
+        kept += rk_prim<C>(a, q, ib, ik, acc) ? 1 : 0;
+      }
+      ib += gb;
+      ik += gk;
+      if (ik >= q.nkpp) {
+        ik -= q.nkpp;
+        ++ib;
+      }
     }
     if (G > 1) {
       for (int o = G >> 1; o > 0; o >>= 1) {
