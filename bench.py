@@ -132,6 +132,54 @@ def measure_peaks(torch):
     return out
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# a class kernel in the timed pass, from an ncu launch list of this same
+# bench command on the full workload (one-pass metrics; the summary and the
+# command line are in profiles/launches_dram_jk_h2o32_cc-pvdz.md).  Keyed by
+# (workload, pass precision mode, kernel).  The traffic does not grow with
+# the primitive quartets (it is the cold read of the pair records, the
+# density and the Boys table), so it is not scaled to other workloads.
+NCU_TRAFFIC_BYTES = {
+    ("h2o32_cc-pvdz", "mixed", "rk_kernel<double,0,0,1,0,J/K>"): 11.6e6,
+    ("h2o32_cc-pvdz", "fp64", "rk_kernel<double,0,0,1,0,J/K>"): 29.9e6,
+    ("h2o32_cc-pvdz", "mixed", "rk_kernel<double,0,0,0,0,J/K>"): 8.2e6,
+    ("h2o32_cc-pvdz", "fp64", "rk_kernel<double,0,0,0,0,J/K>"): 19.1e6,
+}
+
+
+def kernel_name(r):
+    t = "float" if r["fp32"] else "double"
+    la, lb, lc, ld = r["class"]
+    if r["kernel"] == "register":
+        return "rk_kernel<%s,%d,%d,%d,%d,J/K>" % (t, la, lb, lc, ld)
+    post = "generated post (%d%d|%d%d)" % (la, lb, lc, ld) if "generated" in r["kernel"] \
+        else "interpreted post"
+    return "eri_warp_kernel<%s,J/K,%s>" % (t, post)
+
+
+def kernel_roofline(launches, peaks, workload, mode):
+    """Roofline of the dominant class launch of a pass (largest average
+    device time over the timed steps): its algorithmic FLOPs per launch over
+    its average duration, against the FP64 or FP32 pipe peak measured live
+    (cuBLAS DGEMM / SGEMM without TF32)."""
+    if not launches:
+        return None
+    r = max(launches, key=lambda x: x["ms_avg"])
+    total = sum(x["ms_avg"] for x in launches)
+    pipe = "fp32" if r["fp32"] else "fp64"
+    ach = r["flops"] / (r["ms_avg"] * 1e-3) / 1e12
+    name = kernel_name(r)
+    return {"bound": pipe + "-pipe", "kernel": name, "achieved": ach, "peak": peaks[pipe],
+            "unit": "TFLOP/s", "frac": ach / peaks[pipe],
+            "traffic": NCU_TRAFFIC_BYTES.get((workload, mode, name)),
+            "launch_ms": r["ms_avg"], "share_of_pass": r["ms_avg"] / total if total else None,
+            "flops_per_launch": r["flops"], "prim_quartets": r["prim_quartets"],
+            "quartets": r["quartets"],
+            "peak_source": "cuBLAS %s measured live in this run (MEASURED_PEAKS.json holds "
+                           "only HBM and bf16 figures)" % ("SGEMM, no TF32" if r["fp32"]
+                                                           else "DGEMM")}
+
+
 def cpu_baseline(bs, D, Kq, thresh, budget_s, nthreads=0):
     """Oracle J/K over bounded samples of bra shell pairs spread across the
     canonical quartet enumeration; returns ERIs/s and the sample size."""
@@ -222,7 +270,7 @@ def run_gpu(args):
         for _ in range(args.warmup):
             ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, mode, MIXED_THRESH)
         barrier()
-        ms, last = [], None
+        ms, last, launches = [], None, None
         t0 = time.perf_counter()
         for _ in range(args.steps):
             flush.zero_()
@@ -230,15 +278,27 @@ def run_gpu(args):
             last = ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, mode,
                                  MIXED_THRESH)
             ms.append(last.pass_ms)
+            # per-launch device times of this step (events between launches,
+            # recorded by the replayed pass graph itself)
+            rec = ctx.last_pass_launches()
+            if launches is None:
+                launches = rec
+                for r in launches:
+                    r["ms_sum"] = r["ms"]
+            else:
+                for r, x in zip(launches, rec):
+                    r["ms_sum"] += x["ms"]
         barrier()
         wall = time.perf_counter() - t0
-        return ms, last, wall
+        for r in launches or []:
+            r["ms_avg"] = r.pop("ms_sum") / args.steps
+        return ms, last, wall, launches
 
     peaks = measure_peaks(torch)
     with ClockSampler(local) as clk:
-        ms64, st64, wall64 = timed(lg._lgx.LGX_FP64)
+        ms64, st64, wall64, lau64 = timed(lg._lgx.LGX_FP64)
         J64, K64 = dJ.cpu().numpy(), dK.cpu().numpy()
-        msmx, stmx, wallmx = timed(lg._lgx.LGX_MIXED)
+        msmx, stmx, wallmx, laumx = timed(lg._lgx.LGX_MIXED)
         Jmx, Kmx = dJ.cpu().numpy(), dK.cpu().numpy()
     clocks = clk.summary()
 
@@ -277,13 +337,15 @@ def run_gpu(args):
     te2e -= time.perf_counter() - f0
     ve2e = world * st_e.integrals * args.steps / te2e
 
-    # roofline of the mixed pass: time at peak for its FP64 and FP32 work
+    # roofline of the whole mixed pass: time at peak for its FP64 and FP32 work
     fl64, fl32 = stmx.flops_fp64, stmx.flops_fp32
     t_min = fl64 / (peaks["fp64"] * 1e12) + fl32 / (peaks["fp32"] * 1e12)
     t_step = tmx / args.steps
     achieved = (fl64 + fl32) / t_step / 1e12
     peak_blend = (fl64 + fl32) / t_min / 1e12
     roof64 = st64.flops_fp64 / (t64 / args.steps) / 1e12
+    dom = kernel_roofline(laumx, peaks, args.workload, "mixed")
+    dom64 = kernel_roofline(lau64, peaks, args.workload, "fp64")
 
     if rank != 0:
         return 0
@@ -308,18 +370,21 @@ def run_gpu(args):
                    "prim_quartets_per_step": stmx.prim_quartets},
         "fp64": {"value": v64, "unit": "ERI/s", "ms_per_step": t64 / args.steps * 1e3,
                  "quartets": st64.quartets_fp64, "E_J": e64[0], "E_K": e64[1],
-                 "roofline": {"bound": "fp64-pipe", "achieved": roof64, "peak": peaks["fp64"],
-                              "unit": "TFLOP/s", "frac": roof64 / peaks["fp64"]}},
+                 "roofline": dom64,
+                 "roofline_pass": {"bound": "fp64-pipe", "achieved": roof64,
+                                   "peak": peaks["fp64"], "unit": "TFLOP/s",
+                                   "frac": roof64 / peaks["fp64"]}},
         "mixed_error": {"dE_J": abs(emx[0] - e64[0]), "dE_K": abs(emx[1] - e64[1]),
                         "max_abs_dJ": float(np.max(np.abs(Jmx - J64))),
                         "max_abs_dK": float(np.max(np.abs(Kmx - K64)))},
         "speedup_mixed_vs_fp64": vmx / v64,
-        "roofline": {"bound": "fp64+fp32 pipes", "achieved": achieved, "peak": peak_blend,
-                     "unit": "TFLOP/s", "frac": achieved / peak_blend, "traffic": None,
-                     "peak_source": "cuBLAS DGEMM %.2f / SGEMM(no TF32) %.1f TFLOP/s measured "
-                                    "live; blended by the pass's FP64/FP32 work" %
-                                    (peaks["fp64"], peaks["fp32"]),
-                     "flops_fp64": fl64, "flops_fp32": fl32},
+        "roofline": dom,
+        "roofline_pass": {"bound": "fp64+fp32 pipes", "achieved": achieved, "peak": peak_blend,
+                          "unit": "TFLOP/s", "frac": achieved / peak_blend,
+                          "peak_source": "cuBLAS DGEMM %.2f / SGEMM(no TF32) %.1f TFLOP/s "
+                                         "measured live; blended by the pass's FP64/FP32 work"
+                                         % (peaks["fp64"], peaks["fp32"]),
+                          "flops_fp64": fl64, "flops_fp32": fl32},
         "e2e": {"value": ve2e, "unit": "ERI/s", "h2d_bytes_per_step": nbf * nbf * 8,
                 "d2h_bytes_per_step": 2 * nbf * nbf * 8},
         "gpu_launches": int(stmx.launches) * args.steps + int(st64.launches) * args.steps,

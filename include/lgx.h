@@ -176,6 +176,34 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
                                  double* dK, double schwarz_thresh, int mode,
                                  double mixed_thresh, lgx_jk_stats* stats);
 
+/* Statistics of one class launch of the last J/K or gradient pass, the
+ * counterpart of libint's per-class Engine timers (LIBINT2_ENGINE_TIMERS,
+ * include/libint2/engine.h:862-890), which time the primitive prologue,
+ * the build and the transform per call; here one record per class bin and
+ * precision of a whole pass. */
+typedef struct {
+  int32_t la, lb, lc, ld;  /* angular momenta of the class (canonical order)  */
+  int32_t fp32;            /* 1: FP32 arithmetic, 0: FP64                     */
+  int32_t kernel;          /* 0: register kernel, 1: program kernel,
+                              2: program kernel with generated post stage    */
+  int32_t shape;           /* lanes per quartet (kernel 0) or staging rows    */
+  int32_t deriv;           /* derivative order of the pass                    */
+  int64_t quartets;        /* shell quartets of the launch                    */
+  int64_t prim_quartets;   /* primitive quartets entering the VRR             */
+  int64_t integrals;       /* shell-set values computed (per derivative set)  */
+  double flops;            /* algorithmic FP operations (FMA = 2)             */
+  double ms;               /* device time of the launch (CUDA events on the
+                              context's stream; -1 when not recorded)         */
+} lgx_launch_stats;
+
+/* Copies up to `max` per-launch records of the last lgx_jk / lgx_jk_device
+ * / lgx_jk_device_noalloc / lgx_jk_grad pass into `out` (launch order) and
+ * sets *n to the number of launches of that pass.  Timings come from events
+ * recorded between the launches, also when the pass replays its CUDA
+ * graph. */
+lgx_status lgx_last_pass_launches(lgx_context* ctx, lgx_launch_stats* out,
+                                  int max, int* n);
+
 /* Nuclear gradients of E_J = 1/2 sum D.J and E_K = -1/4 sum D.K from
  * deriv_order = 1 integrals (compute_2body_fock_deriv<1>,
  * hartree-fock++.cc:1776-2000, per-atom digestion :1909-1973).

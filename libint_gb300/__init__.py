@@ -346,6 +346,27 @@ class Context:
         self._check(st, "lgx_jk_grad")
         return gJ, gK, stats
 
+    _KERNELS = {0: "register", 1: "program", 2: "program+generated-post"}
+
+    def last_pass_launches(self):
+        """Per-launch records of the last J/K or gradient pass (launch
+        order): class, precision, kernel, quartets, primitive quartets,
+        algorithmic FLOPs and device time (ms) of each class launch."""
+        n = ctypes.c_int()
+        self._check(self._lib.lgx_last_pass_launches(self._h, None, 0, ctypes.byref(n)),
+                    "lgx_last_pass_launches")
+        arr = (_lgx.LgxLaunchStats * max(1, n.value))()
+        self._check(self._lib.lgx_last_pass_launches(self._h, arr, n.value, ctypes.byref(n)),
+                    "lgx_last_pass_launches")
+        out = []
+        for r in arr[:n.value]:
+            out.append({"class": (r.la, r.lb, r.lc, r.ld), "fp32": bool(r.fp32),
+                        "kernel": self._KERNELS.get(r.kernel, str(r.kernel)), "shape": r.shape,
+                        "deriv": r.deriv, "quartets": r.quartets,
+                        "prim_quartets": r.prim_quartets, "integrals": r.integrals,
+                        "flops": r.flops, "ms": r.ms})
+        return out
+
 
 _DEFAULT_CTX = None
 

@@ -44,6 +44,15 @@ class LgxJkStats(ctypes.Structure):
                 ("launches", ctypes.c_int64)]
 
 
+class LgxLaunchStats(ctypes.Structure):
+    _fields_ = [("la", ctypes.c_int32), ("lb", ctypes.c_int32), ("lc", ctypes.c_int32),
+                ("ld", ctypes.c_int32), ("fp32", ctypes.c_int32), ("kernel", ctypes.c_int32),
+                ("shape", ctypes.c_int32), ("deriv", ctypes.c_int32),
+                ("quartets", ctypes.c_int64), ("prim_quartets", ctypes.c_int64),
+                ("integrals", ctypes.c_int64), ("flops", ctypes.c_double),
+                ("ms", ctypes.c_double)]
+
+
 # Every symbol include/lgx.h declares, with its ctypes signature.
 SIGNATURES = {
     "lgx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
@@ -71,6 +80,8 @@ SIGNATURES = {
     "lgx_jk_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                              ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
+    "lgx_last_pass_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(LgxLaunchStats),
+                                              ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lgx_jk_grad": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int,
                                    ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
     "lgx_shell_normalize": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),

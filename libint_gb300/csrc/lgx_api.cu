@@ -165,6 +165,7 @@ struct PassRecs {
   long long integrals = 0, launches = 0;
   size_t nslots = 0;
   bool count = false;
+  bool timed = false;  // per-launch events were recorded (ctx->lev)
 };
 
 // Identity of a captured J/K pass: every pointer and setting its nodes use.
@@ -202,6 +203,11 @@ struct lgx_context {
   cudaGraphExec_t jk_exec = nullptr;
   PassKey jk_key;
   PassRecs jk_recs;
+  // per-launch timing events of the batched passes (recorded before each
+  // class launch; inside a captured pass they are event-record nodes) and
+  // the per-launch statistics of the last pass
+  std::vector<cudaEvent_t> lev;
+  std::vector<lgx_launch_stats> last_launches;
   bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
   BasisDev basis, small;
   DBuf gscratch, counter, errflag, primcount;
@@ -1139,9 +1145,22 @@ lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool al
 // primitive counters live in ctx->primcount ([0, nslots) primitive quartets,
 // [nslots, 2 nslots) work counters) and are zeroed by the first node.
 lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
-                        EriArgs base, PassRecs& pr, std::vector<cudaEvent_t>* pev) {
+                        EriArgs base, PassRecs& pr) {
   BinCache& C = ctx->bins;
   pr = PassRecs{};
+  size_t nlaunch = 0;
+  for (const auto& bin : C.bins) nlaunch += (bin->total[0] > 0) + (bin->total[1] > 0);
+  // per-launch events persist in the context (a captured pass refers to
+  // them); the no-allocation path only uses events that already exist
+  pr.timed = ctx->lev.size() >= nlaunch;
+  if (!pr.timed && !ctx->noalloc) {
+    while (ctx->lev.size() < nlaunch) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      ctx->lev.push_back(e);
+    }
+    pr.timed = true;
+  }
   pr.nslots = 2 * C.bins.size() + 1;
   pr.count = !ctx->noalloc || ctx->primcount.n >= 2 * pr.nslots * sizeof(unsigned long long);
   unsigned long long* counters = nullptr;
@@ -1172,12 +1191,7 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
       const Variant v = tv != ctx->tuned.end()
                             ? tv->second
                             : default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
-      if (pev) {
-        cudaEvent_t e0;
-        CK(cudaEventCreate(&e0));
-        CK(cudaEventRecord(e0, ctx->stream));
-        pev->push_back(e0);
-      }
+      if (pr.timed) CK(cudaEventRecordWithFlags(ctx->lev[pr.recs.size()], ctx->stream, evflags));
       s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg, &v);
       if (s != LGX_OK) return s;
       pr.integrals += bin.integrals[sp];
@@ -1189,72 +1203,80 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
   return LGX_OK;
 }
 
-// After the pass: per-class profile lines (LGX_CLASS_PROFILE=1, the
-// counterpart of libint's per-class Engine timers, engine.h:862-890) and
-// the statistics of the pass.
+// After the pass: per-launch statistics (device time between the launch
+// events, quartets, primitive quartets, algorithmic FP operations), kept in
+// ctx->last_launches and printed per class with LGX_CLASS_PROFILE=1 (the
+// counterpart of libint's per-class Engine timers, engine.h:862-890), and
+// the statistics of the whole pass.
+bool class_profile();
 lgx_status finish_bins(lgx_context* ctx, BasisDev& B, int deriv, bool allow_fp32,
-                       const PassRecs& pr, std::vector<cudaEvent_t>* pev, lgx_jk_stats* stats) {
+                       const PassRecs& pr, lgx_jk_stats* stats) {
   BinCache& C = ctx->bins;
   const auto& recs = pr.recs;
   const size_t nslots = pr.nslots;
-  if (pev) {
-    CK(cudaEventSynchronize(ctx->ev1));
-    std::vector<unsigned long long> pcp(nslots, 0);
-    if (pr.count)
-      CK(cudaMemcpy(pcp.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
-                    cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < recs.size(); ++i) {
+  CK(cudaEventSynchronize(ctx->ev1));
+  std::vector<unsigned long long> pc(nslots, 0);
+  if (pr.count)
+    CK(cudaMemcpy(pc.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
+                  cudaMemcpyDeviceToHost));
+  ctx->last_launches.clear();
+  long long prims = 0;
+  double f64 = 0, f32 = 0;
+  for (size_t i = 0; i < recs.size(); ++i) {
+    const PassRec& r = recs[i];
+    const BinHost& bin = *C.bins[r.bin];
+    ProgDev* P = nullptr;
+    lgx_status s = get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
+    if (s != LGX_OK) return s;
+    const unsigned long long np = pc[2 * r.bin + r.sp];
+    prims += (long long)np;
+    const int pure[4] = {bin.la > 1, bin.lb > 1, bin.lc > 1, bin.ld > 1};
+    const double q = double(bin.total[r.sp]);
+    const int nsets = deriv ? 12 : 1;
+    double nsph = 1;
+    const int lq[4] = {bin.la, bin.lb, bin.lc, bin.ld};
+    for (int k = 0; k < 4; ++k) nsph *= pure[k] ? 2 * lq[k] + 1 : ncart(lq[k]);
+    // VRR + post stage + transform, then the prologue and the digestion,
+    // which run in the launch's precision too
+    const double flops = double(np) * (double(P->host.vrr_flops) + prologue_flops(P->host.mmax)) +
+                         q * (double(P->host.post_flops) +
+                              nsets * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure) +
+                              nsets * 12.0 * nsph);
+    if (r.fp32) f32 += flops; else f64 += flops;
+    lgx_launch_stats ls{};
+    ls.la = bin.la; ls.lb = bin.lb; ls.lc = bin.lc; ls.ld = bin.ld;
+    ls.fp32 = r.fp32 ? 1 : 0;
+    ls.kernel = r.v.kind;
+    ls.shape = r.v.kind == 0 ? r.v.group : r.v.rows;
+    ls.deriv = deriv;
+    ls.quartets = bin.total[r.sp];
+    ls.prim_quartets = (long long)np;
+    ls.integrals = (long long)(q * nsph);
+    ls.flops = flops;
+    ls.ms = -1.0;
+    if (pr.timed) {
       float ms = 0;
-      CK(cudaEventElapsedTime(&ms, (*pev)[i], i + 1 < pev->size() ? (*pev)[i + 1] : ctx->ev1));
-      const BinHost& bin = *C.bins[recs[i].bin];
-      ProgDev* P = nullptr;
-      get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
-      const Variant& v = recs[i].v;
+      CK(cudaEventElapsedTime(&ms, ctx->lev[i], i + 1 < recs.size() ? ctx->lev[i + 1] : ctx->ev1));
+      ls.ms = ms;
+    }
+    ctx->last_launches.push_back(ls);
+    if (class_profile()) {
       char kind[32];
-      if (v.kind == 0) snprintf(kind, sizeof(kind), "rk/G%d", v.group);
-      else snprintf(kind, sizeof(kind), "%s/R%d", v.kind == 2 ? "gen" : "prog", v.rows);
-      const int pure[4] = {bin.la > 1, bin.lb > 1, bin.lc > 1, bin.ld > 1};
-      const double np = double(pcp[2 * recs[i].bin + recs[i].sp]);
-      const double gflop = 1e-9 * (np * double(P->host.vrr_flops) +
-                                   double(bin.total[recs[i].sp]) *
-                                       (double(P->host.post_flops) +
-                                        (deriv ? 12 : 1) * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure)));
+      if (r.v.kind == 0) snprintf(kind, sizeof(kind), "rk/G%d", r.v.group);
+      else snprintf(kind, sizeof(kind), "%s/R%d", r.v.kind == 2 ? "gen" : "prog", r.v.rows);
       fprintf(stderr, "lgx-class (%d%d|%d%d) %s %s quartets %lld prims %.0f nq_avg %.1f  %.3f ms"
               "  %.1f GFLOP %.3f TFLOP/s\n",
-              bin.la, bin.lb, bin.lc, bin.ld, recs[i].fp32 ? "fp32" : "fp64", kind,
-              (long long)bin.total[recs[i].sp], np, bin.nq_avg, ms, gflop, gflop / ms);
-      cudaEventDestroy((*pev)[i]);
+              bin.la, bin.lb, bin.lc, bin.ld, r.fp32 ? "fp32" : "fp64", kind,
+              (long long)bin.total[r.sp], double(np), bin.nq_avg, ls.ms, 1e-9 * flops,
+              ls.ms > 0 ? 1e-9 * flops / ls.ms : 0.0);
     }
   }
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
-    CK(cudaEventSynchronize(ctx->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    std::vector<unsigned long long> pc(nslots, 0);
-    if (pr.count)
-      CK(cudaMemcpy(pc.data(), ctx->primcount.p, nslots * sizeof(unsigned long long),
-                    cudaMemcpyDeviceToHost));
-    long long prims = 0;
-    for (const auto& r : recs) {
-      const BinHost& bin = *C.bins[r.bin];
-      ProgDev* P = nullptr;
-      get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
-      const unsigned long long np = pc[2 * r.bin + r.sp];
-      prims += (long long)np;
-      int pure[4] = {bin.la > 1, bin.lb > 1, bin.lc > 1, bin.ld > 1};
-      const double q = double(bin.total[r.sp]);
-      const int nsets = deriv ? 12 : 1;
-      const double tflops = double(np) * double(P->host.vrr_flops) +
-                            q * (double(P->host.post_flops) +
-                                 nsets * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure));
-      double nsph = 1;
-      const int lq[4] = {bin.la, bin.lb, bin.lc, bin.ld};
-      for (int k = 0; k < 4; ++k) nsph *= pure[k] ? 2 * lq[k] + 1 : ncart(lq[k]);
-      // prologue and digestion run in the launch's precision too
-      const double dflops = double(np) * prologue_flops(P->host.mmax) + q * nsets * 12.0 * nsph;
-      if (r.fp32) stats->flops_fp32 += tflops + dflops; else stats->flops_fp64 += tflops + dflops;
-    }
+    stats->flops_fp64 = f64;
+    stats->flops_fp32 = f32;
     stats->quartets_fp64 = C.quartets[0] + (allow_fp32 ? 0 : C.quartets[1]);
     stats->quartets_fp32 = allow_fp32 ? C.quartets[1] : 0;
     stats->integrals = pr.integrals;
@@ -1273,11 +1295,9 @@ bool class_profile() {
 lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
                     EriArgs base, lgx_jk_stats* stats) {
   PassRecs pr;
-  std::vector<cudaEvent_t> pev;
-  std::vector<cudaEvent_t>* pp = class_profile() ? &pev : nullptr;
-  lgx_status s = enqueue_bins(ctx, B, mode, deriv, allow_fp32, base, pr, pp);
+  lgx_status s = enqueue_bins(ctx, B, mode, deriv, allow_fp32, base, pr);
   if (s != LGX_OK) return s;
-  return finish_bins(ctx, B, deriv, allow_fp32, pr, pp, stats);
+  return finish_bins(ctx, B, deriv, allow_fp32, pr, stats);
 }
 
 }  // namespace
@@ -1328,6 +1348,9 @@ lgx_status lgx_create(lgx_context** out, int device) {
             tay[(size_t(k) * (kBoysMaxM + 1) + m) * kBoysTaylorStride + i] =
                 boys[size_t(k) * kBoysCols + m + i] / f;
           }
+          if (m == 0)
+            tay[size_t(k) * (kBoysMaxM + 1) * kBoysTaylorStride + 7] =
+                double(expl(-(long double)k * kBoysDT));
         }
       CK(c->boys_tay.ensure(tay.size() * sizeof(double)));
       CK(cudaMemcpy(c->boys_tay.p, tay.data(), tay.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -1394,6 +1417,7 @@ lgx_status lgx_destroy(lgx_context* ctx) {
   if (ctx->ev2) cudaEventDestroy(ctx->ev2);
   if (ctx->ev3) cudaEventDestroy(ctx->ev3);
   if (ctx->jk_exec) cudaGraphExecDestroy(ctx->jk_exec);
+  for (cudaEvent_t e : ctx->lev) cudaEventDestroy(e);
   cudaStream_t st = ctx->stream;
   delete ctx;
   if (st) cudaStreamDestroy(st);
@@ -1576,11 +1600,11 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   s = tune_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a);
   if (s != LGX_OK) return s;
   // the pass: zero the accumulators, FP32 copy of D, every class bin, J/K
-  auto enqueue = [&](PassRecs& pr, std::vector<cudaEvent_t>* pev) -> lgx_status {
+  auto enqueue = [&](PassRecs& pr) -> lgx_status {
     CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
     CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
     if (mode == LGX_MIXED) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
-    lgx_status r = enqueue_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, pr, pev);
+    lgx_status r = enqueue_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, pr);
     if (r != LGX_OK) return r;
     CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
                           ctx->stream));
@@ -1597,20 +1621,18 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   key.mixed = mode == LGX_MIXED ? mixed : 0.0;
   key.mode = mode;
   key.version = ctx->version;
-  std::vector<cudaEvent_t> pev;
-  std::vector<cudaEvent_t>* pp = class_profile() ? &pev : nullptr;
-  const bool graphable = ctx->use_graphs && !pp;
+  const bool graphable = ctx->use_graphs;
   const bool replay = graphable && ctx->jk_exec && ctx->jk_key == key;
   CK(cudaEventRecord(ctx->ev2, ctx->stream));
   if (replay) {
     CK(cudaGraphLaunch(ctx->jk_exec, ctx->stream));
   } else {
-    s = enqueue(ctx->jk_recs, pp);
+    s = enqueue(ctx->jk_recs);
     if (s != LGX_OK) return s;
   }
   CK(cudaEventRecord(ctx->ev3, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  s = finish_bins(ctx, B, 0, mode == LGX_MIXED, ctx->jk_recs, pp, stats);
+  s = finish_bins(ctx, B, 0, mode == LGX_MIXED, ctx->jk_recs, stats);
   if (s != LGX_OK) return s;
   float pass_ms = 0;
   CK(cudaEventElapsedTime(&pass_ms, ctx->ev2, ctx->ev3));
@@ -1623,7 +1645,7 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
     }
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
     PassRecs tmp;
-    const lgx_status cs = enqueue(tmp, nullptr);
+    const lgx_status cs = enqueue(tmp);
     cudaGraph_t graph = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
     if (cs != LGX_OK) {
@@ -1762,6 +1784,15 @@ lgx_status lgx_jk(lgx_context* ctx, const double* D, double* J, double* K, doubl
   CK(cudaMemcpyAsync(J, ctx->Jd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(K, ctx->Kd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_last_pass_launches(lgx_context* ctx, lgx_launch_stats* out, int max, int* n) {
+  if (!ctx || !n || max < 0 || (max > 0 && !out)) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const int cnt = int(ctx->last_launches.size());
+  *n = cnt;
+  for (int i = 0; i < cnt && i < max; ++i) out[i] = ctx->last_launches[i];
   return LGX_OK;
 }
 

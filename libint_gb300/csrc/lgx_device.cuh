@@ -12,20 +12,22 @@ namespace lgx {
 // stable downward recursion F_m = (2T F_{m+1} + e^{-T})/(2m+1).
 // For T > kBoysTmax: F_0 = sqrt(pi/T)/2 (erf(sqrt T) == 1 to double there)
 // and the upward recursion F_{m+1} = ((2m+1) F_m - e^{-T})/(2T), stable for
-// 2T > 2m+1.  This is the scheme of libint's FmEval_Taylor
+// 2T > 2m+1 (the register kernels, m <= 6, drop the e^{-T} terms, which
+// are below 2e-15 relative there).  This is the scheme of libint's FmEval_Taylor
 // (include/libint2/boys.h:519-879); the table is generated on the host from
 // the Maclaurin series in extended precision.
 constexpr double kBoysInvDT = 32.0;
 constexpr double kBoysDT = 1.0 / 32.0;
-constexpr double kBoysTmax = 33.0;
+constexpr double kBoysTmax = 50.0;
 constexpr int kBoysTerms = 7;
 constexpr int kBoysMaxM = 16;                         // largest mmax served
 constexpr int kBoysCols = kBoysMaxM + kBoysTerms;     // 23 columns
-constexpr int kBoysRows = int(kBoysTmax * 32.0) + 2;  // 1058 grid points
+constexpr int kBoysRows = int(kBoysTmax * 32.0) + 2;  // 1602 grid points
 
 // Pre-divided Taylor table: [kBoysRows][kBoysMaxM+1][8] with
 // entry i = F_{m+i}(T_k) / i! (i < 7), so that
-// F_m(T_k + d) = sum_i entry_i (-d)^i by Horner without extra products.
+// F_m(T_k + d) = sum_i entry_i (-d)^i by Horner without extra products;
+// entry 7 of the m = 0 row holds e^{-T_k}.
 constexpr int kBoysTaylorStride = 8;
 
 // ------------------------------------------------------------ basis data

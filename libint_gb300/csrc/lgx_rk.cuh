@@ -20,21 +20,28 @@ namespace lgx {
 __device__ __forceinline__ double rk_f64(double x) { return x; }
 __device__ __forceinline__ double rk_f64(float x) { return f2d_int(x); }
 
-// Boys F_0..F_MMAX(T) (times nothing).  FP64: 7-term Taylor about the grid
-// point (every m directly when MMAX <= 2, else the top m plus the downward
-// recursion); FP32: 4-term Taylor on the same grid.  T > kBoysTmax:
-// asymptotic F_0 and upward recursion.
+// Boys F_0..F_MMAX(T) times the primitive prefactor pfac.
+//  T <= kBoysTmax: 7-term Taylor expansion about the nearest grid point
+//   T_k = k/32 of the pre-divided table; every m directly when MMAX <= 2,
+//   else the top m plus the downward recursion, with e^{-T} formed as the
+//   tabulated e^{-T_k} (slot 7 of the m = 0 row) times the 7-term Maclaurin
+//   series of e^{T_k - T} (|T_k - T| <= 1/64: relative error < 5e-17).
+//  T > kBoysTmax (= 50): F_0 = sqrt(pi/T)/2 and the upward recursion
+//   F_{m+1} = (2m+1)/(2T) F_m with the e^{-T} terms dropped; the relative
+//   error of that, the regularised upper incomplete gamma Q(m+1/2, T), is
+//   below 2e-16 for m <= 5 and 1.7e-15 for m = 6 at T = 50.
 template <int MMAX>
-__device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T, double* F) {
+__device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T, double pfac,
+                                        double* F) {
+  static_assert(MMAX <= 6, "asymptotic branch without e^{-T} is exact to 2e-15 only for m <= 6");
   if (T > kBoysTmax) {
-    const double rT = 1.0 / T;
-    const double oo2T = 0.5 * rT;
-    const double eT = exp(-T);
-    double f = 0.88622692545275801365 * sqrt(rT);
+    const double rs = rsqrt(T);
+    const double oo2T = 0.5 * (rs * rs);
+    double f = (0.88622692545275801365 * pfac) * rs;
     F[0] = f;
 #pragma unroll
     for (int m = 0; m < MMAX; ++m) {
-      f = ((2 * m + 1) * f - eT) * oo2T;
+      f *= (2 * m + 1) * oo2T;
       F[m + 1] = f;
     }
     return;
@@ -52,33 +59,43 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T
       double s = __ldg(c + 6);
 #pragma unroll
       for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
-      F[m] = s;
+      F[m] = s * pfac;
     }
   } else {
     const double* c = row + MMAX * kBoysTaylorStride;
     double s = __ldg(c + 6);
 #pragma unroll
     for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
+    s *= pfac;
     F[MMAX] = s;
-    const double eT = exp(-T);
+    double e = 1.0 / 720.0;
+    e = fma(e, md, 1.0 / 120.0);
+    e = fma(e, md, 1.0 / 24.0);
+    e = fma(e, md, 1.0 / 6.0);
+    e = fma(e, md, 0.5);
+    e = fma(e, md, 1.0);
+    e = fma(e, md, 1.0);
+    const double eTp = (__ldg(row + 7) * pfac) * e;  // pfac e^{-T}
     const double twoT = 2.0 * T;
 #pragma unroll
     for (int m = MMAX - 1; m >= 0; --m) {
-      s = fma(twoT, s, eT) * (1.0 / (2 * m + 1));
+      s = fma(twoT, s, eTp) * (1.0 / (2 * m + 1));
       F[m] = s;
     }
   }
 }
 
 template <int MMAX>
-__device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, float* F) {
+__device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, float pfac,
+                                        float* F) {
   if (T > float(kBoysTmax)) {
-    const float rT = 1.0f / T;
-    float f = 0.886226925f * rsqrtf(T);
+    const float rs = rsqrtf(T);
+    const float oo2T = 0.5f * (rs * rs);
+    float f = (0.886226925f * pfac) * rs;
     F[0] = f;
 #pragma unroll
     for (int m = 0; m < MMAX; ++m) {
-      f = (2 * m + 1) * f * (0.5f * rT);  // e^{-T} < 5e-15 is below FP32 resolution
+      f *= (2 * m + 1) * oo2T;  // e^{-T} < 2e-22 is below FP32 resolution
       F[m + 1] = f;
     }
     return;
@@ -91,13 +108,14 @@ __device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, 
   s = fmaf(s, c3, __ldg(row + MMAX + 2));
   s = fmaf(s, c2, __ldg(row + MMAX + 1));
   s = fmaf(s, c1, __ldg(row + MMAX));
+  s *= pfac;
   F[MMAX] = s;
   if (MMAX > 0) {
-    const float eT = __expf(-T);
+    const float eTp = __expf(-T) * pfac;
     const float twoT = 2.0f * T;
 #pragma unroll
     for (int m = MMAX - 1; m >= 0; --m) {
-      s = fmaf(twoT, s, eT) * (1.0f / (2 * m + 1));
+      s = fmaf(twoT, s, eTp) * (1.0f / (2 * m + 1));
       F[m] = s;
     }
   }
@@ -175,9 +193,7 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double
   const double rho = zeta * eta * oogpq;
   const double T = rho * fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
   double F[C::kMmax + 1];
-  rk_boys<C::kMmax>(a.boys_tay, T, F);
-#pragma unroll
-  for (int m = 0; m <= C::kMmax; ++m) F[m] *= pfac;
+  rk_boys<C::kMmax>(a.boys_tay, T, pfac, F);
   rk::Geo<double> g;
   const double ez = eta * oogpq, zz = zeta * oogpq;
   g.PAx = bp.P[0] - q.A[0]; g.PAy = bp.P[1] - q.A[1]; g.PAz = bp.P[2] - q.A[2];
@@ -235,9 +251,7 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
   const float rho = zeta * eta * oogpq;
   const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
   float F[C::kMmax + 1];
-  rk_boys<C::kMmax>(a.boys32, T, F);
-#pragma unroll
-  for (int m = 0; m <= C::kMmax; ++m) F[m] *= pfac;
+  rk_boys<C::kMmax>(a.boys32, T, pfac, F);
   rk::Geo<float> g;
   const float ez = eta * oogpq, zz = zeta * oogpq;
   g.PAx = PA[0]; g.PAy = PA[1]; g.PAz = PA[2];

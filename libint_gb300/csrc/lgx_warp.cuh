@@ -52,10 +52,10 @@ __device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
                                               int mmax, double pfac, double* __restrict__ F) {
   if (T > kBoysTmax) {
     const double eT = exp(-T);
-    const double rT = 1.0 / T;
-    double f = 0.88622692545275801365 * sqrt(rT);
+    const double rs = rsqrt(T);
+    double f = 0.88622692545275801365 * rs;
     F[0] = f * pfac;
-    const double oo2T = 0.5 * rT;
+    const double oo2T = 0.5 * (rs * rs);
     for (int m = 0; m < mmax; ++m) {
       f = ((2 * m + 1) * f - eT) * oo2T;
       F[m + 1] = f * pfac;
@@ -87,11 +87,12 @@ __device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
 __device__ __forceinline__ void boys_to_stage(const float* __restrict__ tab, float T, int mmax,
                                               float pfac, float* __restrict__ F) {
   if (T > float(kBoysTmax)) {
-    const float rT = 1.0f / T;
-    float f = 0.886226925f * rsqrtf(T);
+    const float rs = rsqrtf(T);
+    const float oo2T = 0.5f * (rs * rs);
+    float f = 0.886226925f * rs;
     F[0] = f * pfac;
     for (int m = 0; m < mmax; ++m) {
-      f = (2 * m + 1) * f * (0.5f * rT);
+      f = (2 * m + 1) * f * oo2T;
       F[m + 1] = f * pfac;
     }
     return;
