@@ -302,13 +302,26 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
   // Warp chunks of per_warp consecutive quartets, strided over the grid:
   // consecutive quartets share a bin segment (same bra pair, same depth).
   for (long long c = warp_id; c * per_warp < total; c += nwarps) {
-    const long long qi = c * per_warp + (lane / G);
+    const long long c0 = c * per_warp;
+    const long long qi = c0 + (lane / G);
+    int seg = 0;
+    if (a.implicit) {
+      // One (warp-uniform) binary search per chunk; the segment starts
+      // inside the chunk come from one coalesced load of the next 32
+      // starts (segments are non-empty, so at most per_warp - 1 of them
+      // fall inside), and each quartet's segment is seg0 plus the starts
+      // at or before its offset.
+      const int seg0 = bin_segment(a.bin, c0);
+      const int k = seg0 + 1 + lane;
+      const long long m = (k <= a.bin.nseg ? a.bin.seg_start[k] : total + 64) - c0;  // >= 1
+      const unsigned starts = __reduce_or_sync(0xffffffffu, m < per_warp ? 1u << m : 0u);
+      seg = seg0 + __popc(starts & ((2u << (lane / G)) - 1u));
+    }
     if (qi >= total) continue;
     int bpair, kpair, flags, orig = 0;
     long long outoff = 0;
     int2 brec = make_int2(0, 0), krec = make_int2(0, 0);
     if (a.implicit) {
-      const int seg = bin_segment(a.bin, qi);
       const int j = int(qi - a.bin.seg_start[seg]) + a.bin.seg_j0[seg];
       const int bpos = a.bin.seg_bra[seg];
       bpair = a.bin.bra_pairs[bpos];

@@ -737,6 +737,28 @@ int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
   return compute_quartet(bs, tgt, deriv, precision, method, w, out);
 }
 
+// Batched Engine::compute over an explicit list (4 shell indices per
+// quartet, caller order), OpenMP over quartets: set q is written at
+// out + offsets[q] (nsets sets back to back); is_null[q] = 1 when every
+// primitive quartet was screened out.  Returns 0, or -1 on bad arguments.
+int orc_compute_batch(const orc_basis* bs, const int* quartets, int64_t n, int deriv,
+                      double precision, int method, const int64_t* offsets, double* out,
+                      int* is_null, int nthreads) {
+  if (deriv < 0 || deriv > 1 || n < 0) return -1;
+  const int nt = nthreads_or_default(nthreads);
+#pragma omp parallel num_threads(nt)
+  {
+    Work w;
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t q = 0; q < n; ++q) {
+      const int r = compute_quartet(bs, quartets + 4 * q, deriv, precision, method, w,
+                                    out + offsets[q]);
+      is_null[q] = r == 0 ? 1 : 0;
+    }
+  }
+  return 0;
+}
+
 void orc_schwarz(const orc_basis* bs, double* Kmat, int nthreads) {
   const int ns = bs->nshell;
   const int nt = nthreads_or_default(nthreads);

@@ -167,6 +167,27 @@ def compute_quartet(basis: OracleBasis, s1, s2, s3, s4, deriv=0,
     return [out[i * r:(i + 1) * r].reshape(n) for i in range(nsets)]
 
 
+def compute_batch(basis: OracleBasis, quartets, offsets, total, deriv=0,
+                  precision=np.finfo(float).eps, method=0, nthreads=0):
+    """Engine::compute over an explicit quartet list (n x 4 shell indices),
+    OpenMP over quartets; set q lands at out[offsets[q]:...] as in
+    lgx_compute_batch.  Returns (out, is_null)."""
+    q = np.ascontiguousarray(quartets, np.int32).reshape(-1, 4)
+    offs = np.ascontiguousarray(offsets, np.int64)
+    out = np.zeros(max(1, int(total)))
+    isnull = np.zeros(max(1, len(q)), np.int32)
+    lib = _lib()
+    lib.orc_compute_batch.argtypes = [ctypes.POINTER(_Basis), _ip, ctypes.c_int64, ctypes.c_int,
+                                      ctypes.c_double, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_int64), _dp, _ip, ctypes.c_int]
+    r = lib.orc_compute_batch(ctypes.byref(basis._c), _ptr(q, ctypes.c_int), len(q), deriv,
+                              precision, method, _ptr(offs, ctypes.c_int64),
+                              _ptr(out, ctypes.c_double), _ptr(isnull, ctypes.c_int), nthreads)
+    if r < 0:
+        raise ValueError("oracle: bad arguments")
+    return out, isnull[:len(q)]
+
+
 def schwarz(basis: OracleBasis, nthreads=0) -> np.ndarray:
     K = np.zeros((basis.nshell, basis.nshell))
     _lib().orc_schwarz(ctypes.byref(basis._c), _ptr(K, ctypes.c_double), nthreads)
