@@ -214,8 +214,15 @@ lgx_status lgx_jk_grad(lgx_context* ctx, const double* D, double* gJ,
 
 /* -------------------------------------------------------- host utilities */
 
+/* Shell::do_enforce_unit_normalization (shell.h:891-901): flag 0 or 1 sets
+ * whether lgx_shell_normalize and lgx_basis_load rescale each contraction to
+ * unit self-overlap (process-wide, on by default, like the reference's
+ * static switch); flag < 0 only queries.  Returns the setting in effect. */
+int lgx_enforce_unit_normalization(int flag);
+
 /* Shell::renorm (shell.h:958-999): coeff_out = normalization-embedded
- * coefficients for unit-normalized-primitive input coefficients. */
+ * coefficients for unit-normalized-primitive input coefficients (the
+ * contraction renormalized to unity unless disabled above). */
 lgx_status lgx_shell_normalize(int l, int nprim, const double* alpha,
                                const double* coeff_in, double* coeff_out);
 

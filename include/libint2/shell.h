@@ -82,6 +82,14 @@ struct Shell {
     return s[l];
   }
 
+  /// Shell::do_enforce_unit_normalization (shell.h:891-901): with no
+  /// argument reports, otherwise sets whether renorm() rescales each
+  /// contraction to unit self-overlap (process-wide, default true).
+  static bool do_enforce_unit_normalization() { return lgx_enforce_unit_normalization(-1) != 0; }
+  static bool do_enforce_unit_normalization(bool flag) {
+    return lgx_enforce_unit_normalization(flag ? 1 : 0) != 0;
+  }
+
   /// "unit" shell: exponent 0, coefficient 1, at the origin
   static const Shell& unit() {
     static const Shell u = [] {

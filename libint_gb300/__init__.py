@@ -72,6 +72,13 @@ class Shell:
         self.O = np.asarray(center, dtype=float).reshape(3).copy()
         self.pure = bool(pure)
 
+    @staticmethod
+    def do_enforce_unit_normalization(flag=None) -> bool:
+        """Shell::do_enforce_unit_normalization (shell.h:891-901): reports,
+        or sets when flag is given, whether new shells (and basis sets) have
+        their contractions rescaled to unit self-overlap; process-wide."""
+        return bool(_lgx.load().lgx_enforce_unit_normalization(-1 if flag is None else int(bool(flag))))
+
     @classmethod
     def from_normalized(cls, L, alpha, coeff, center, pure):
         s = cls.__new__(cls)

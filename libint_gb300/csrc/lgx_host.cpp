@@ -1,5 +1,6 @@
 // Host utilities of liblgx: shell normalization, the G94 basis-set reader
 // and the synthetic water-cluster builder.  Plain C++ (no CUDA).
+#include <atomic>
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -21,7 +22,13 @@ double dfac(int n) {  // n!!, (-1)!! = 1
   return r;
 }
 
-// Shell::renorm (include/libint2/shell.h:958-999).
+// Shell::do_enforce_unit_normalization (include/libint2/shell.h:891-901):
+// process-wide, on by default.
+std::atomic<bool> g_unit_normalization{true};
+
+// Shell::renorm (include/libint2/shell.h:958-999): primitive normalization
+// embedded into the coefficients, then (when enforced) the contraction
+// rescaled to unit self-overlap.
 void normalize(int l, int nprim, const double* alpha, const double* cin, double* cout) {
   const double sqrt_pi3 = 5.56832799683170784528481798212;  // pi^{3/2}
   std::vector<double> c(cin, cin + nprim);
@@ -30,6 +37,10 @@ void normalize(int l, int nprim, const double* alpha, const double* cin, double*
     const double two_a = 2 * alpha[p];
     const double t = std::pow(two_a, l + 1) * std::sqrt(two_a);
     c[p] *= std::sqrt(std::pow(2.0, l) * t / (sqrt_pi3 * dfac(2 * l - 1)));
+  }
+  if (!g_unit_normalization.load()) {
+    for (int p = 0; p < nprim; ++p) cout[p] = c[p];
+    return;
   }
   double norm = 0;
   for (int p = 0; p < nprim; ++p)
@@ -178,6 +189,11 @@ thread_local std::string g_host_error;
 }  // namespace
 
 extern "C" {
+
+int lgx_enforce_unit_normalization(int flag) {
+  if (flag >= 0) g_unit_normalization.store(flag != 0);
+  return g_unit_normalization.load() ? 1 : 0;
+}
 
 lgx_status lgx_shell_normalize(int l, int nprim, const double* alpha,
                                const double* coeff_in, double* coeff_out) {

@@ -14,6 +14,14 @@ Outputs (numpy .npz, committed):
   basis.npz       BasisSet("cc-pVDZ"/"cc-pVTZ") for one water
   derivmap.npz    first-derivative shell-set order and bra/ket-swap map
   eri.npz         brute-force contracted shell sets, d0 and d1, many classes
+  hf.npz          system-level golden values of the reference's Hartree-Fock
+                  tests, read as text: the rotated-water geometry
+                  (tests/hartree-fock/h2o_rotated.xyz) with the aug-cc-pVDZ
+                  energy and 2-body forces its validator checks
+                  (hartree-fock++-validate.py), and the water geometry and
+                  6-31G energy of python/tests/test_hf.py
+
+    python tests/golden/make_golden.py --hf-only    # hf.npz alone
 """
 import ctypes
 import itertools
@@ -147,5 +155,57 @@ def main():
     print("cases", len(cases), "values", off)
 
 
-if __name__ == "__main__":
+REFERENCE = "/root/reference"
+SYMBOL_Z = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10}
+
+
+def _floats_after(text, name):
+    """The list literal assigned to `name` in a Python source text."""
+    import re
+    m = re.search(r"^%s\s*=\s*\[([^\]]*)\]" % re.escape(name), text, re.M)
+    return [float(x) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+
+
+def _scalar_after(text, name):
+    import re
+    m = re.search(r"^%s\s*=\s*([-+0-9.eE]+)" % re.escape(name), text, re.M)
+    return float(m.group(1))
+
+
+def hf_fixtures(root=REFERENCE):
+    import re
+    hf = os.path.join(root, "tests", "hartree-fock")
+    with open(os.path.join(hf, "h2o_rotated.xyz")) as f:
+        lines = f.read().splitlines()
+    nat = int(lines[0].split()[0])
+    Z, xyz = [], []
+    for ln in lines[2:2 + nat]:
+        t = ln.split()
+        Z.append(SYMBOL_Z[t[0]])
+        xyz.append([float(v) for v in t[1:4]])
+    with open(os.path.join(hf, "hartree-fock++-validate.py")) as f:
+        val = f.read()
+    eref = _floats_after(val, "eref")[0]
+    etol = _scalar_after(val, "etol")
+    F2 = _floats_after(val, "F2ref")
+    F2tol = _scalar_after(val, "F2tol")
+    with open(os.path.join(root, "python", "tests", "test_hf.py")) as f:
+        py = f.read()
+    m = re.search(r"h2o\s*=\s*\[(.*?)\n\]", py, re.S)
+    atoms631 = re.findall(r"\(\s*(\d+)\s*,\s*\[([^\]]*)\]\s*\)", m.group(1))
+    Z631 = [int(a) for a, _ in atoms631]
+    xyz631 = [[float(v) for v in b.split(",")] for _, b in atoms631]
+    e631 = float(re.search(r"assertAlmostEqual\(rhf\.energy\(\),\s*([-0-9.]+)\)", py).group(1))
+    np.savez(os.path.join(HERE, "hf.npz"),
+             rot_Z=np.array(Z, np.int32), rot_xyz_angstrom=np.array(xyz),
+             rot_basis="aug-cc-pVDZ", rot_energy=eref, rot_energy_tol=etol,
+             rot_F2=np.array(F2).reshape(nat, 3), rot_F2_tol=F2tol,
+             h2o631_Z=np.array(Z631, np.int32), h2o631_xyz_bohr=np.array(xyz631),
+             h2o631_basis="6-31G", h2o631_energy=e631, h2o631_places=7)
+
+
+if __name__ == "__main__" and "--hf-only" in sys.argv:
+    hf_fixtures()
+elif __name__ == "__main__":
+    hf_fixtures()
     main()
