@@ -54,7 +54,8 @@ enum class Operator {
   last_2body_oper = stg_x_coulomb
 };
 
-/// BraKet enum (engine.h:188-206); only xx_xx is served.
+/// BraKet enum (engine.h:188-206); xx_xx, and the 3- and 2-centre xs_xx /
+/// xs_xs through Shell::unit() as the reference does (engine.impl.h:140-175).
 enum class BraKet { x_x = 0, xx_xx, xs_xx, xx_xs, xs_xs, invalid = -1 };
 
 enum class CartesianShellNormalization { standard, uniform };
@@ -134,9 +135,11 @@ class Engine {
         lmax_(max_l),
         deriv_order_(deriv_order),
         screening_(screening) {
-    if (oper_ != Operator::coulomb || braket_ != BraKet::xx_xx)
+    if (oper_ != Operator::coulomb ||
+        (braket_ != BraKet::xx_xx && braket_ != BraKet::xs_xx && braket_ != BraKet::xs_xs))
       throw std::invalid_argument(
-          "libint2::Engine (GB300): only Operator::coulomb with BraKet::xx_xx is implemented");
+          "libint2::Engine (GB300): only Operator::coulomb with BraKet::xx_xx, xs_xx or xs_xs "
+          "is implemented");
     if (max_l < 0 || max_l > LGX_MAX_L) throw lmax_exceeded("eri", LGX_MAX_L, max_l);
     if (deriv_order < 0 || deriv_order > LGX_MAX_DERIV)
       throw std::invalid_argument("libint2::Engine (GB300): deriv_order must be 0 or 1");
@@ -149,8 +152,12 @@ class Engine {
   Operator oper() const { return oper_; }
   BraKet braket() const { return braket_; }
   int deriv_order() const { return deriv_order_; }
+  /// rank of the braket: 4 (xx_xx), 3 (xs_xx), 2 (xs_xs) (engine.h:408-417)
+  int braket_rank() const {
+    return braket_ == BraKet::xs_xs ? 2 : (braket_ == BraKet::xs_xx ? 3 : 4);
+  }
   unsigned int nshellsets() const {
-    return unsigned(num_geometrical_derivatives(4, size_t(deriv_order_)));
+    return unsigned(num_geometrical_derivatives(size_t(braket_rank()), size_t(deriv_order_)));
   }
   const target_ptr_vec& results() const { return targets_; }
 
@@ -185,10 +192,21 @@ class Engine {
     return *this;
   }
 
-  /// Engine::compute (engine.impl.h:140-175)
+  /// Engine::compute (engine.impl.h:140-175): 4 shells for xx_xx, 3 for
+  /// xs_xx (bra1 | ket1 ket2), 2 for xs_xs (bra1 | ket1); the missing
+  /// positions take Shell::unit() as in the reference.
   const target_ptr_vec& compute(const Shell& s1, const Shell& s2, const Shell& s3,
                                 const Shell& s4) {
+    if (braket_rank() != 4) throw std::invalid_argument("Engine::compute: braket needs 4 shells");
     return compute_impl(s1, s2, s3, s4);
+  }
+  const target_ptr_vec& compute(const Shell& s1, const Shell& s2, const Shell& s3) {
+    if (braket_rank() != 3) throw std::invalid_argument("Engine::compute: braket needs 3 shells");
+    return compute_impl(s1, Shell::unit(), s2, s3);
+  }
+  const target_ptr_vec& compute(const Shell& s1, const Shell& s2) {
+    if (braket_rank() != 2) throw std::invalid_argument("Engine::compute: braket needs 2 shells");
+    return compute_impl(s1, Shell::unit(), s2, Shell::unit());
   }
   /// Engine::compute2<op, braket, deriv> (engine.h:787-791); the optional
   /// ShellPair data is not needed by the GPU path.
@@ -196,10 +214,11 @@ class Engine {
   const target_ptr_vec& compute2(const Shell& s1, const Shell& s2, const Shell& s3,
                                  const Shell& s4, const ShellPair* = nullptr,
                                  const ShellPair* = nullptr) {
-    static_assert(op == Operator::coulomb && bk == BraKet::xx_xx,
-                  "only coulomb / xx_xx is implemented on the GPU path");
-    if (int(deriv) != deriv_order_)
-      throw std::invalid_argument("Engine::compute2: deriv_order mismatch");
+    static_assert(op == Operator::coulomb &&
+                      (bk == BraKet::xx_xx || bk == BraKet::xs_xx || bk == BraKet::xs_xs),
+                  "only coulomb / xx_xx, xs_xx, xs_xs is implemented on the GPU path");
+    if (int(deriv) != deriv_order_ || bk != braket_)
+      throw std::invalid_argument("Engine::compute2: deriv_order or braket mismatch");
     return compute_impl(s1, s2, s3, s4);
   }
 
@@ -236,7 +255,7 @@ class Engine {
       nv *= sh[k]->size();
     }
     const unsigned ns = nshellsets();
-    buf_.resize(nv * ns);
+    buf_.resize(nv * (deriv_order_ ? 12 : 1));
     int nsets = 0, nvalues = 0, is_null = 0;
     const int method =
         screening_ == ScreeningMethod::Conservative ? LGX_SCREEN_CONSERVATIVE : LGX_SCREEN_ORIGINAL;
@@ -249,7 +268,17 @@ class Engine {
       throw std::runtime_error(std::string("libint2::Engine::compute: ") + lgx_last_error(rt.ctx));
     targets_.assign(ns, nullptr);
     if (is_null) return targets_;
-    for (unsigned s = 0; s < ns; ++s) targets_[s] = buf_.data() + size_t(s) * nv;
+    // derivative sets of the real centres only: the unit shells' sets (zero)
+    // are left out, which leaves the reference's order (centres A, C, D for
+    // xs_xx; A, C for xs_xs; each x, y, z)
+    static const int kSet3[9] = {0, 1, 2, 6, 7, 8, 9, 10, 11};
+    static const int kSet2[6] = {0, 1, 2, 6, 7, 8};
+    for (unsigned s = 0; s < ns; ++s) {
+      const int src = (deriv_order_ == 0 || braket_rank() == 4)
+                          ? int(s)
+                          : (braket_rank() == 3 ? kSet3[s] : kSet2[s]);
+      targets_[s] = buf_.data() + size_t(src) * nv;
+    }
     return targets_;
   }
 };

@@ -33,9 +33,20 @@ class Operator(enum.Enum):
 
 
 class BraKet(enum.Enum):
-    """libint2::BraKet; only xx_xx (four-centre) is implemented."""
+    """libint2::BraKet (engine.h:188-206; binding names XXXX, XSXX, XSXS):
+    four-centre xx_xx, and the three- and two-centre xs_xx / xs_xs that the
+    reference computes with Shell.unit() in the empty positions."""
     XXXX = 1
     xx_xx = 1
+    XSXX = 3
+    xs_xx = 3
+    XSXS = 4
+    xs_xs = 4
+
+
+_BRAKET_RANK = {BraKet.xx_xx: 4, BraKet.xs_xx: 3, BraKet.xs_xs: 2}
+# derivative sets of the real centres within the 12 four-centre sets
+_DERIV_SETS = {4: list(range(12)), 3: [0, 1, 2, 6, 7, 8, 9, 10, 11], 2: [0, 1, 2, 6, 7, 8]}
 
 
 class ScreeningMethod(enum.IntEnum):
@@ -78,6 +89,12 @@ class Shell:
         or sets when flag is given, whether new shells (and basis sets) have
         their contractions rescaled to unit self-overlap; process-wide."""
         return bool(_lgx.load().lgx_enforce_unit_normalization(-1 if flag is None else int(bool(flag))))
+
+    @classmethod
+    def unit(cls):
+        """Shell::unit() (shell.h:904-914): exponent 0, coefficient 1, at the
+        origin; the placeholder of the 3- and 2-centre brakets."""
+        return cls.from_normalized(0, [0.0], [1.0], (0.0, 0.0, 0.0), False)
 
     @classmethod
     def from_normalized(cls, L, alpha, coeff, center, pure):
@@ -414,14 +431,14 @@ class Engine:
                  context: Context | None = None):
         if oper != Operator.coulomb:
             raise NotImplementedError("only Operator.coulomb is implemented")
-        if braket not in (None, BraKet.xx_xx):
-            raise NotImplementedError("only BraKet.xx_xx is implemented")
+        if braket not in (None, BraKet.xx_xx, BraKet.xs_xx, BraKet.xs_xs):
+            raise NotImplementedError("only BraKet xx_xx, xs_xx and xs_xs are implemented")
         if max_l > MAX_AM:
             raise LgxError(_lgx.LGX_ERR_LMAX_EXCEEDED, "max_l exceeds LGX_MAX_L")
         if deriv_order not in (0, 1):
             raise NotImplementedError("deriv_order must be 0 or 1")
         self.oper = oper
-        self.braket = BraKet.xx_xx
+        self.braket = braket or BraKet.xx_xx
         self.max_nprim = max_nprim
         self.max_l = max_l
         self.deriv_order = deriv_order
@@ -441,23 +458,38 @@ class Engine:
         self.screening = ScreeningMethod(screening)
         return self
 
+    def braket_rank(self):
+        return _BRAKET_RANK[self.braket]
+
     def nshellsets(self):
-        return 12 if self.deriv_order else 1
+        return 3 * self.braket_rank() if self.deriv_order else 1
 
     def results(self):
         return self._results
 
     def compute(self, *shells):
+        """compute(s1, s2, s3, s4) for xx_xx, (s1, s2, s3) for xs_xx,
+        (s1, s2) for xs_xs (the binding's compute2/3/4, engine.cc:165-202);
+        arrays shaped by the given shells, None when screened out."""
+        rank = self.braket_rank()
+        if len(shells) != rank:
+            raise ValueError("compute: %s takes %d shells" % (self.braket.name, rank))
         if len(shells) == 4 and all(isinstance(s, BasisSet) or isinstance(s, list)
                                     for s in shells) and not isinstance(shells[0], Shell):
             return self._compute_basis(*shells)
-        if len(shells) != 4:
-            raise NotImplementedError("only four-centre (xx_xx) integrals are implemented")
         for s in shells:
             if s.l > self.max_l:
                 raise LgxError(_lgx.LGX_ERR_LMAX_EXCEEDED, "lmax_exceeded")
+        full = list(shells)
+        if rank == 3:
+            full = [shells[0], Shell.unit(), shells[1], shells[2]]
+        elif rank == 2:
+            full = [shells[0], Shell.unit(), shells[1], Shell.unit()]
         ctx = self._ctx or _default_context()
-        r = ctx.compute_shellset(shells, self.deriv_order, self._precision, self.screening)
+        r = ctx.compute_shellset(full, self.deriv_order, self._precision, self.screening)
+        if r is not None:
+            shape = tuple(s.size() for s in shells)
+            r = [r[i].reshape(shape) for i in (_DERIV_SETS[rank] if self.deriv_order else [0])]
         self._results = r if r is not None else [None] * self.nshellsets()
         if r is None:
             return None

@@ -28,14 +28,18 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, P
     B[x] = b.O[3 * s2 + x];
     AB2 += (A[x] - B[x]) * (A[x] - B[x]);
   }
-  const double gamma = a1 + a2, oog = 1.0 / gamma;
+  // a pair of two unit shells (exponent 0, Shell::unit()) has no Gaussian
+  // product; no braket uses it, so it is stored as a dropped pair
+  const bool degenerate = !(a1 + a2 > 0.0);
+  const double gamma = a1 + a2, oog = degenerate ? 0.0 : 1.0 / gamma;
   const double rho = a1 * a2 * oog;
   const double mrAB2 = -rho * AB2;
   double ln_scr = mrAB2 + log(fabs(c1)) + log(fabs(c2));
   PrimPairRec r;
   for (int x = 0; x < 3; ++x) r.P[x] = (AB2 == 0.0) ? A[x] : (a1 * A[x] + a2 * B[x]) * oog;
   double nonsph = 0;
-  bool drop = (method == 0 && ln_scr < ln_prec);
+  if (degenerate) ln_scr = -1.0e300;
+  bool drop = degenerate || (method == 0 && ln_scr < ln_prec);
   if (method == 1) {
     double mPA = 0, mPB = 0;
     for (int x = 0; x < 3; ++x) {
@@ -50,9 +54,9 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, P
     nonsph = fmax(t1, t2);
     ln_scr += 1.777485947591722872387900 + log(oog) + log(fmax(nonsph, 1.0)) +
               log(double(b.nprim[s1] * b.nprim[s2]));
-    drop = ln_scr < ln_prec;
+    drop = degenerate || ln_scr < ln_prec;
   }
-  r.Kc = 5.9149671727956128778 * exp(mrAB2) * oog * c1 * c2;
+  r.Kc = degenerate ? 0.0 : 5.9149671727956128778 * exp(mrAB2) * oog * c1 * c2;
   r.oog = oog;
   r.zeta = gamma;
   r.a1 = a1;

@@ -11,7 +11,7 @@ import os
 import sys
 
 NAMES = ["cc-pvdz", "cc-pvtz", "augmentation-cc-pvdz", "augmentation-cc-pvtz",
-         "6-31g", "sto-3g"]
+         "6-31g", "sto-3g", "cc-pvdz-jkfit"]
 KEEP = {"H", "He", "Li", "Be", "B", "C", "N", "O", "F", "Ne"}
 
 

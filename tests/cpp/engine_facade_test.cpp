@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <fstream>
 #include <iostream>
+#include <limits>
 #include <vector>
 
 int main(int argc, char** argv) {
@@ -64,6 +65,26 @@ int main(int argc, char** argv) {
   jk.compute(D, J, K, 0.0);
   for (double v : J) put(v);
   for (double v : K) put(v);
+  // 3- and 2-centre integrals (density fitting): BraKet::xs_xx / xs_xs
+  libint2::Engine e3(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 0,
+                     std::numeric_limits<double>::epsilon(), nullptr, libint2::BraKet::xs_xx);
+  libint2::Engine e3d(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 1,
+                      std::numeric_limits<double>::epsilon(), nullptr, libint2::BraKet::xs_xx);
+  libint2::Engine e2(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 0,
+                     std::numeric_limits<double>::epsilon(), nullptr, libint2::BraKet::xs_xs);
+  const size_t t3[][3] = {{5, 3, 8}, {3, 5, 14}, {0, 9, 2}};
+  for (const auto& t : t3) {
+    const size_t n = obs[t[0]].size() * obs[t[1]].size() * obs[t[2]].size();
+    const auto& r = e3.compute(obs[t[0]], obs[t[1]], obs[t[2]]);
+    for (size_t i = 0; i < n; ++i) put(r[0][i]);
+    const auto& rd = e3d.compute2<libint2::Operator::coulomb, libint2::BraKet::xs_xx, 1>(
+        obs[t[0]], libint2::Shell::unit(), obs[t[1]], obs[t[2]]);
+    put(double(e3d.nshellsets()));
+    for (unsigned s = 0; s < e3d.nshellsets(); ++s)
+      for (size_t i = 0; i < n; ++i) put(rd[s][i]);
+    const auto& r2 = e2.compute(obs[t[0]], obs[t[1]]);
+    for (size_t i = 0; i < obs[t[0]].size() * obs[t[1]].size(); ++i) put(r2[0][i]);
+  }
   libint2::finalize();
   std::cout << "ok" << std::endl;
   return 0;

@@ -14,6 +14,9 @@ Outputs (numpy .npz, committed):
   basis.npz       BasisSet("cc-pVDZ"/"cc-pVTZ") for one water
   derivmap.npz    first-derivative shell-set order and bra/ket-swap map
   eri.npz         brute-force contracted shell sets, d0 and d1, many classes
+  eri3c.npz       brute-force 3-centre (a 1|c d) and 2-centre (a 1|c 1) shell
+                  sets, d0 and d1 (1 = Shell::unit(), exponent 0), same layout
+                  as eri.npz plus the braket rank
   hf.npz          system-level golden values of the reference's Hartree-Fock
                   tests, read as text: the rotated-water geometry
                   (tests/hartree-fock/h2o_rotated.xyz) with the aug-cc-pVDZ
@@ -22,6 +25,7 @@ Outputs (numpy .npz, committed):
                   6-31G energy of python/tests/test_hf.py
 
     python tests/golden/make_golden.py --hf-only    # hf.npz alone
+    python tests/golden/make_golden.py --eri3c-only # eri3c.npz alone
 """
 import ctypes
 import itertools
@@ -155,6 +159,62 @@ def main():
     print("cases", len(cases), "values", off)
 
 
+def eri3c_fixtures():
+    """3- and 2-centre shell sets from the reference's brute-force eri.h with
+    unit shells (l = 0, exponent 0, coefficient 1, at the origin) in the
+    empty positions, as Engine::compute does for xs_xx / xs_xs
+    (engine.impl.h:140-175)."""
+    oracle.build_ref()
+    ref = oracle.ref_lib()
+    assert ref is not None, "reference build missing"
+    rng = np.random.default_rng(20240602)
+    unit = (0, 0, np.array([0.0]), np.array([1.0]), np.zeros(3))
+    cases = []
+    for la, lc, ld in itertools.product(range(4), repeat=3):
+        cases.append(((la, 0, lc, ld), 3, 0))
+        if la + lc + ld <= 5:
+            cases.append(((la, 0, lc, ld), 3, 1))
+    for la, lc in itertools.product(range(4), repeat=2):
+        cases.append(((la, 0, lc, 0), 2, 0))
+        cases.append(((la, 0, lc, 0), 2, 1))
+    recs = {"l": [], "pure": [], "nprim": [], "alpha": [], "coeff": [], "O": [], "deriv": [],
+            "rank": [], "offset": []}
+    off, vals = 0, []
+    for ls, rank, d in cases:
+        shells = []
+        for k, l in enumerate(ls):
+            if k == 1 or (rank == 2 and k == 3):
+                shells.append(unit)
+                continue
+            n = 1 if l == 3 else (2 if l > 0 else 3)
+            a = np.sort(rng.uniform(0.15, 5.0, n))[::-1].copy()
+            c = rng.uniform(0.2, 1.0, n)
+            cn, _ = oracle.shell_normalize(l, a, c)
+            shells.append((l, 1 if l > 1 else 0, a, cn, rng.uniform(-1.2, 1.2, 3)))
+        r = oracle.ref_eri_shellset(ref, shells, d)
+        v = np.concatenate([x.reshape(-1) for x in r])
+        recs["l"].append(ls); recs["pure"].append([s[1] for s in shells])
+        recs["nprim"].append([len(s[2]) for s in shells])
+        recs["alpha"].append(np.concatenate([s[2] for s in shells]))
+        recs["coeff"].append(np.concatenate([s[3] for s in shells]))
+        recs["O"].append(np.concatenate([s[4] for s in shells]))
+        recs["deriv"].append(d); recs["rank"].append(rank)
+        recs["offset"].append(off)
+        vals.append(v)
+        off += v.size
+    maxp = max(len(a) for a in recs["alpha"])
+    alpha = np.zeros((len(cases), maxp)); coeff = np.zeros((len(cases), maxp))
+    for i in range(len(cases)):
+        alpha[i, :len(recs["alpha"][i])] = recs["alpha"][i]
+        coeff[i, :len(recs["coeff"][i])] = recs["coeff"][i]
+    np.savez_compressed(os.path.join(HERE, "eri3c.npz"), l=np.array(recs["l"], np.int32),
+                        pure=np.array(recs["pure"], np.int32),
+                        nprim=np.array(recs["nprim"], np.int32), alpha=alpha, coeff=coeff,
+                        O=np.array(recs["O"]), deriv=np.array(recs["deriv"], np.int32),
+                        rank=np.array(recs["rank"], np.int32),
+                        offset=np.array(recs["offset"], np.int64), values=np.concatenate(vals))
+
+
 REFERENCE = "/root/reference"
 SYMBOL_Z = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10}
 
@@ -206,6 +266,9 @@ def hf_fixtures(root=REFERENCE):
 
 if __name__ == "__main__" and "--hf-only" in sys.argv:
     hf_fixtures()
+elif __name__ == "__main__" and "--eri3c-only" in sys.argv:
+    eri3c_fixtures()
 elif __name__ == "__main__":
     hf_fixtures()
+    eri3c_fixtures()
     main()

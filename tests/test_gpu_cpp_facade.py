@@ -62,3 +62,23 @@ def test_cpp_engine_facade(lgx, oracle_mod, tmp_path):
     Jr, Kr, _ = oracle_mod.jk(ob, D, Kq, 0.0)
     assert np.max(np.abs(J - Jr)) < 1e-10
     assert np.max(np.abs(K - Kr)) < 1e-10
+    pos += 2 * nbf * nbf
+    # xs_xx (d0 and 9 derivative sets through compute2) and xs_xs, against
+    # the oracle with Shell::unit() in the empty positions
+    full = lgx.BasisSet(list(bs) + [lgx.Shell.unit()])
+    obu = oracle_mod.OracleBasis.from_basis(full)
+    u = len(bs)
+    for a, c, d in [(5, 3, 8), (3, 5, 14), (0, 9, 2)]:
+        ref = oracle_mod.compute_quartet(obu, a, u, c, d)[0].reshape(-1)
+        assert np.max(np.abs(vals[pos:pos + ref.size] - ref)) < 1e-12
+        pos += ref.size
+        assert vals[pos] == 9.0
+        pos += 1
+        rd = oracle_mod.compute_quartet(obu, a, u, c, d, deriv=1)
+        rd = np.concatenate([rd[s].reshape(-1) for s in (0, 1, 2, 6, 7, 8, 9, 10, 11)])
+        assert np.max(np.abs(vals[pos:pos + rd.size] - rd)) < 1e-12
+        pos += rd.size
+        r2 = oracle_mod.compute_quartet(obu, a, u, c, u)[0].reshape(-1)
+        assert np.max(np.abs(vals[pos:pos + r2.size] - r2)) < 1e-12
+        pos += r2.size
+    assert pos == vals.size

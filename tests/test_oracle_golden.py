@@ -42,6 +42,17 @@ def test_eri_shellsets_vs_reference_bruteforce(oracle_mod):
     print("worst", worst)
 
 
+def test_eri3c_2c_shellsets_vs_reference_bruteforce(oracle_mod):
+    # 3-centre (a 1|c d) and 2-centre (a 1|c 1) sets with Shell::unit()
+    from golden_util import eri3c_cases
+    for l, pure, nprim, alpha, coeff, O, deriv, rank, vals in eri3c_cases():
+        ob = oracle_mod.OracleBasis(l, pure, nprim, O, alpha, coeff)
+        r = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, deriv, precision=0.0)
+        got = np.concatenate([x.reshape(-1) for x in r])
+        err = float(np.max(np.abs(got - vals)))
+        assert err < 1e-12, (tuple(l), rank, deriv, err)
+
+
 def test_derivative_order_and_map(oracle_mod):
     g = load("derivmap.npz")
     # sets ordered A_x, A_y, A_z, B_x, ..., D_z
