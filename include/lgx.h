@@ -53,6 +53,11 @@ typedef int lgx_status;
 #define LGX_FP64 0  /* every quartet in FP64                                 */
 #define LGX_MIXED 1 /* FP32 VRR/HRR/contraction when K12*K34 < mixed_thresh  */
 
+/* Two-body operators (libint2::Operator, include/libint2/engine.h:98-184). */
+#define LGX_OP_COULOMB 0       /* 1/r                                        */
+#define LGX_OP_ERF_COULOMB 1   /* erf(omega r)/r  (Operator::erf_coulomb)    */
+#define LGX_OP_ERFC_COULOMB 2  /* erfc(omega r)/r (Operator::erfc_coulomb)   */
+
 typedef struct lgx_context lgx_context;
 
 /* One contracted shell (libint2::Shell with one contraction). */
@@ -74,6 +79,15 @@ typedef struct {
 lgx_status lgx_create(lgx_context** ctx, int device);
 /* libint2::finalize() counterpart; releases every device resource. */
 lgx_status lgx_destroy(lgx_context* ctx);
+/* Engine::set(Operator) + Engine::set_params(omega) (engine.h:658-700) for
+ * every later call on the context (shell sets, batches, Schwarz factors,
+ * J/K and gradient passes): op is one of LGX_OP_*, omega >= 0 the range-
+ * separation parameter of erf/erfc (ignored for coulomb).  The attenuated
+ * operators use libint's core integrals (boys.h:1913-1980) on the program
+ * kernel; changing the operator drops the context's Schwarz factors and
+ * quartet bins. */
+lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega);
+
 /* Message of the last failed call on this context (never NULL). */
 const char* lgx_last_error(const lgx_context* ctx);
 /* Library version string. */

@@ -27,7 +27,8 @@
 
 namespace libint2 {
 
-/// Operator enum of the reference (engine.h:98-184); only coulomb is served.
+/// Operator enum of the reference (engine.h:98-184); coulomb, erf_coulomb
+/// and erfc_coulomb are served (the attenuated ones take omega as params).
 enum class Operator {
   overlap = 0,
   kinetic,
@@ -125,6 +126,14 @@ class Engine {
   };
 
   Engine() = default;
+  /// erf_coulomb / erfc_coulomb: params = omega, the range-separation
+  /// parameter (operator_traits<erf_coulomb>::oper_params_type, engine.h:353-370)
+  Engine(Operator oper, size_t max_nprim, int max_l, int deriv_order,
+         scalar_type precision, double omega, BraKet braket = BraKet::invalid,
+         ScreeningMethod screening = default_screening_method())
+      : Engine(oper, max_nprim, max_l, deriv_order, precision, nullptr, braket, screening) {
+    set_params(omega);
+  }
   Engine(Operator oper, size_t max_nprim, int max_l, int deriv_order = 0,
          scalar_type precision = std::numeric_limits<scalar_type>::epsilon(),
          std::nullptr_t /*params*/ = nullptr, BraKet braket = BraKet::invalid,
@@ -135,11 +144,12 @@ class Engine {
         lmax_(max_l),
         deriv_order_(deriv_order),
         screening_(screening) {
-    if (oper_ != Operator::coulomb ||
+    if ((oper_ != Operator::coulomb && oper_ != Operator::erf_coulomb &&
+         oper_ != Operator::erfc_coulomb) ||
         (braket_ != BraKet::xx_xx && braket_ != BraKet::xs_xx && braket_ != BraKet::xs_xs))
       throw std::invalid_argument(
-          "libint2::Engine (GB300): only Operator::coulomb with BraKet::xx_xx, xs_xx or xs_xs "
-          "is implemented");
+          "libint2::Engine (GB300): only Operator::coulomb, erf_coulomb, erfc_coulomb with "
+          "BraKet::xx_xx, xs_xx or xs_xs is implemented");
     if (max_l < 0 || max_l > LGX_MAX_L) throw lmax_exceeded("eri", LGX_MAX_L, max_l);
     if (deriv_order < 0 || deriv_order > LGX_MAX_DERIV)
       throw std::invalid_argument("libint2::Engine (GB300): deriv_order must be 0 or 1");
@@ -150,6 +160,13 @@ class Engine {
   }
 
   Operator oper() const { return oper_; }
+  /// Engine::set_params (engine.h:685-700): omega of erf/erfc_coulomb
+  Engine& set_params(double omega) {
+    if (!(omega >= 0)) throw std::invalid_argument("Engine::set_params: omega must be >= 0");
+    omega_ = omega;
+    return *this;
+  }
+  double params() const { return omega_; }
   BraKet braket() const { return braket_; }
   int deriv_order() const { return deriv_order_; }
   /// rank of the braket: 4 (xx_xx), 3 (xs_xx), 2 (xs_xs) (engine.h:408-417)
@@ -214,11 +231,13 @@ class Engine {
   const target_ptr_vec& compute2(const Shell& s1, const Shell& s2, const Shell& s3,
                                  const Shell& s4, const ShellPair* = nullptr,
                                  const ShellPair* = nullptr) {
-    static_assert(op == Operator::coulomb &&
+    static_assert((op == Operator::coulomb || op == Operator::erf_coulomb ||
+                   op == Operator::erfc_coulomb) &&
                       (bk == BraKet::xx_xx || bk == BraKet::xs_xx || bk == BraKet::xs_xs),
-                  "only coulomb / xx_xx, xs_xx, xs_xs is implemented on the GPU path");
-    if (int(deriv) != deriv_order_ || bk != braket_)
-      throw std::invalid_argument("Engine::compute2: deriv_order or braket mismatch");
+                  "only coulomb / erf_coulomb / erfc_coulomb with xx_xx, xs_xx, xs_xs is "
+                  "implemented on the GPU path");
+    if (int(deriv) != deriv_order_ || bk != braket_ || op != oper_)
+      throw std::invalid_argument("Engine::compute2: deriv_order, operator or braket mismatch");
     return compute_impl(s1, s2, s3, s4);
   }
 
@@ -230,6 +249,7 @@ class Engine {
   int deriv_order_ = 0;
   scalar_type precision_ = 0, ln_precision_ = 0;
   ScreeningMethod screening_ = ScreeningMethod::Original;
+  double omega_ = 0;
   bool initialized_ = false;
   std::vector<value_type> buf_;
   target_ptr_vec targets_;
@@ -260,6 +280,12 @@ class Engine {
     const int method =
         screening_ == ScreeningMethod::Conservative ? LGX_SCREEN_CONSERVATIVE : LGX_SCREEN_ORIGINAL;
     auto& rt = detail::runtime();
+    // the runtime context is shared by every Engine: set this one's operator
+    const int opc = oper_ == Operator::erf_coulomb
+                        ? LGX_OP_ERF_COULOMB
+                        : (oper_ == Operator::erfc_coulomb ? LGX_OP_ERFC_COULOMB : LGX_OP_COULOMB);
+    if (lgx_set_operator(rt.ctx, opc, omega_) != LGX_OK)
+      throw std::runtime_error(std::string("libint2::Engine::compute: ") + lgx_last_error(rt.ctx));
     const lgx_status st = lgx_compute_shellset(rt.ctx, d, deriv_order_, precision_, method,
                                                buf_.data(), buf_.size(), &nsets, &nvalues,
                                                &is_null);

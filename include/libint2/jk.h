@@ -12,6 +12,7 @@
 
 #include "../lgx.h"
 #include "basis.h"
+#include "engine.h"
 
 namespace libint2 {
 namespace gb300 {
@@ -66,6 +67,17 @@ class JKBuilder {
     return st;
   }
   int nbf() const { return nbf_; }
+  /// Operator of the J/K and gradient passes: Operator::coulomb (default),
+  /// erf_coulomb or erfc_coulomb with range-separation parameter omega
+  /// (the long- / short-range exchange of range-separated functionals)
+  void set_operator(Operator op, double omega = 0.0) {
+    const int opc = op == Operator::erf_coulomb
+                        ? LGX_OP_ERF_COULOMB
+                        : (op == Operator::erfc_coulomb ? LGX_OP_ERFC_COULOMB : LGX_OP_COULOMB);
+    if (op != Operator::coulomb && op != Operator::erf_coulomb && op != Operator::erfc_coulomb)
+      throw std::invalid_argument("JKBuilder::set_operator: unsupported operator");
+    check(lgx_set_operator(ctx_, opc, omega));
+  }
 
  private:
   lgx_context* ctx_ = nullptr;

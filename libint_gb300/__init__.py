@@ -28,8 +28,15 @@ BOHR_TO_ANGSTROM = 0.529177210903  # CODATA 2018 (include/libint2/atom.h:52-55)
 
 
 class Operator(enum.Enum):
-    """libint2::Operator (engine.h:98-184); only coulomb is implemented."""
+    """libint2::Operator (engine.h:98-184): coulomb, and the attenuated
+    erf_coulomb / erfc_coulomb (params = omega)."""
     coulomb = 2
+    erf_coulomb = 16
+    erfc_coulomb = 17
+
+
+_OP_CODE = {Operator.coulomb: _lgx.LGX_OP_COULOMB, Operator.erf_coulomb: _lgx.LGX_OP_ERF_COULOMB,
+            Operator.erfc_coulomb: _lgx.LGX_OP_ERFC_COULOMB}
 
 
 class BraKet(enum.Enum):
@@ -274,6 +281,12 @@ class Context:
     def _check(self, st, what):
         _lgx.check(st, self._h, what)
 
+    def set_operator(self, oper: Operator = Operator.coulomb, omega: float = 0.0):
+        """Operator of every later call (lgx_set_operator): coulomb, or
+        erf_coulomb / erfc_coulomb with range-separation parameter omega."""
+        self._check(self._lib.lgx_set_operator(self._h, _OP_CODE[Operator(oper)], float(omega)),
+                    "lgx_set_operator")
+
     # ------------------------------------------------------------ engine
     def compute_shellset(self, shells, deriv=0, precision=np.finfo(float).eps,
                          screening=ScreeningMethod.Original):
@@ -429,8 +442,8 @@ class Engine:
                  precision: float = float(np.finfo(float).eps), braket=None,
                  screening: ScreeningMethod = ScreeningMethod.Original,
                  context: Context | None = None):
-        if oper != Operator.coulomb:
-            raise NotImplementedError("only Operator.coulomb is implemented")
+        if oper not in _OP_CODE:
+            raise NotImplementedError("only Operator coulomb, erf_coulomb, erfc_coulomb")
         if braket not in (None, BraKet.xx_xx, BraKet.xs_xx, BraKet.xs_xs):
             raise NotImplementedError("only BraKet xx_xx, xs_xx and xs_xs are implemented")
         if max_l > MAX_AM:
@@ -446,6 +459,14 @@ class Engine:
         self.set_precision(precision)
         self._ctx = context
         self._results = [None]
+        self._omega = 0.0
+
+    def set_params(self, omega: float):
+        """Engine::set_params: omega of erf_coulomb / erfc_coulomb."""
+        if not omega >= 0:
+            raise ValueError("omega must be >= 0")
+        self._omega = float(omega)
+        return self
 
     def set_precision(self, prec: float):
         self._precision = max(float(prec), 0.0)
@@ -486,6 +507,7 @@ class Engine:
         elif rank == 2:
             full = [shells[0], Shell.unit(), shells[1], Shell.unit()]
         ctx = self._ctx or _default_context()
+        ctx.set_operator(self.oper, self._omega)  # contexts are shared between engines
         r = ctx.compute_shellset(full, self.deriv_order, self._precision, self.screening)
         if r is not None:
             shape = tuple(s.size() for s in shells)

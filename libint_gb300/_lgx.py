@@ -19,6 +19,10 @@ LGX_ERR_WATCHDOG = 5
 LGX_ERR_TOO_LARGE = 6
 LGX_ERR_NO_DEVICE = 7
 
+LGX_OP_COULOMB = 0
+LGX_OP_ERF_COULOMB = 1
+LGX_OP_ERFC_COULOMB = 2
+
 LGX_FP64 = 0
 LGX_MIXED = 1
 LGX_NOALLOC_MAX_NBF = 768
@@ -57,6 +61,7 @@ class LgxLaunchStats(ctypes.Structure):
 SIGNATURES = {
     "lgx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "lgx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "lgx_set_operator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
     "lgx_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "lgx_version": (ctypes.c_char_p, []),
     "lgx_compute_shellset": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(LgxShell),

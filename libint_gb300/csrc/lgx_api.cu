@@ -209,6 +209,9 @@ struct lgx_context {
   std::vector<cudaEvent_t> lev;
   std::vector<lgx_launch_stats> last_launches;
   bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
+  // two-body operator of every pass (lgx_set_operator): LGX_OP_* and omega
+  int op = LGX_OP_COULOMB;
+  double omega = 0.0;
   BasisDev basis, small;
   DBuf gscratch, counter, errflag, primcount;
   DBuf items, out, isnull;
@@ -625,13 +628,15 @@ void fill_common(const lgx_context* ctx, const BasisDev& B, EriArgs& a) {
   a.sph_cd = ctx->sph_cd.as<double>();
   a.sph_cf = ctx->sph_cf.as<float>();
   a.error_flag = ctx->errflag.as<int>();
+  a.op = ctx->op;
+  a.omega2 = ctx->omega * ctx->omega;
   a.fprecision = float(a.precision);
   a.fln_prec = float(std::max(a.ln_prec, -1.0e30));
 }
 
 bool rk_eligible(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode,
                  bool fp32) {
-  if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0) return false;
+  if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0 || ctx->op != LGX_OP_COULOMB) return false;
   return rk_available(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld);
 }
 
@@ -644,6 +649,7 @@ int choose_group(double nq_avg) {
 bool post_gen_ok(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode) {
   int nacc = 0, slots = 0;
   return ctx->use_post && mode == kModeJK && B.std_pure && P.host.deriv == 0 &&
+         ctx->op == LGX_OP_COULOMB &&
          post_info(P.host.la, P.host.lb, P.host.lc, P.host.ld, &nacc, &slots);
 }
 
@@ -1040,8 +1046,9 @@ double sph_flops(int la, int lb, int lc, int ld, const int* pure) {
   return f;
 }
 
-int tune_key(const BinHost& bin, int deriv, int mode, bool fp32) {
-  return ((class_index(bin.la, bin.lb, bin.lc, bin.ld) * 2 + deriv) * 4 + mode) * 2 + (fp32 ? 1 : 0);
+int tune_key(const BinHost& bin, int deriv, int mode, bool fp32, int op) {
+  return (((class_index(bin.la, bin.lb, bin.lc, bin.ld) * 2 + deriv) * 4 + mode) * 2 +
+          (fp32 ? 1 : 0)) * 4 + op;
 }
 
 // Work description of precision space sp of a class bin.
@@ -1079,7 +1086,7 @@ lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool al
     for (int sp = 0; sp < 2; ++sp) {
       if (bin.total[sp] == 0) continue;
       const bool fp32 = (sp == 1) && allow_fp32;
-      const int key = tune_key(bin, deriv, mode, fp32);
+      const int key = tune_key(bin, deriv, mode, fp32, ctx->op);
       if (ctx->tuned.count(key)) continue;
       std::vector<Variant> cand;
       const Variant d = default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
@@ -1187,7 +1194,7 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
       bin_args(C, bin, sp, a);
       a.prim_count = pr.count ? ctx->primcount.as<unsigned long long>() + 2 * bi + sp : nullptr;
       a.counter = counters ? counters + 2 * bi + sp : nullptr;
-      const auto tv = ctx->tuned.find(tune_key(bin, deriv, mode, fp32));
+      const auto tv = ctx->tuned.find(tune_key(bin, deriv, mode, fp32, ctx->op));
       const Variant v = tv != ctx->tuned.end()
                             ? tv->second
                             : default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
@@ -1784,6 +1791,24 @@ lgx_status lgx_jk(lgx_context* ctx, const double* D, double* J, double* K, doubl
   CK(cudaMemcpyAsync(J, ctx->Jd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(K, ctx->Kd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (op != LGX_OP_COULOMB && op != LGX_OP_ERF_COULOMB && op != LGX_OP_ERFC_COULOMB)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "unknown operator");
+  if (!(omega >= 0.0) || !std::isfinite(omega))
+    return fail(ctx, LGX_ERR_INVALID_ARG, "omega must be finite and >= 0");
+  if (op == LGX_OP_COULOMB) omega = 0.0;
+  if (op == ctx->op && omega == ctx->omega) return LGX_OK;
+  ctx->op = op;
+  ctx->omega = omega;
+  // Schwarz factors, quartet bins and the captured pass depend on the operator
+  ctx->basis.schwarz_ok = false;
+  ctx->bins.valid = false;
+  ++ctx->version;
   return LGX_OK;
 }
 

@@ -116,6 +116,22 @@ __global__ void jk_finalize_kernel(const double* Jacc, const double* Kacc, doubl
 
 cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int block, size_t smem,
                        cudaStream_t st) {
+  if (a.op != 0) {  // erf / erfc: the attenuated instantiations
+    if (!fp32) {
+      switch (mode) {
+        case kModeStore: return launch_eri_t<double, kModeStore, PostInterpAtten>(a, grid, block, smem, st);
+        case kModeSchwarz: return launch_eri_t<double, kModeSchwarz, PostInterpAtten>(a, grid, block, smem, st);
+        case kModeJK: return launch_eri_t<double, kModeJK, PostInterpAtten>(a, grid, block, smem, st);
+        case kModeGrad: return launch_eri_t<double, kModeGrad, PostInterpAtten>(a, grid, block, smem, st);
+      }
+    } else {
+      switch (mode) {
+        case kModeStore: return launch_eri_t<float, kModeStore, PostInterpAtten>(a, grid, block, smem, st);
+        case kModeJK: return launch_eri_t<float, kModeJK, PostInterpAtten>(a, grid, block, smem, st);
+      }
+    }
+    return cudaErrorInvalidValue;
+  }
   if (!fp32) {
     switch (mode) {
       case kModeStore: return launch_eri_t<double, kModeStore>(a, grid, block, smem, st);

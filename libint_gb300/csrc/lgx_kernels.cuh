@@ -72,6 +72,10 @@ struct EriArgs {
   double precision, ln_prec;
   float fprecision, fln_prec;
   int screening;  // 0 Original, 1 Conservative
+  // two-body operator: 0 coulomb 1/r, 1 erf(omega r)/r, 2 erfc(omega r)/r
+  // (program kernel only; the register kernels serve coulomb)
+  int op;
+  double omega2;  // omega^2
   // work
   const QuartetItem* items;
   long long nitems;

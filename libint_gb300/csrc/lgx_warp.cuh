@@ -115,6 +115,47 @@ __device__ __forceinline__ void boys_to_stage(const float* __restrict__ tab, flo
   }
 }
 
+// Core integrals of the attenuated operators (libint's erf_coulomb_gm_eval
+// and erfc_coulomb_gm_eval, include/libint2/boys.h:1913-1980): with
+// s = omega^2 / (omega^2 + rho),
+//   erf(omega r)/r :  G_m = s^{m+1/2} F_m(s T)
+//   erfc(omega r)/r:  G_m = F_m(T) - s^{m+1/2} F_m(s T)
+// (dG_m/dT = -G_{m+1} as for F_m, so the recurrences are unchanged).
+// F holds F_m(T) * pfac for op 0 on entry; G[] is scratch of mmax+1 values.
+template <typename T>
+__device__ __forceinline__ void attenuate(const EriArgs& a, T Tval, T rho, int mmax, T pfac,
+                                          T* __restrict__ F);
+template <>
+__device__ __forceinline__ void attenuate<double>(const EriArgs& a, double Tval, double rho,
+                                                  int mmax, double pfac,
+                                                  double* __restrict__ F) {
+  if (a.op == 1 && !(a.omega2 > 0.0)) {
+    for (int m = 0; m <= mmax; ++m) F[m] = 0.0;
+    return;
+  }
+  if (a.op == 2 && !(a.omega2 > 0.0)) return;  // erfc(0) = 1: plain Coulomb
+  const double s = a.omega2 / (a.omega2 + rho);
+  double G[kBoysMaxM + 1];
+  boys_to_stage(a.boys, a.inv_odd, Tval * s, mmax, pfac, G);
+  double f = sqrt(s);
+  for (int m = 0; m <= mmax; ++m, f *= s) F[m] = a.op == 1 ? f * G[m] : F[m] - f * G[m];
+}
+template <>
+__device__ __forceinline__ void attenuate<float>(const EriArgs& a, float Tval, float rho, int mmax,
+                                                 float pfac, float* __restrict__ F) {
+  if (a.op == 1 && !(a.omega2 > 0.0)) {
+    for (int m = 0; m <= mmax; ++m) F[m] = 0.0f;
+    return;
+  }
+  if (a.op == 2 && !(a.omega2 > 0.0)) return;
+  const float w2 = float(a.omega2);
+  const float s = w2 / (w2 + rho);
+  float G[kBoysMaxM + 1];
+  boys_to_stage(a.boys32, Tval * s, mmax, pfac, G);
+  float f = sqrtf(s);
+  for (int m = 0; m <= mmax; ++m, f *= s) F[m] = a.op == 1 ? f * G[m] : F[m] - f * G[m];
+}
+
 // Quartet geometry in the kernel's precision.  FP32 differences come from
 // the hi/lo float centres, so they keep FP32 relative precision.
 template <typename T>
@@ -173,6 +214,9 @@ __device__ __forceinline__ T sel3(int d, T x, T y, T z) {
 
 // Prologue of one primitive quartet into the staging row st (kStage values
 // of T).  Returns false if screened out.
+// ATT: instantiation for the attenuated operators (a.op = erf / erfc); the
+// Coulomb instantiations carry none of that code.
+template <bool ATT>
 __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<double>& g, int idx,
                                          double npbraket, double* st) {
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
@@ -190,7 +234,12 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
   const double PQx = bp.P[0] - kp.P[0], PQy = bp.P[1] - kp.P[1], PQz = bp.P[2] - kp.P[2];
   const double rho = zeta * eta * oogpq;
   const double T = rho * fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
-  boys_to_stage(a.boys, a.inv_odd, T, a.prog.mmax, pfac, st + kStF);
+  if constexpr (ATT) {
+    if (a.op != 1) boys_to_stage(a.boys, a.inv_odd, T, a.prog.mmax, pfac, st + kStF);
+    attenuate<double>(a, T, rho, a.prog.mmax, pfac, st + kStF);
+  } else {
+    boys_to_stage(a.boys, a.inv_odd, T, a.prog.mmax, pfac, st + kStF);
+  }
   const double ez = eta * oogpq, zz = zeta * oogpq;
   st[kStPA + 0] = bp.P[0] - g.A[0];
   st[kStPA + 1] = bp.P[1] - g.A[1];
@@ -215,6 +264,7 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
   return true;
 }
 
+template <bool ATT>
 __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<float>& g, int idx,
                                          double npbraket, float* st) {
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
@@ -235,7 +285,12 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<flo
               PQz = PA[2] - QC[2] + g.AC[2];
   const float rho = zeta * eta * oogpq;
   const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
-  boys_to_stage(a.boys32, T, a.prog.mmax, pfac, st + kStF);
+  if constexpr (ATT) {
+    if (a.op != 1) boys_to_stage(a.boys32, T, a.prog.mmax, pfac, st + kStF);
+    attenuate<float>(a, T, rho, a.prog.mmax, pfac, st + kStF);
+  } else {
+    boys_to_stage(a.boys32, T, a.prog.mmax, pfac, st + kStF);
+  }
   const float ez = eta * oogpq, zz = zeta * oogpq;
   st[kStPA + 0] = PA[0];
   st[kStPA + 1] = PA[1];
@@ -298,7 +353,7 @@ __device__ __forceinline__ PostOp load_post_op(const DevProg& P, int op) {
 
 // Steps 1-2: contracted (e0|f0) accumulators in slots[0, nacc).  Returns the
 // number of primitive quartets that survived screening.
-template <typename T>
+template <typename T, bool ATT = false>
 __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __restrict__ slots,
                                 T* __restrict__ stage, int lane) {
   const DevProg& P = a.prog;
@@ -312,7 +367,7 @@ __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __
     // lane r < R prepares primitive quartet base + r in its own staging row
     const int idx = base + lane;
     bool keep = false;
-    if (lane < R && idx < nq) keep = prologue(a, g, idx, npbraket, stage + lane * kStage);
+    if (lane < R && idx < nq) keep = prologue<ATT>(a, g, idx, npbraket, stage + lane * kStage);
     unsigned ballot = __ballot_sync(0xffffffffu, keep);
     __syncwarp();
     kept += __popc(ballot);
@@ -650,6 +705,17 @@ __device__ void digest_grad(const EriArgs& a, const QuartetGeom<T>& g, const int
 struct PostInterp {
   static constexpr bool kGenerated = false;
 };
+// The same policy for the attenuated operators (erf / erfc core integrals
+// in the prologue); the generated policies serve Coulomb only.
+struct PostInterpAtten : PostInterp {};
+template <typename Post>
+struct PostAtten {
+  static constexpr bool value = false;
+};
+template <>
+struct PostAtten<PostInterpAtten> {
+  static constexpr bool value = true;
+};
 
 template <typename T, int MODE, typename Post = PostInterp>
 __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
@@ -702,7 +768,7 @@ __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
       }
       QuartetGeom<T> g;
       load_geom<T>(a, bpair, kpair, flags & 1, (flags >> 1) & 1, g);
-      const int kept = contract_quartet<T>(a, g, slots, stage, lane);
+      const int kept = contract_quartet<T, PostAtten<Post>::value>(a, g, slots, stage, lane);
       my_prims += kept;
       if (MODE == kModeStore && a.is_null && lane == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
       if (kept == 0) {

@@ -143,6 +143,32 @@ void boys(double T, int mmax, double* F) {
   }
 }
 
+// Two-body operator of the oracle's integrals: 0 coulomb, 1 erf(omega r)/r,
+// 2 erfc(omega r)/r, with the core integrals of libint's
+// erf_coulomb_gm_eval / erfc_coulomb_gm_eval (include/libint2/boys.h:1913-1980):
+// s = omega^2/(omega^2 + rho), G_m = s^{m+1/2} F_m(s T) for erf and
+// F_m(T) - s^{m+1/2} F_m(s T) for erfc.
+int g_op = 0;
+double g_omega = 0.0;
+
+void core_ints(double T, double rho, int mmax, double* F) {
+  if (g_op == 0 || (g_op == 2 && !(g_omega > 0))) {
+    boys(T, mmax, F);
+    return;
+  }
+  if (g_op == 1 && !(g_omega > 0)) {
+    for (int m = 0; m <= mmax; ++m) F[m] = 0.0;
+    return;
+  }
+  const double w2 = g_omega * g_omega;
+  const double s = w2 / (w2 + rho);
+  double G[64];
+  boys(T * s, mmax, G);
+  if (g_op == 2) boys(T, mmax, F);
+  double f = std::sqrt(s);
+  for (int m = 0; m <= mmax; ++m, f *= s) F[m] = g_op == 1 ? f * G[m] : F[m] - f * G[m];
+}
+
 // ------------------------------------------------------- solid harmonics
 // Coefficient of x^lx y^ly z^lz in the real solid harmonic S_{l,m}
 // (Schlegel & Frisch, IJQC 54, 83 (1995), eq. 15), for Cartesian Gaussians
@@ -465,7 +491,7 @@ int compute_quartet(const orc_basis* bs, const int* tgt, int deriv,
       ++nkept;
       const double rho = zeta * eta * oogpq;
       const double T = PQ2 * rho;
-      boys(T, mmax, F);
+      core_ints(T, rho, mmax, F);
       for (int m = 0; m <= mmax; ++m) V(0, 0, m) = F[m] * pfac;
       double W[3], PA[3], WP[3], QC[3], WQ[3];
       for (int i = 0; i < 3; ++i) {
@@ -671,6 +697,13 @@ int nthreads_or_default(int n) {
 extern "C" {
 
 void orc_boys(double T, int mmax, double* F) { boys(T, mmax, F); }
+
+int orc_set_operator(int op, double omega) {
+  if (op < 0 || op > 2 || !(omega >= 0)) return -1;
+  g_op = op;
+  g_omega = op == 0 ? 0.0 : omega;
+  return 0;
+}
 
 double orc_solid_coeff(int l, int m, int lx, int ly, int lz) {
   return solid_coeff(l, m, lx, ly, lz);

@@ -27,6 +27,10 @@ extern "C" {
 
 // Boys function F_m(T), m = 0..mmax (mmax <= 40).
 void orc_boys(double T, int mmax, double* F);
+/* Operator of every later oracle call: 0 coulomb, 1 erf(omega r)/r,
+ * 2 erfc(omega r)/r (libint's erf/erfc_coulomb core integrals,
+ * include/libint2/boys.h:1913-1980).  Process-wide.  Returns 0 or -1. */
+int orc_set_operator(int op, double omega);
 
 // Shell::renorm(): embeds primitive normalization and rescales the
 // contraction to unit self-overlap.  coeff_out/max_ln_coeff_out: nprim each.

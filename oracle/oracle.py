@@ -119,6 +119,19 @@ def boys(T: float, mmax: int) -> np.ndarray:
     return F
 
 
+OP_COULOMB, OP_ERF_COULOMB, OP_ERFC_COULOMB = 0, 1, 2
+
+
+def set_operator(op: int = OP_COULOMB, omega: float = 0.0):
+    """Operator of every later oracle call (process-wide): coulomb, or
+    erf/erfc(omega r)/r with libint's core integrals."""
+    lib = _lib()
+    lib.orc_set_operator.argtypes = [ctypes.c_int, ctypes.c_double]
+    lib.orc_set_operator.restype = ctypes.c_int
+    if lib.orc_set_operator(int(op), float(omega)) != 0:
+        raise ValueError("oracle: bad operator")
+
+
 def solid_coeff(l, m, lx, ly, lz) -> float:
     return _lib().orc_solid_coeff(l, m, lx, ly, lz)
 

@@ -85,6 +85,14 @@ int main(int argc, char** argv) {
     const auto& r2 = e2.compute(obs[t[0]], obs[t[1]]);
     for (size_t i = 0; i < obs[t[0]].size() * obs[t[1]].size(); ++i) put(r2[0][i]);
   }
+  // range-separated operator: erfc(omega r)/r with omega as the params argument
+  libint2::Engine ec(libint2::Operator::erfc_coulomb, obs.max_nprim(), obs.max_l(), 0,
+                     std::numeric_limits<double>::epsilon(), 0.3);
+  for (const auto& q : q1) {
+    const auto& r = ec.compute(obs[q[0]], obs[q[1]], obs[q[2]], obs[q[3]]);
+    const size_t n = obs[q[0]].size() * obs[q[1]].size() * obs[q[2]].size() * obs[q[3]].size();
+    for (size_t i = 0; i < n; ++i) put(r[0][i]);
+  }
   libint2::finalize();
   std::cout << "ok" << std::endl;
   return 0;

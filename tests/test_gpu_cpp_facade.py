@@ -81,4 +81,12 @@ def test_cpp_engine_facade(lgx, oracle_mod, tmp_path):
         r2 = oracle_mod.compute_quartet(obu, a, u, c, u)[0].reshape(-1)
         assert np.max(np.abs(vals[pos:pos + r2.size] - r2)) < 1e-12
         pos += r2.size
+    oracle_mod.set_operator(2, 0.3)
+    try:
+        for q in [(5, 3, 8, 0), (3, 5, 5, 9), (0, 14, 5, 3)]:
+            ref = oracle_mod.compute_quartet(ob, *q)[0].reshape(-1)
+            assert np.max(np.abs(vals[pos:pos + ref.size] - ref)) < 1e-12
+            pos += ref.size
+    finally:
+        oracle_mod.set_operator(0)
     assert pos == vals.size

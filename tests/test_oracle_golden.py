@@ -70,3 +70,56 @@ def test_derivative_order_and_map(oracle_mod):
                 ]
                 for s in range(12):
                     assert g["map"][sbk, stb, stk, s] == perm[s // 3] * 3 + s % 3
+
+
+def _random_quartet_basis(oracle_mod, rng):
+    shells = []
+    for l in rng.integers(0, 4, 4):
+        n = int(rng.integers(1, 3))
+        a = rng.uniform(0.2, 3.0, n)
+        c, _ = oracle_mod.shell_normalize(int(l), a, rng.uniform(0.3, 1.0, n))
+        shells.append((int(l), int(l > 1), a, c, rng.uniform(-1, 1, 3)))
+    return oracle_mod.OracleBasis(np.array([s[0] for s in shells], np.int32),
+                                  np.array([s[1] for s in shells], np.int32),
+                                  np.array([len(s[2]) for s in shells], np.int32),
+                                  np.concatenate([s[4] for s in shells]),
+                                  np.concatenate([s[2] for s in shells]),
+                                  np.concatenate([s[3] for s in shells]))
+
+
+def test_attenuated_operators_identities(oracle_mod):
+    # erf + erfc = coulomb; erf(omega -> large) -> coulomb; and the closed
+    # form of two normalized s Gaussians under erf(omega r)/r:
+    # (pi/a)^{3/2} (pi/g)^{3/2} erf(mu R)/R, 1/mu^2 = 1/a + 1/g + 1/omega^2
+    import math
+    rng = np.random.default_rng(5)
+    try:
+        for t in range(20):
+            ob = _random_quartet_basis(oracle_mod, rng)
+            d = int(t % 3 == 0)
+            oracle_mod.set_operator(0)
+            c = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, d, precision=0.0)
+            oracle_mod.set_operator(1, 0.7)
+            e = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, d, precision=0.0)
+            oracle_mod.set_operator(2, 0.7)
+            f = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, d, precision=0.0)
+            oracle_mod.set_operator(1, 1e4)
+            big = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, d, precision=0.0)
+            for x, y, z, w in zip(c, e, f, big):
+                assert np.max(np.abs(x - (y + z))) < 1e-13
+                assert np.max(np.abs(x - w)) < 1e-7
+        a, g, w = 1.1, 0.7, 0.4
+        ca = oracle_mod.shell_normalize(0, np.array([a]), np.array([1.0]))[0][0]
+        cg = oracle_mod.shell_normalize(0, np.array([g]), np.array([1.0]))[0][0]
+        A, C = np.zeros(3), np.array([0.3, -0.2, 0.5])
+        z = np.zeros(4, np.int32)
+        ob = oracle_mod.OracleBasis(z, z, np.ones(4, np.int32), np.concatenate([A, A, C, A]),
+                                    np.array([a, 0.0, g, 0.0]), np.array([ca, 1.0, cg, 1.0]))
+        oracle_mod.set_operator(1, w)
+        v = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, precision=0.0)[0].item()
+        R = np.linalg.norm(A - C)
+        mu = 1 / math.sqrt(1 / a + 1 / g + 1 / w ** 2)
+        ref = (math.pi / a) ** 1.5 * (math.pi / g) ** 1.5 * ca * cg * math.erf(mu * R) / R
+        assert abs(v - ref) < 1e-13 * abs(ref)
+    finally:
+        oracle_mod.set_operator(0)
