@@ -125,6 +125,7 @@ struct BinHost {
   int bra_class, ket_class;
   long long total[2];   // [0] FP64 space, [1] FP32 space
   long long integrals[2];
+  double last_ms[2] = {0, 0};  // device time of the space's launch in the last pass
   DBuf seg_start[2], seg_bra[2], seg_j0[2];
   int nseg[2];
 };
@@ -166,16 +167,17 @@ struct PassRecs {
   size_t nslots = 0;
   bool count = false;
   bool timed = false;  // per-launch events were recorded (ctx->lev)
+  bool split = false;  // FP64 / FP32 launches on parallel streams
 };
 
 // Identity of a captured J/K pass: every pointer and setting its nodes use.
 struct PassKey {
-  const void* ptr[8] = {};
+  const void* ptr[9] = {};
   double thresh = 0, mixed = 0;
   int mode = -1;
   unsigned long long version = 0;
   bool operator==(const PassKey& o) const {
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < 9; ++i)
       if (ptr[i] != o.ptr[i]) return false;
     return thresh == o.thresh && mixed == o.mixed && mode == o.mode && version == o.version;
   }
@@ -203,9 +205,37 @@ struct lgx_context {
   cudaGraphExec_t jk_exec = nullptr;
   PassKey jk_key;
   PassRecs jk_recs;
-  // per-launch timing events of the batched passes (recorded before each
-  // class launch; inside a captured pass they are event-record nodes) and
-  // the per-launch statistics of the last pass
+  // mixed passes: the FP64 and the FP32 class launches run on two streams
+  // forked from and joined back into `stream` (parallel branches of the
+  // captured pass), so that FP32 launches use the issue slots that the
+  // FP64-pipe-bound launches leave idle; FP64 launches then hold at most
+  // fp64_bps blocks per SM (0: no cap).  `launch_stream` / `scratch` are
+  // the stream and the program-kernel slot scratch of the launch being
+  // enqueued (the FP32 branch has its own scratch).
+  static constexpr int kMaxBranches = 4;  // streams per precision
+  bool overlap = true;
+  int branches = 3;
+  // 0: longest first onto the least-loaded branch, issued longest first;
+  // 1: round-robin in bin order (default: best or level on (H2O)32 cc-pVDZ,
+  // (H2O)8 and (H2O)64 cc-pVTZ); 2: as 0 but issued in bin order
+  int branch_policy = 1;
+  int fp64_bps = 0;
+  cudaStream_t s64[kMaxBranches] = {}, s32[kMaxBranches] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[2 * kMaxBranches] = {};
+  cudaStream_t launch_stream = nullptr;
+  DBuf gscratch_br[2 * kMaxBranches];  // program-kernel slot scratch per branch
+  DBuf* scratch = nullptr;
+  // identity of the branch scratch buffers (their addresses enter a
+  // captured pass): changes whenever one of them is reallocated
+  const void* scratch_sig() const {
+    unsigned long long h = 1469598103934665603ull;
+    for (const auto& b : gscratch_br) h = (h ^ reinterpret_cast<uintptr_t>(b.p)) * 1099511628211ull;
+    return reinterpret_cast<const void*>(uintptr_t(h));
+  }
+  // per-launch timing events of the batched passes (a start and an end
+  // event around each class launch, on the launch's stream; inside a
+  // captured pass they are event-record nodes) and the per-launch
+  // statistics of the last pass
   std::vector<cudaEvent_t> lev;
   std::vector<lgx_launch_stats> last_launches;
   bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
@@ -597,13 +627,14 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
     const size_t per_block = size_t(L.wpb) * slot_bytes;
     const size_t cap = size_t(2) << 30;  // 2 GiB of per-warp slot scratch at most
     grid = std::min<long long>(grid, std::max<size_t>(1, cap / per_block));
+    DBuf& scr = ctx->scratch ? *ctx->scratch : ctx->gscratch;
     if (ctx->noalloc) {  // use the slot scratch a previous pass left, never grow it
-      if (ctx->gscratch.n < per_block)
+      if (scr.n < per_block)
         return fail(ctx, LGX_ERR_INVALID_ARG,
                     "slot scratch not prepared: call lgx_jk_device once with the same settings");
-      grid = std::min<long long>(grid, (long long)(ctx->gscratch.n / per_block));
+      grid = std::min<long long>(grid, (long long)(scr.n / per_block));
     } else {
-      CK(ctx->gscratch.ensure(size_t(grid) * per_block));
+      CK(scr.ensure(size_t(grid) * per_block));
     }
   }
   L.grid = int(grid);
@@ -671,7 +702,7 @@ lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, boo
   fill_common(ctx, B, a);
   a.group = group;
   CK(rk_launch(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, nwork, ctx->nsm,
-               ctx->stream));
+               ctx->launch_stream ? ctx->launch_stream : ctx->stream));
   return LGX_OK;
 }
 
@@ -691,16 +722,18 @@ lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bo
   a.slot_stride = L.stride;
   a.stage_rows = L.rows;
   a.global_slots = L.global ? 1 : 0;
-  a.gscratch = ctx->gscratch.p;
+  a.gscratch = (ctx->scratch ? ctx->scratch : &ctx->gscratch)->p;
+  if (a.max_bps > 0) L.grid = std::min(L.grid, ctx->nsm * a.max_bps);
+  cudaStream_t lst = ctx->launch_stream ? ctx->launch_stream : ctx->stream;
   const long long nwarps = (long long)L.grid * L.wpb;
   a.chunk = int(std::max<long long>(1, std::min<long long>(32, nwork / (nwarps * 8))));
   a.max_chunks = nwork / a.chunk + 2;
-  if (own_counter) CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream));
+  if (own_counter) CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), lst));
   if (gen)
     CK(post_launch(fp32, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, L.grid, L.block, L.smem,
-                   ctx->stream));
+                   lst));
   else
-    CK(launch_eri(a, mode, fp32, L.grid, L.block, L.smem, ctx->stream));
+    CK(launch_eri(a, mode, fp32, L.grid, L.block, L.smem, lst));
   return LGX_OK;
 }
 
@@ -1155,13 +1188,62 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
                         EriArgs base, PassRecs& pr) {
   BinCache& C = ctx->bins;
   pr = PassRecs{};
-  size_t nlaunch = 0;
-  for (const auto& bin : C.bins) nlaunch += (bin->total[0] > 0) + (bin->total[1] > 0);
+  // the launches of the pass: one per class bin and precision space
+  struct Job {
+    size_t bi;
+    int sp;
+    bool fp32;
+    double est;  // expected device time (ms, or a relative cost before any pass)
+    int branch;
+  };
+  std::vector<Job> jobs;
+  for (size_t bi = 0; bi < C.bins.size(); ++bi) {
+    const BinHost& bin = *C.bins[bi];
+    for (int sp = 0; sp < 2; ++sp) {
+      if (bin.total[sp] == 0) continue;
+      const bool fp32 = (sp == 1) && allow_fp32;
+      const double est = bin.last_ms[sp] > 0
+                             ? bin.last_ms[sp]
+                             : 1e-9 * double(bin.total[sp]) * bin.nq_avg * (fp32 ? 1.0 : 8.0);
+      jobs.push_back({bi, sp, fp32, est, 0});
+    }
+  }
+  const size_t nlaunch = jobs.size();
+  // Parallel branches: each precision's launches spread over nbr streams
+  // (round-robin, or longest first onto the least-loaded branch with the
+  // bins' device times of the previous pass as estimates), so that the
+  // tails of the persistent class launches overlap with other launches and
+  // FP32 launches run beside FP64-pipe-bound ones.
+  const bool split = ctx->overlap && !ctx->noalloc && nlaunch > 1;
+  pr.split = split;
+  const int nbr = std::max(1, std::min(ctx->branches, lgx_context::kMaxBranches));
+  if (split && ctx->branch_policy == 1) {  // round-robin in bin order
+    int nxt[2] = {0, 0};
+    for (auto& j : jobs) j.branch = nxt[j.fp32 ? 1 : 0]++ % nbr;
+  } else if (split) {  // longest first onto the least-loaded branch
+    std::vector<size_t> ord(jobs.size());
+    for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](size_t x, size_t y) { return jobs[x].est > jobs[y].est; });
+    double load[2][lgx_context::kMaxBranches] = {};
+    for (size_t i : ord) {
+      Job& j = jobs[i];
+      double* l = load[j.fp32 ? 1 : 0];
+      int b = 0;
+      for (int k = 1; k < nbr; ++k)
+        if (l[k] < l[b]) b = k;
+      j.branch = b;
+      l[b] += j.est;
+    }
+    if (ctx->branch_policy == 0)  // issue longest first too (else in bin order)
+      std::stable_sort(jobs.begin(), jobs.end(),
+                       [](const Job& x, const Job& y) { return x.est > y.est; });
+  }
   // per-launch events persist in the context (a captured pass refers to
   // them); the no-allocation path only uses events that already exist
-  pr.timed = ctx->lev.size() >= nlaunch;
+  pr.timed = ctx->lev.size() >= 2 * nlaunch;
   if (!pr.timed && !ctx->noalloc) {
-    while (ctx->lev.size() < nlaunch) {
+    while (ctx->lev.size() < 2 * nlaunch) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e));
       ctx->lev.push_back(e);
@@ -1182,28 +1264,59 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
   CK(cudaStreamIsCapturing(ctx->stream, &cap));
   const unsigned evflags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0;
   CK(cudaEventRecordWithFlags(ctx->ev0, ctx->stream, evflags));
-  for (size_t bi = 0; bi < C.bins.size(); ++bi) {
-    BinHost& bin = *C.bins[bi];
+  if (split) {
+    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+    for (int b = 0; b < nbr; ++b) {
+      CK(cudaStreamWaitEvent(ctx->s64[b], ctx->ev_fork, 0));
+      CK(cudaStreamWaitEvent(ctx->s32[b], ctx->ev_fork, 0));
+    }
+  }
+  struct Restore {  // launch stream / scratch back to the context defaults
+    lgx_context* c;
+    ~Restore() {
+      c->launch_stream = nullptr;
+      c->scratch = nullptr;
+    }
+  } restore{ctx};
+  for (const Job& j : jobs) {
+    BinHost& bin = *C.bins[j.bi];
     ProgDev* P = nullptr;
     lgx_status s = get_prog(ctx, bin.la, bin.lb, bin.lc, bin.ld, deriv, &P);
     if (s != LGX_OK) return s;
-    for (int sp = 0; sp < 2; ++sp) {
-      if (bin.total[sp] == 0) continue;
-      const bool fp32 = (sp == 1) && allow_fp32;
-      EriArgs a = base;
-      bin_args(C, bin, sp, a);
-      a.prim_count = pr.count ? ctx->primcount.as<unsigned long long>() + 2 * bi + sp : nullptr;
-      a.counter = counters ? counters + 2 * bi + sp : nullptr;
-      const auto tv = ctx->tuned.find(tune_key(bin, deriv, mode, fp32, ctx->op));
-      const Variant v = tv != ctx->tuned.end()
-                            ? tv->second
-                            : default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
-      if (pr.timed) CK(cudaEventRecordWithFlags(ctx->lev[pr.recs.size()], ctx->stream, evflags));
-      s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg, &v);
-      if (s != LGX_OK) return s;
-      pr.integrals += bin.integrals[sp];
-      ++pr.launches;
-      pr.recs.push_back({int(bi), sp, fp32, v});
+    const int sp = j.sp;
+    const bool fp32 = j.fp32;
+    EriArgs a = base;
+    bin_args(C, bin, sp, a);
+    a.prim_count = pr.count ? ctx->primcount.as<unsigned long long>() + 2 * j.bi + sp : nullptr;
+    a.counter = counters ? counters + 2 * j.bi + sp : nullptr;
+    const auto tv = ctx->tuned.find(tune_key(bin, deriv, mode, fp32, ctx->op));
+    const Variant v = tv != ctx->tuned.end()
+                          ? tv->second
+                          : default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
+    cudaStream_t st = ctx->stream;
+    if (split) {
+      const int b = j.branch;
+      st = fp32 ? ctx->s32[b] : ctx->s64[b];
+      // program-kernel slot scratch: one region per branch
+      ctx->scratch = (fp32 || b > 0) ? &ctx->gscratch_br[(fp32 ? nbr : 0) + b] : &ctx->gscratch;
+      if (!fp32 && allow_fp32) a.max_bps = ctx->fp64_bps;
+    }
+    ctx->launch_stream = st;
+    const size_t li = pr.recs.size();
+    if (pr.timed) CK(cudaEventRecordWithFlags(ctx->lev[2 * li], st, evflags));
+    s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg, &v);
+    if (s != LGX_OK) return s;
+    if (pr.timed) CK(cudaEventRecordWithFlags(ctx->lev[2 * li + 1], st, evflags));
+    pr.integrals += bin.integrals[sp];
+    ++pr.launches;
+    pr.recs.push_back({int(j.bi), sp, fp32, v});
+  }
+  if (split) {
+    for (int b = 0; b < nbr; ++b) {
+      CK(cudaEventRecord(ctx->ev_join[2 * b], ctx->s64[b]));
+      CK(cudaEventRecord(ctx->ev_join[2 * b + 1], ctx->s32[b]));
+      CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[2 * b], 0));
+      CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[2 * b + 1], 0));
     }
   }
   CK(cudaEventRecordWithFlags(ctx->ev1, ctx->stream, evflags));
@@ -1263,8 +1376,9 @@ lgx_status finish_bins(lgx_context* ctx, BasisDev& B, int deriv, bool allow_fp32
     ls.ms = -1.0;
     if (pr.timed) {
       float ms = 0;
-      CK(cudaEventElapsedTime(&ms, ctx->lev[i], i + 1 < recs.size() ? ctx->lev[i + 1] : ctx->ev1));
+      CK(cudaEventElapsedTime(&ms, ctx->lev[2 * i], ctx->lev[2 * i + 1]));
       ls.ms = ms;
+      C.bins[r.bin]->last_ms[r.sp] = ms;
     }
     ctx->last_launches.push_back(ls);
     if (class_profile()) {
@@ -1340,6 +1454,12 @@ lgx_status lgx_create(lgx_context** out, int device) {
     CK(cudaEventCreate(&c->ev1));
     CK(cudaEventCreate(&c->ev2));
     CK(cudaEventCreate(&c->ev3));
+    for (int b = 0; b < lgx_context::kMaxBranches; ++b) {
+      CK(cudaStreamCreateWithFlags(&c->s64[b], cudaStreamNonBlocking));
+      CK(cudaStreamCreateWithFlags(&c->s32[b], cudaStreamNonBlocking));
+    }
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    for (auto& e : c->ev_join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     const auto boys = make_boys_table();
     const auto sph = make_sph_table();
     CK(c->boys.ensure(boys.size() * sizeof(double)));
@@ -1398,6 +1518,10 @@ lgx_status lgx_create(lgx_context** out, int device) {
     if (const char* e = getenv("LGX_DISABLE_POST")) c->use_post = (e[0] == '0');
     if (const char* e = getenv("LGX_TUNE")) c->tune = (e[0] != '0');
     if (const char* e = getenv("LGX_GRAPHS")) c->use_graphs = (e[0] != '0');
+    if (const char* e = getenv("LGX_OVERLAP")) c->overlap = (e[0] != '0');
+    if (const char* e = getenv("LGX_FP64_BPS")) c->fp64_bps = std::max(0, atoi(e));
+    if (const char* e = getenv("LGX_BRANCHES")) c->branches = std::max(1, atoi(e));
+    if (const char* e = getenv("LGX_BRANCH_POLICY")) c->branch_policy = std::min(2, std::max(0, atoi(e)));
     if (const char* e = getenv("LGX_TUNE_MIN")) c->tune_min = std::max(1LL, atoll(e));
 
     {
@@ -1425,9 +1549,19 @@ lgx_status lgx_destroy(lgx_context* ctx) {
   if (ctx->ev3) cudaEventDestroy(ctx->ev3);
   if (ctx->jk_exec) cudaGraphExecDestroy(ctx->jk_exec);
   for (cudaEvent_t e : ctx->lev) cudaEventDestroy(e);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  for (cudaEvent_t e : ctx->ev_join)
+    if (e) cudaEventDestroy(e);
+  std::vector<cudaStream_t> side;
+  for (int b = 0; b < lgx_context::kMaxBranches; ++b) {
+    side.push_back(ctx->s64[b]);
+    side.push_back(ctx->s32[b]);
+  }
   cudaStream_t st = ctx->stream;
   delete ctx;
   if (st) cudaStreamDestroy(st);
+  for (cudaStream_t x : side)
+    if (x) cudaStreamDestroy(x);
   return LGX_OK;
 }
 
@@ -1622,8 +1756,8 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   // also makes every allocation) and is then captured for the next call.
   PassKey key;
   const void* kp[] = {dD, dJ, dK, ctx->Df.p, ctx->Jacc.p, ctx->Kacc.p, ctx->gscratch.p,
-                      ctx->primcount.p};
-  for (int i = 0; i < 8; ++i) key.ptr[i] = kp[i];
+                      ctx->primcount.p, ctx->scratch_sig()};
+  for (int i = 0; i < 9; ++i) key.ptr[i] = kp[i];
   key.thresh = thresh;
   key.mixed = mode == LGX_MIXED ? mixed : 0.0;
   key.mode = mode;
@@ -1645,7 +1779,8 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   CK(cudaEventElapsedTime(&pass_ms, ctx->ev2, ctx->ev3));
   s = check_errflag(ctx);
   if (s != LGX_OK) return s;
-  if (!replay && graphable && key.ptr[6] == ctx->gscratch.p && key.ptr[7] == ctx->primcount.p) {
+  if (!replay && graphable && key.ptr[6] == ctx->gscratch.p && key.ptr[7] == ctx->primcount.p &&
+      key.ptr[8] == ctx->scratch_sig()) {
     if (ctx->jk_exec) {
       cudaGraphExecDestroy(ctx->jk_exec);
       ctx->jk_exec = nullptr;
@@ -1667,6 +1802,7 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
       return fail(ctx, LGX_ERR_CUDA, cudaGetErrorString(ie));
     }
     ctx->jk_key = key;
+    ctx->jk_recs = tmp;  // replays follow the captured launch order
   }
   if (stats) {
     stats->pass_ms = pass_ms;

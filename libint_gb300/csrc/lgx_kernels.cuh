@@ -83,6 +83,7 @@ struct EriArgs {
   int implicit;   // 1: use bin, 0: use items
   int chunk;
   int group;           // register kernels: lanes per quartet (power of 2)
+  int max_bps;         // host-side launch cap: blocks per SM (0: occupancy limit)
   unsigned long long* counter;
   // slots
   int slot_stride;     // slots per warp (elements of T)

@@ -541,6 +541,7 @@ cudaError_t rk_launch_one(const EriArgs& a, long long work, int nsm, cudaStream_
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, block, 0) != cudaSuccess || occ < 1)
     occ = 1;
+  if (a.max_bps > 0 && occ > a.max_bps) occ = a.max_bps;
   long long grid = (long long)nsm * occ;
   const long long need = (work * a.group + block - 1) / block;
   if (need < grid) grid = need < 1 ? 1 : need;
