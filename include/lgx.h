@@ -40,9 +40,10 @@ typedef int lgx_status;
 #define LGX_ERR_TOO_LARGE 6     /* request exceeds a documented size limit   */
 #define LGX_ERR_NO_DEVICE 7     /* no CUDA device / wrong architecture       */
 
-/* Largest angular momentum per shell and derivative order supported. */
+/* Largest angular momentum per shell and derivative order supported
+ * (deriv_order 2 through lgx_compute_shellset for shells up to l = 2). */
 #define LGX_MAX_L 3
-#define LGX_MAX_DERIV 1
+#define LGX_MAX_DERIV 2
 #define LGX_MAX_NPRIM 16
 
 /* Primitive-screening methods (ScreeningMethod, shell.h:1041-1059). */
@@ -104,6 +105,10 @@ const char* lgx_version(void);
  * buffer `out` (capacity `out_capacity` doubles), and *is_null = 1 when every
  * primitive quartet was screened out (libint returns results()[0]==nullptr,
  * engine.impl.h:1781-1784; `out` is then untouched). */
+/* deriv 2 (compute2<coulomb, xx_xx, 2>): 78 second-derivative sets in
+ * libint's order (coordinate pairs c1 <= c2 over A_x..D_z, row-major,
+ * CartesianDerivIterator<4>(2) of include/libint2/deriv_iter.h), for shells
+ * up to l = 2 (LGX_ERR_LMAX_EXCEEDED above). */
 lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4],
                                 int deriv, double precision, int screening,
                                 double* out, size_t out_capacity, int* nsets,

@@ -152,7 +152,9 @@ class Engine {
           "BraKet::xx_xx, xs_xx or xs_xs is implemented");
     if (max_l < 0 || max_l > LGX_MAX_L) throw lmax_exceeded("eri", LGX_MAX_L, max_l);
     if (deriv_order < 0 || deriv_order > LGX_MAX_DERIV)
-      throw std::invalid_argument("libint2::Engine (GB300): deriv_order must be 0 or 1");
+      throw std::invalid_argument("libint2::Engine (GB300): deriv_order must be 0, 1 or 2");
+    if (deriv_order == 2 && braket_ != BraKet::xx_xx)
+      throw std::invalid_argument("libint2::Engine (GB300): deriv_order 2 needs BraKet::xx_xx");
     set_precision(precision);
     if (!initialized()) initialize();
     targets_.assign(nshellsets(), nullptr);
@@ -275,7 +277,7 @@ class Engine {
       nv *= sh[k]->size();
     }
     const unsigned ns = nshellsets();
-    buf_.resize(nv * (deriv_order_ ? 12 : 1));
+    buf_.resize(nv * (deriv_order_ == 2 ? 78 : (deriv_order_ ? 12 : 1)));
     int nsets = 0, nvalues = 0, is_null = 0;
     const int method =
         screening_ == ScreeningMethod::Conservative ? LGX_SCREEN_CONSERVATIVE : LGX_SCREEN_ORIGINAL;

@@ -291,7 +291,7 @@ class Context:
     def compute_shellset(self, shells, deriv=0, precision=np.finfo(float).eps,
                          screening=ScreeningMethod.Original):
         arr = (_lgx.LgxShell * 4)(*[s._c() for s in shells])
-        nsets = 12 if deriv else 1
+        nsets = {0: 1, 1: 12, 2: 78}[int(deriv)]
         nv = int(np.prod([s.size() for s in shells]))
         out = np.zeros(nsets * nv)
         ns, nvals, isnull = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -448,8 +448,10 @@ class Engine:
             raise NotImplementedError("only BraKet xx_xx, xs_xx and xs_xs are implemented")
         if max_l > MAX_AM:
             raise LgxError(_lgx.LGX_ERR_LMAX_EXCEEDED, "max_l exceeds LGX_MAX_L")
-        if deriv_order not in (0, 1):
-            raise NotImplementedError("deriv_order must be 0 or 1")
+        if deriv_order not in (0, 1, 2):
+            raise NotImplementedError("deriv_order must be 0, 1 or 2")
+        if deriv_order == 2 and braket not in (None, BraKet.xx_xx):
+            raise NotImplementedError("deriv_order 2 is implemented for BraKet.xx_xx")
         self.oper = oper
         self.braket = braket or BraKet.xx_xx
         self.max_nprim = max_nprim
@@ -483,6 +485,8 @@ class Engine:
         return _BRAKET_RANK[self.braket]
 
     def nshellsets(self):
+        if self.deriv_order == 2:
+            return 78
         return 3 * self.braket_rank() if self.deriv_order else 1
 
     def results(self):
@@ -511,7 +515,9 @@ class Engine:
         r = ctx.compute_shellset(full, self.deriv_order, self._precision, self.screening)
         if r is not None:
             shape = tuple(s.size() for s in shells)
-            r = [r[i].reshape(shape) for i in (_DERIV_SETS[rank] if self.deriv_order else [0])]
+            sel = [0] if self.deriv_order == 0 else (
+                _DERIV_SETS[rank] if self.deriv_order == 1 else range(78))
+            r = [r[i].reshape(shape) for i in sel]
         self._results = r if r is not None else [None] * self.nshellsets()
         if r is None:
             return None

@@ -1421,6 +1421,179 @@ lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool all
   return finish_bins(ctx, B, deriv, allow_fp32, pr, stats);
 }
 
+// Cartesian component index and exponents in the standard order
+// (cgshell_ordering.h:125-131): lx descending, then ly descending.
+int cart_idx(int l, int lx, int ly) {
+  const int i = l - lx;
+  return i * (i + 1) / 2 + (i - ly);
+}
+void cart_exp(int l, int c, int* e) {
+  int i = 0;
+  while ((i + 1) * (i + 2) / 2 <= c) ++i;
+  const int ly = i - (c - i * (i + 1) / 2);
+  e[0] = l - i;
+  e[1] = ly;
+  e[2] = l - e[0] - e[1];
+}
+
+// deriv_order = 2 (Engine::compute2<coulomb, xx_xx, 2>): the 78 second-
+// derivative shell sets, composed from first-derivative sets that the GPU
+// computes in one batched launch.  With X' = shell X raised by one angular
+// momentum quantum, Cartesian, every primitive coefficient times 2 alpha, and
+// X_ = X lowered by one,
+//   d/dY_j d/dX_i (..x..) = d/dY_j (..X'(x+1_i)..) - x_i d/dY_j (..X_(x-1_i)..)
+// for every pair of centres (both factors act at the primitive level, so for
+// Y = X the 2 alpha of X' multiplies the one the inner derivative brings).
+// Sets in libint's order (CartesianDerivIterator<4>(2),
+// include/libint2/deriv_iter.h: coordinate pairs c1 <= c2, row-major over
+// A_x..D_z) and in the caller's shell order, so no derivative remap is
+// needed; pure shells are transformed after the Cartesian composition.
+// Shells up to l = 2: the raised copies reach LGX_MAX_L.
+lgx_status shellset_deriv2(lgx_context* ctx, const lgx_shell shells[4], double precision,
+                           int screening, double* out, size_t out_capacity, int* nsets,
+                           int* nvalues, int* is_null) {
+  if (screening != LGX_SCREEN_ORIGINAL && screening != LGX_SCREEN_CONSERVATIVE)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "unsupported screening method");
+  int lx[4], n[4];
+  size_t nv = 1;
+  for (int k = 0; k < 4; ++k) {
+    if (!shells[k].alpha || !shells[k].coeff) return fail(ctx, LGX_ERR_INVALID_ARG, "null shell data");
+    lx[k] = shells[k].l;
+    if (lx[k] < 0 || lx[k] > kMaxL - 1)
+      return fail(ctx, LGX_ERR_LMAX_EXCEEDED,
+                  "deriv_order 2: shell angular momentum above LGX_MAX_L - 1");
+    n[k] = nfunc(lx[k], shells[k].pure ? 1 : 0);
+    nv *= size_t(n[k]);
+  }
+  if (nv * 78 > out_capacity) return fail(ctx, LGX_ERR_TOO_LARGE, "output buffer too small");
+  CK(cudaSetDevice(ctx->device));
+  // small basis: 0-3 the shells, 4+X raised X, 8+X lowered X
+  int l[12], pure[12], np[12], atom[12];
+  double O[36];
+  std::vector<double> al, co;
+  auto push = [&](int k, int X, int dl, bool scale) {
+    const lgx_shell& sh = shells[X];
+    l[k] = sh.l + dl;
+    pure[k] = dl == 0 ? (sh.pure ? 1 : 0) : 0;
+    np[k] = sh.nprim;
+    atom[k] = X;
+    for (int x = 0; x < 3; ++x) O[3 * k + x] = sh.origin[x];
+    for (int p = 0; p < sh.nprim; ++p) {
+      al.push_back(sh.alpha[p]);
+      co.push_back(scale ? 2.0 * sh.alpha[p] * sh.coeff[p] : sh.coeff[p]);
+    }
+  };
+  // primitive data must follow the shell index order (upload_basis
+  // derives the primitive offsets from it)
+  for (int X = 0; X < 4; ++X) push(X, X, 0, false);
+  for (int X = 0; X < 4; ++X) push(4 + X, X, +1, true);
+  for (int X = 0; X < 4; ++X) push(8 + X, X, lx[X] > 0 ? -1 : 0, false);
+  lgx_status s = upload_basis(ctx, ctx->small, 12, l, pure, np, atom, O, al.data(), co.data());
+  if (s != LGX_OK) return s;
+  const double ln_prec =
+      precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
+  s = ensure_pairs(ctx, ctx->small, ln_prec, screening);
+  if (s != LGX_OK) return s;
+  // first-derivative sets of the raised / lowered quartets, one launch
+  std::vector<int32_t> q;
+  std::vector<int64_t> off;
+  size_t su[4] = {0, 0, 0, 0}, sd[4] = {0, 0, 0, 0}, total = 0;
+  int64_t offu[4] = {0, 0, 0, 0}, offd[4] = {-1, -1, -1, -1};
+  for (int X = 0; X < 4; ++X)
+    for (int dir = 0; dir < 2; ++dir) {
+      if (dir == 1 && lx[X] == 0) continue;
+      int qq[4] = {0, 1, 2, 3};
+      qq[X] = (dir == 0 ? 4 : 8) + X;
+      size_t sz = 12;
+      for (int k = 0; k < 4; ++k) sz *= size_t(k == X ? ncart(l[qq[k]]) : n[k]);
+      q.insert(q.end(), qq, qq + 4);
+      off.push_back(int64_t(total));
+      if (dir == 0) { offu[X] = int64_t(total); su[X] = sz / 12; }
+      else { offd[X] = int64_t(total); sd[X] = sz / 12; }
+      total += sz;
+    }
+  const long long nq = (long long)off.size();
+  CK(ctx->out.ensure(std::max<size_t>(total, 1) * sizeof(double)));
+  CK(ctx->isnull.ensure(size_t(nq) * sizeof(int)));
+  CK(cudaMemsetAsync(ctx->out.p, 0, total * sizeof(double), ctx->stream));
+  s = run_explicit(ctx, ctx->small, q.data(), nq, 1, kModeStore, 0.0, off.data(),
+                   ctx->out.as<double>(), ctx->isnull.as<int>(), precision, screening, nullptr);
+  if (s != LGX_OK) return s;
+  std::vector<double> d1(total);
+  std::vector<int> nul(nq);
+  CK(cudaMemcpyAsync(d1.data(), ctx->out.p, total * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(nul.data(), ctx->isnull.p, nq * sizeof(int), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  s = check_errflag(ctx);
+  if (s != LGX_OK) return s;
+  *nsets = 78;
+  *nvalues = int(nv);
+  bool all_null = true;
+  for (int v : nul) all_null = all_null && v != 0;
+  *is_null = all_null ? 1 : 0;
+  if (all_null) return LGX_OK;
+  std::vector<double> cart;
+  int set = 0;
+  for (int c1 = 0; c1 < 12; ++c1)
+    for (int c2 = c1; c2 < 12; ++c2, ++set) {
+      const int X = c1 / 3, i = c1 % 3;
+      int dc[4] = {n[0], n[1], n[2], n[3]}, du[4] = {n[0], n[1], n[2], n[3]},
+          dd[4] = {n[0], n[1], n[2], n[3]};
+      dc[X] = ncart(lx[X]);
+      du[X] = ncart(lx[X] + 1);
+      dd[X] = lx[X] > 0 ? ncart(lx[X] - 1) : 0;
+      const double* U = d1.data() + offu[X] + size_t(c2) * su[X];
+      const double* Dn = lx[X] > 0 ? d1.data() + offd[X] + size_t(c2) * sd[X] : nullptr;
+      cart.assign(size_t(dc[0]) * dc[1] * dc[2] * dc[3], 0.0);
+      int ix[4];
+      size_t o = 0;
+      for (ix[0] = 0; ix[0] < dc[0]; ++ix[0])
+        for (ix[1] = 0; ix[1] < dc[1]; ++ix[1])
+          for (ix[2] = 0; ix[2] < dc[2]; ++ix[2])
+            for (ix[3] = 0; ix[3] < dc[3]; ++ix[3], ++o) {
+              int e[3];
+              cart_exp(lx[X], ix[X], e);
+              int iu[4] = {ix[0], ix[1], ix[2], ix[3]};
+              int eu[3] = {e[0], e[1], e[2]};
+              ++eu[i];
+              iu[X] = cart_idx(lx[X] + 1, eu[0], eu[1]);
+              double v = U[((size_t(iu[0]) * du[1] + iu[1]) * du[2] + iu[2]) * du[3] + iu[3]];
+              if (e[i] > 0) {
+                int id[4] = {ix[0], ix[1], ix[2], ix[3]};
+                int ed[3] = {e[0], e[1], e[2]};
+                --ed[i];
+                id[X] = cart_idx(lx[X] - 1, ed[0], ed[1]);
+                v -= e[i] * Dn[((size_t(id[0]) * dd[1] + id[1]) * dd[2] + id[2]) * dd[3] + id[3]];
+              }
+              cart[o] = v;
+            }
+      double* dst = out + size_t(set) * nv;
+      if (!shells[X].pure) {
+        std::memcpy(dst, cart.data(), nv * sizeof(double));
+        continue;
+      }
+      size_t outer = 1, inner = 1;
+      for (int t = 0; t < X; ++t) outer *= size_t(dc[t]);
+      for (int t = X + 1; t < 4; ++t) inner *= size_t(dc[t]);
+      const int ncx = dc[X], npx = 2 * lx[X] + 1;
+      std::fill(dst, dst + nv, 0.0);
+      for (size_t a = 0; a < outer; ++a)
+        for (int p = 0; p < npx; ++p)
+          for (int c = 0; c < ncx; ++c) {
+            int e[3];
+            cart_exp(lx[X], c, e);
+            const double coef = solid_coeff(lx[X], p - lx[X], e[0], e[1], e[2]);
+            if (coef == 0.0) continue;
+            const double* src = &cart[(a * ncx + c) * inner];
+            double* d = &dst[(a * npx + p) * inner];
+            for (size_t b = 0; b < inner; ++b) d[b] += coef * src[b];
+          }
+    }
+  return LGX_OK;
+}
+
 }  // namespace
 
 // =================================================================== C ABI
@@ -1572,8 +1745,11 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!shells || !out || !nsets || !nvalues || !is_null)
     return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (deriv == 2)
+    return shellset_deriv2(ctx, shells, precision, screening, out, out_capacity, nsets, nvalues,
+                           is_null);
   if (deriv < 0 || deriv > kMaxDeriv)
-    return fail(ctx, LGX_ERR_INVALID_ARG, "deriv must be 0 or 1");
+    return fail(ctx, LGX_ERR_INVALID_ARG, "deriv must be 0, 1 or 2");
   if (screening != LGX_SCREEN_ORIGINAL && screening != LGX_SCREEN_CONSERVATIVE)
     return fail(ctx, LGX_ERR_INVALID_ARG, "unsupported screening method");
   CK(cudaSetDevice(ctx->device));

@@ -694,6 +694,128 @@ int nthreads_or_default(int n) {
 }  // namespace
 
 // ===================================================================== C API
+// Second derivatives (deriv_order = 2) by composition of first derivatives:
+// with X' = shell X raised by one angular momentum quantum and every
+// primitive coefficient multiplied by 2 alpha (Cartesian), and X_ = X
+// lowered by one,
+//   d/dY_j d/dX_i (..x..) = d/dY_j (..X'(x+1_i)..) - x_i d/dY_j (..X_(x-1_i)..)
+// for every pair of centres (X, Y) (both first-derivative factors act at the
+// primitive level, so the 2 alpha of X' multiplies the one the inner
+// derivative brings when Y = X).  The 78 sets come in libint's order
+// (CartesianDerivIterator<4>(2): coordinate pairs c1 <= c2, row-major over
+// the 12 coordinates A_x..D_z), in the caller's shell order; pure shells
+// are transformed after the Cartesian composition.  Shells up to l = 2
+// (their raised copies reach l = 3).
+int compute_quartet_d2(const orc_basis* bs, const int* tgt, double precision, int method,
+                       Work& w, double* out) {
+  std::vector<int> l(12, 0), pure(12, 0), np(12, 0), off(12, 0), atom(12, 0);
+  std::vector<double> O(36, 0.0), al, co;
+  auto push = [&](int k, int src, int dl, bool scale) {
+    l[k] = bs->l[src] + dl;
+    pure[k] = dl == 0 ? bs->pure[src] : 0;
+    np[k] = bs->nprim[src];
+    off[k] = int(al.size());
+    for (int x = 0; x < 3; ++x) O[3 * k + x] = bs->O[3 * src + x];
+    for (int p = 0; p < np[k]; ++p) {
+      const double a = bs->alpha[bs->prim_off[src] + p], c = bs->coeff[bs->prim_off[src] + p];
+      al.push_back(a);
+      co.push_back(scale ? 2.0 * a * c : c);
+    }
+  };
+  int lx[4], n[4];
+  for (int X = 0; X < 4; ++X) {
+    lx[X] = bs->l[tgt[X]];
+    n[X] = bs->pure[tgt[X]] ? npure(lx[X]) : ncart(lx[X]);
+    push(X, tgt[X], 0, false);
+    push(4 + X, tgt[X], +1, true);
+    push(8 + X, tgt[X], lx[X] > 0 ? -1 : 0, false);
+  }
+  const orc_basis lb = {12, l.data(), pure.data(), np.data(), off.data(), atom.data(),
+                        O.data(), al.data(), co.data()};
+  const size_t nv = size_t(n[0]) * n[1] * n[2] * n[3];
+  {
+    std::vector<double> t0(nv);
+    const int q0[4] = {0, 1, 2, 3};
+    if (compute_quartet(&lb, q0, 0, precision, method, w, t0.data()) == 0) return 0;
+  }
+  std::vector<double> up[4], dn[4];
+  size_t su[4], sd[4];
+  for (int X = 0; X < 4; ++X) {
+    int q[4] = {0, 1, 2, 3};
+    int du[4] = {n[0], n[1], n[2], n[3]};
+    du[X] = ncart(lx[X] + 1);
+    su[X] = size_t(du[0]) * du[1] * du[2] * du[3];
+    up[X].assign(12 * su[X], 0.0);
+    q[X] = 4 + X;
+    compute_quartet(&lb, q, 1, precision, method, w, up[X].data());
+    if (lx[X] > 0) {
+      int dd[4] = {n[0], n[1], n[2], n[3]};
+      dd[X] = ncart(lx[X] - 1);
+      sd[X] = size_t(dd[0]) * dd[1] * dd[2] * dd[3];
+      dn[X].assign(12 * sd[X], 0.0);
+      q[X] = 8 + X;
+      compute_quartet(&lb, q, 1, precision, method, w, dn[X].data());
+    }
+  }
+  int s = 0;
+  for (int c1 = 0; c1 < 12; ++c1)
+    for (int c2 = c1; c2 < 12; ++c2, ++s) {
+      const int X = c1 / 3, i = c1 % 3, ys = c2;  // set of d/dY_j in the first-derivative output
+      int dc[4] = {n[0], n[1], n[2], n[3]};
+      dc[X] = ncart(lx[X]);
+      int du[4] = {n[0], n[1], n[2], n[3]}, dd[4] = {n[0], n[1], n[2], n[3]};
+      du[X] = ncart(lx[X] + 1);
+      dd[X] = lx[X] > 0 ? ncart(lx[X] - 1) : 0;
+      const double* U = up[X].data() + size_t(ys) * su[X];
+      const double* Dn = lx[X] > 0 ? dn[X].data() + size_t(ys) * sd[X] : nullptr;
+      std::vector<double> cart(size_t(dc[0]) * dc[1] * dc[2] * dc[3]);
+      int ix[4];
+      size_t o = 0;
+      for (ix[0] = 0; ix[0] < dc[0]; ++ix[0])
+        for (ix[1] = 0; ix[1] < dc[1]; ++ix[1])
+          for (ix[2] = 0; ix[2] < dc[2]; ++ix[2])
+            for (ix[3] = 0; ix[3] < dc[3]; ++ix[3], ++o) {
+              int e[3];
+              cart_exps(lx[X], ix[X], e);
+              int iu[4] = {ix[0], ix[1], ix[2], ix[3]};
+              int eu[3] = {e[0], e[1], e[2]};
+              ++eu[i];
+              iu[X] = cart_index(lx[X] + 1, eu[0], eu[1]);
+              double v = U[((size_t(iu[0]) * du[1] + iu[1]) * du[2] + iu[2]) * du[3] + iu[3]];
+              if (e[i] > 0) {
+                int id[4] = {ix[0], ix[1], ix[2], ix[3]};
+                int ed[3] = {e[0], e[1], e[2]};
+                --ed[i];
+                id[X] = cart_index(lx[X] - 1, ed[0], ed[1]);
+                v -= e[i] * Dn[((size_t(id[0]) * dd[1] + id[1]) * dd[2] + id[2]) * dd[3] + id[3]];
+              }
+              cart[o] = v;
+            }
+      double* dst = out + size_t(s) * nv;
+      if (!bs->pure[tgt[X]]) {
+        std::memcpy(dst, cart.data(), nv * sizeof(double));
+        continue;
+      }
+      // solid-harmonic transform of index X
+      const auto& M = sph_matrix(lx[X]);
+      size_t outer = 1, inner = 1;
+      for (int t = 0; t < X; ++t) outer *= dc[t];
+      for (int t = X + 1; t < 4; ++t) inner *= dc[t];
+      const int ncx = dc[X], npx = npure(lx[X]);
+      std::fill(dst, dst + nv, 0.0);
+      for (size_t a = 0; a < outer; ++a)
+        for (int p = 0; p < npx; ++p)
+          for (int c = 0; c < ncx; ++c) {
+            const double coef = M[size_t(p) * ncx + c];
+            if (coef == 0.0) continue;
+            const double* src = &cart[(a * ncx + c) * inner];
+            double* d = &dst[(a * npx + p) * inner];
+            for (size_t b = 0; b < inner; ++b) d[b] += coef * src[b];
+          }
+    }
+  return int(nv);
+}
+
 extern "C" {
 
 void orc_boys(double T, int mmax, double* F) { boys(T, mmax, F); }
@@ -764,9 +886,14 @@ int orc_shellpair_init(int l1, int nprim1, const double* alpha1,
 
 int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
                         int deriv, double precision, int method, double* out) {
-  if (deriv < 0 || deriv > 1) return -1;
+  if (deriv < 0 || deriv > 2) return -1;
   thread_local Work w;
   const int tgt[4] = {s1, s2, s3, s4};
+  if (deriv == 2) {
+    for (int k = 0; k < 4; ++k)
+      if (bs->l[tgt[k]] > 2) return -1;
+    return compute_quartet_d2(bs, tgt, precision, method, w, out);
+  }
   return compute_quartet(bs, tgt, deriv, precision, method, w, out);
 }
 
@@ -777,15 +904,18 @@ int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
 int orc_compute_batch(const orc_basis* bs, const int* quartets, int64_t n, int deriv,
                       double precision, int method, const int64_t* offsets, double* out,
                       int* is_null, int nthreads) {
-  if (deriv < 0 || deriv > 1 || n < 0) return -1;
+  if (deriv < 0 || deriv > 2 || n < 0) return -1;
   const int nt = nthreads_or_default(nthreads);
 #pragma omp parallel num_threads(nt)
   {
     Work w;
 #pragma omp for schedule(dynamic, 256)
     for (int64_t q = 0; q < n; ++q) {
-      const int r = compute_quartet(bs, quartets + 4 * q, deriv, precision, method, w,
-                                    out + offsets[q]);
+      const int r = deriv == 2
+                        ? compute_quartet_d2(bs, quartets + 4 * q, precision, method, w,
+                                             out + offsets[q])
+                        : compute_quartet(bs, quartets + 4 * q, deriv, precision, method, w,
+                                          out + offsets[q]);
       is_null[q] = r == 0 ? 1 : 0;
     }
   }

@@ -168,7 +168,7 @@ def compute_quartet(basis: OracleBasis, s1, s2, s3, s4, deriv=0,
     """Engine::compute(s1,s2,s3,s4): list of nsets arrays (n1,n2,n3,n4), or
     None when every primitive quartet was screened out."""
     n = [int(basis.nfunc[s]) for s in (s1, s2, s3, s4)]
-    nsets = 12 if deriv else 1
+    nsets = {0: 1, 1: 12, 2: 78}[deriv]
     out = np.zeros(nsets * int(np.prod(n)))
     r = _lib().orc_compute_quartet(ctypes.byref(basis._c), s1, s2, s3, s4, deriv,
                                    ctypes.c_double(precision), method,
@@ -261,6 +261,16 @@ def ref_lib():
     return lib
 
 
+def ref_deriv_order2(lib):
+    """(c1, c2) coordinate pairs (0..11, c1 <= c2) of libint's 78
+    second-derivative shell sets, from the reference's CartesianDerivIterator."""
+    c1 = np.zeros(78, np.int32)
+    c2 = np.zeros(78, np.int32)
+    n = lib.ref_deriv_order2(_ptr(c1, ctypes.c_int), _ptr(c2, ctypes.c_int))
+    assert n == 78
+    return c1, c2
+
+
 def ref_eri_shellset(lib, shells, deriv=0):
     """Brute-force shell set from the reference's eri.h.  shells: 4 tuples
     (l, pure, alpha, coeff_normalized, origin)."""
@@ -271,7 +281,7 @@ def ref_eri_shellset(lib, shells, deriv=0):
     coeff = np.concatenate([np.asarray(s[3], float) for s in shells])
     O = np.concatenate([np.asarray(s[4], float) for s in shells])
     n = [(2 * s[0] + 1) if s[1] else (s[0] + 1) * (s[0] + 2) // 2 for s in shells]
-    nsets = 12 if deriv else 1
+    nsets = {0: 1, 1: 12, 2: 78}[deriv]
     out = np.zeros(nsets * int(np.prod(n)))
     lib.ref_eri_shellset(_ptr(l, ctypes.c_int), _ptr(pure, ctypes.c_int),
                          _ptr(nprim, ctypes.c_int), _ptr(alpha, ctypes.c_double),

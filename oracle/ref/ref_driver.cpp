@@ -132,6 +132,28 @@ int ref_deriv_order1(int* coord_of_set) {
   return di;
 }
 
+// Order of the 78 second-derivative shell sets (CartesianDerivIterator<4>(2)):
+// for each set, the two differentiated coordinates c1 <= c2 (0..11).
+int ref_deriv_order2(int* c1, int* c2) {
+  libint2::CartesianDerivIterator<4> diter(2);
+  int di = 0;
+  bool last = false;
+  do {
+    const auto& v = *diter;
+    int a = -1, b = -1;
+    for (int c = 0; c < 12; ++c) {
+      if (v[c] == 2) a = b = c;
+      if (v[c] == 1) (a < 0 ? a : b) = c;
+    }
+    c1[di] = a;
+    c2[di] = b;
+    ++di;
+    last = diter.last();
+    if (!last) diter.next();
+  } while (!last);
+  return di;
+}
+
 // Brute-force contracted shell set from src/bin/test_eri/eri.h:121-468, with
 // the contraction loop of tests/unit/test-2body.cc:246-289 and the
 // Cartesian->solid-harmonic steps of engine.impl.h:1965-1985 (reference
@@ -147,7 +169,7 @@ int ref_eri_shellset(const int* l, const int* pure, const int* nprim,
                             coeff_flat + off, O + 3 * i, false));
     off += nprim[i];
   }
-  const int nderiv = deriv == 0 ? 1 : 12;
+  const int nderiv = deriv == 0 ? 1 : (deriv == 1 ? 12 : 78);
   size_t ncart = 1, npure = 1;
   for (int i = 0; i < 4; ++i) {
     ncart *= sh[i].cartesian_size();

@@ -85,6 +85,17 @@ int main(int argc, char** argv) {
     const auto& r2 = e2.compute(obs[t[0]], obs[t[1]]);
     for (size_t i = 0; i < obs[t[0]].size() * obs[t[1]].size(); ++i) put(r2[0][i]);
   }
+  // second derivatives: compute2<coulomb, xx_xx, 2>, 78 sets (shells up to d)
+  libint2::Engine d2(libint2::Operator::coulomb, obs.max_nprim(), 2, 2);
+  const size_t q2[][4] = {{5, 3, 8, 0}, {3, 0, 1, 9}};
+  for (const auto& q : q2) {
+    const auto& r = d2.compute2<libint2::Operator::coulomb, libint2::BraKet::xx_xx, 2>(
+        obs[q[0]], obs[q[1]], obs[q[2]], obs[q[3]]);
+    const size_t n = obs[q[0]].size() * obs[q[1]].size() * obs[q[2]].size() * obs[q[3]].size();
+    put(double(d2.nshellsets()));
+    for (unsigned s = 0; s < d2.nshellsets(); ++s)
+      for (size_t i = 0; i < n; ++i) put(r[s][i]);
+  }
   // range-separated operator: erfc(omega r)/r with omega as the params argument
   libint2::Engine ec(libint2::Operator::erfc_coulomb, obs.max_nprim(), obs.max_l(), 0,
                      std::numeric_limits<double>::epsilon(), 0.3);

@@ -17,6 +17,9 @@ Outputs (numpy .npz, committed):
   eri3c.npz       brute-force 3-centre (a 1|c d) and 2-centre (a 1|c 1) shell
                   sets, d0 and d1 (1 = Shell::unit(), exponent 0), same layout
                   as eri.npz plus the braket rank
+  eri_d2.npz      brute-force second-derivative (deriv_order 2) shell sets, 78
+                  per quartet in libint's order (CartesianDerivIterator<4>(2)),
+                  shells up to d, with that order as coordinate pairs
   hf.npz          system-level golden values of the reference's Hartree-Fock
                   tests, read as text: the rotated-water geometry
                   (tests/hartree-fock/h2o_rotated.xyz) with the aug-cc-pVDZ
@@ -26,6 +29,7 @@ Outputs (numpy .npz, committed):
 
     python tests/golden/make_golden.py --hf-only    # hf.npz alone
     python tests/golden/make_golden.py --eri3c-only # eri3c.npz alone
+    python tests/golden/make_golden.py --d2-only    # eri_d2.npz alone
 """
 import ctypes
 import itertools
@@ -215,6 +219,49 @@ def eri3c_fixtures():
                         offset=np.array(recs["offset"], np.int64), values=np.concatenate(vals))
 
 
+def eri_d2_fixtures():
+    """Second-derivative shell sets from the reference's brute-force eri.h
+    (any derivative order, via CartesianDerivIterator<4>(2))."""
+    oracle.build_ref()
+    ref = oracle.ref_lib()
+    assert ref is not None, "reference build missing"
+    rng = np.random.default_rng(20240603)
+    c1, c2 = oracle.ref_deriv_order2(ref)
+    cases = [(0, 0, 0, 0), (1, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 0), (0, 0, 0, 1), (1, 1, 0, 0),
+             (1, 0, 1, 0), (0, 1, 0, 1), (1, 1, 1, 1), (2, 0, 0, 0), (0, 2, 1, 0), (2, 1, 0, 1),
+             (1, 0, 2, 1), (2, 2, 0, 0), (0, 0, 2, 2), (2, 1, 1, 2)]
+    recs = {"l": [], "pure": [], "nprim": [], "alpha": [], "coeff": [], "O": [], "offset": []}
+    off, vals = 0, []
+    for t, ls in enumerate(cases):
+        shells = []
+        for k, l in enumerate(ls):
+            n = 2 if (l < 2 and sum(ls) <= 3) else 1
+            a = np.sort(rng.uniform(0.2, 3.0, n))[::-1].copy()
+            c = rng.uniform(0.3, 1.0, n)
+            cn, _ = oracle.shell_normalize(l, a, c)
+            shells.append((l, (1 if l > 1 else 0) if t % 2 else 0, a, cn, rng.uniform(-1.0, 1.0, 3)))
+        r = oracle.ref_eri_shellset(ref, shells, 2)
+        v = np.concatenate([x.reshape(-1) for x in r])
+        recs["l"].append(ls); recs["pure"].append([s[1] for s in shells])
+        recs["nprim"].append([len(s[2]) for s in shells])
+        recs["alpha"].append(np.concatenate([s[2] for s in shells]))
+        recs["coeff"].append(np.concatenate([s[3] for s in shells]))
+        recs["O"].append(np.concatenate([s[4] for s in shells]))
+        recs["offset"].append(off)
+        vals.append(v)
+        off += v.size
+    maxp = max(len(a) for a in recs["alpha"])
+    alpha = np.zeros((len(cases), maxp)); coeff = np.zeros((len(cases), maxp))
+    for i in range(len(cases)):
+        alpha[i, :len(recs["alpha"][i])] = recs["alpha"][i]
+        coeff[i, :len(recs["coeff"][i])] = recs["coeff"][i]
+    np.savez_compressed(os.path.join(HERE, "eri_d2.npz"), l=np.array(recs["l"], np.int32),
+                        pure=np.array(recs["pure"], np.int32),
+                        nprim=np.array(recs["nprim"], np.int32), alpha=alpha, coeff=coeff,
+                        O=np.array(recs["O"]), offset=np.array(recs["offset"], np.int64),
+                        values=np.concatenate(vals), c1=c1, c2=c2)
+
+
 REFERENCE = "/root/reference"
 SYMBOL_Z = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10}
 
@@ -249,6 +296,8 @@ def hf_fixtures(root=REFERENCE):
     etol = _scalar_after(val, "etol")
     F2 = _floats_after(val, "F2ref")
     F2tol = _scalar_after(val, "F2tol")
+    H2 = _floats_after(val, "H2ref")
+    H2tol = _scalar_after(val, "H2tol")
     with open(os.path.join(root, "python", "tests", "test_hf.py")) as f:
         py = f.read()
     m = re.search(r"h2o\s*=\s*\[(.*?)\n\]", py, re.S)
@@ -260,6 +309,7 @@ def hf_fixtures(root=REFERENCE):
              rot_Z=np.array(Z, np.int32), rot_xyz_angstrom=np.array(xyz),
              rot_basis="aug-cc-pVDZ", rot_energy=eref, rot_energy_tol=etol,
              rot_F2=np.array(F2).reshape(nat, 3), rot_F2_tol=F2tol,
+             rot_H2_upper=np.array(H2), rot_H2_tol=H2tol,
              h2o631_Z=np.array(Z631, np.int32), h2o631_xyz_bohr=np.array(xyz631),
              h2o631_basis="6-31G", h2o631_energy=e631, h2o631_places=7)
 
@@ -268,7 +318,10 @@ if __name__ == "__main__" and "--hf-only" in sys.argv:
     hf_fixtures()
 elif __name__ == "__main__" and "--eri3c-only" in sys.argv:
     eri3c_fixtures()
+elif __name__ == "__main__" and "--d2-only" in sys.argv:
+    eri_d2_fixtures()
 elif __name__ == "__main__":
     hf_fixtures()
     eri3c_fixtures()
+    eri_d2_fixtures()
     main()

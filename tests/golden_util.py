@@ -32,3 +32,15 @@ def eri3c_cases():
         yield (g["l"][i], g["pure"][i], g["nprim"][i], g["alpha"][i][:n], g["coeff"][i][:n],
                g["O"][i], int(g["deriv"][i]), int(g["rank"][i]),
                g["values"][offs[i]:offs[i + 1]])
+
+
+def eri_d2_cases():
+    """Yields (l[4], pure[4], nprim[4], alpha, coeff, O[12], values[78*n]) of
+    the second-derivative fixtures; load("eri_d2.npz")["c1"/"c2"] hold the
+    reference's set order."""
+    g = load("eri_d2.npz")
+    offs = list(g["offset"]) + [len(g["values"])]
+    for i in range(len(g["l"])):
+        n = int(g["nprim"][i].sum())
+        yield (g["l"][i], g["pure"][i], g["nprim"][i], g["alpha"][i][:n], g["coeff"][i][:n],
+               g["O"][i], g["values"][offs[i]:offs[i + 1]])

@@ -81,6 +81,12 @@ def test_cpp_engine_facade(lgx, oracle_mod, tmp_path):
         r2 = oracle_mod.compute_quartet(obu, a, u, c, u)[0].reshape(-1)
         assert np.max(np.abs(vals[pos:pos + r2.size] - r2)) < 1e-12
         pos += r2.size
+    for q in [(5, 3, 8, 0), (3, 0, 1, 9)]:
+        assert vals[pos] == 78.0
+        pos += 1
+        ref = np.concatenate([x.reshape(-1) for x in oracle_mod.compute_quartet(ob, *q, deriv=2)])
+        assert np.max(np.abs(vals[pos:pos + ref.size] - ref)) < 1e-12
+        pos += ref.size
     oracle_mod.set_operator(2, 0.3)
     try:
         for q in [(5, 3, 8, 0), (3, 5, 5, 9), (0, 14, 5, 3)]:

@@ -27,3 +27,25 @@ def test_engine_vs_reference_bruteforce(lgx):
         assert err < 1e-12, (tuple(l), deriv, err)
     print("worst", worst)
     ctx.close()
+
+
+def test_engine_deriv2_vs_reference_bruteforce(lgx):
+    # deriv_order 2 (78 sets per quartet, shells up to d) through Engine
+    from golden_util import eri_d2_cases
+    worst = 0.0
+    for l, pure, nprim, alpha, coeff, O, vals in eri_d2_cases():
+        shells, off = [], 0
+        for k in range(4):
+            n = int(nprim[k])
+            shells.append(lgx.Shell.from_normalized(int(l[k]), alpha[off:off + n],
+                                                    coeff[off:off + n], O[3 * k:3 * k + 3],
+                                                    bool(pure[k])))
+            off += n
+        eng = lgx.Engine(lgx.Operator.coulomb, 4, 2, 2, precision=0.0)
+        assert eng.nshellsets() == 78
+        r = eng.compute(*shells)
+        got = np.concatenate([x.reshape(-1) for x in r])
+        err = float(np.max(np.abs(got - vals)))
+        worst = max(worst, err)
+        assert err < 1e-12, (tuple(l), err)
+    print("worst", worst)

@@ -53,6 +53,19 @@ def test_eri3c_2c_shellsets_vs_reference_bruteforce(oracle_mod):
         assert err < 1e-12, (tuple(l), rank, deriv, err)
 
 
+def test_deriv2_shellsets_vs_reference_bruteforce(oracle_mod):
+    # deriv_order 2: 78 sets per quartet, order = CartesianDerivIterator<4>(2)
+    from golden_util import eri_d2_cases
+    g = load("eri_d2.npz")
+    assert [(int(a), int(b)) for a, b in zip(g["c1"], g["c2"])] == \
+        [(c1, c2) for c1 in range(12) for c2 in range(c1, 12)]
+    for l, pure, nprim, alpha, coeff, O, vals in eri_d2_cases():
+        ob = oracle_mod.OracleBasis(l, pure, nprim, O, alpha, coeff)
+        r = oracle_mod.compute_quartet(ob, 0, 1, 2, 3, 2, precision=0.0)
+        got = np.concatenate([x.reshape(-1) for x in r])
+        assert np.max(np.abs(got - vals)) < 1e-12, tuple(l)
+
+
 def test_derivative_order_and_map(oracle_mod):
     g = load("derivmap.npz")
     # sets ordered A_x, A_y, A_z, B_x, ..., D_z
