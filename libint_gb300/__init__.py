@@ -325,6 +325,8 @@ class Context:
 
     def compute_batch(self, quartets, deriv=0, mode=_lgx.LGX_FP64, mixed_thresh=1e-4):
         q = np.ascontiguousarray(quartets, dtype=np.int32).reshape(-1, 4)
+        if q.size and (q.min() < 0 or q.max() >= len(self.basis)):
+            raise LgxError(_lgx.LGX_ERR_INVALID_ARG, "quartet shell index out of range")
         sizes = np.array([s.size() for s in self.basis], np.int64)
         nv = sizes[q[:, 0]] * sizes[q[:, 1]] * sizes[q[:, 2]] * sizes[q[:, 3]] * (12 if deriv else 1)
         offs = np.zeros(len(q), np.int64)
