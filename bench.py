@@ -437,6 +437,86 @@ def run_gpu(args):
     return 0
 
 
+def _prim_inputs(rng, ls, depth, deriv, dtype):
+    """Caller-side Libint_t prefactors of random raw shells (what a libint
+    caller computes before libint2_build_eri*), Boys values from scipy."""
+    from scipy.special import gamma, gammainc
+    sh = []
+    for l in ls:
+        a = np.sort(rng.uniform(0.3, 3.0, depth))[::-1].copy()
+        sh.append((l, a, rng.uniform(0.4, 1.2, depth), rng.uniform(-1.2, 1.2, 3)))
+    (_, a1s, c1s, A), (_, a2s, c2s, B), (_, a3s, c3s, C), (_, a4s, c4s, D) = sh
+    mmax = sum(ls) + deriv
+    m = np.arange(mmax + 1) + 0.5
+    recs = []
+    for a1, c1 in zip(a1s, c1s):
+        for a2, c2 in zip(a2s, c2s):
+            for a3, c3 in zip(a3s, c3s):
+                for a4, c4 in zip(a4s, c4s):
+                    z, e = a1 + a2, a3 + a4
+                    P, Q = (a1 * A + a2 * B) / z, (a3 * C + a4 * D) / e
+                    rho = z * e / (z + e)
+                    W = (z * P + e * Q) / (z + e)
+                    T = rho * np.dot(P - Q, P - Q)
+                    F = (gammainc(m, T) * gamma(m) / (2 * T ** m) if T > 1e-12
+                         else 1.0 / (2 * m))
+                    pfac = (2 * np.pi ** 2.5 * np.exp(-a1 * a2 / z * np.dot(A - B, A - B))
+                            * np.exp(-a3 * a4 / e * np.dot(C - D, C - D))
+                            / (z * e * np.sqrt(z + e)) * c1 * c2 * c3 * c4)
+                    r = np.zeros((), dtype)
+                    r["PA"], r["QC"], r["WP"], r["WQ"] = P - A, Q - C, W - P, W - Q
+                    r["oo2z"], r["oo2e"], r["oo2ze"] = 0.5 / z, 0.5 / e, 0.5 / (z + e)
+                    r["roz"], r["roe"] = rho / z, rho / e
+                    r["two_alpha"] = [2 * a1, 2 * a2, 2 * a3, 2 * a4]
+                    ss = np.zeros(dtype["ss"].shape)
+                    ss[:mmax + 1] = pfac * F
+                    r["ss"] = ss
+                    recs.append(r)
+    return sh, np.array(recs, dtype=dtype), A - B, C - D
+
+
+def run_primitive_api(args):
+    """--primitive-api: latency of the generated-library entry
+    (lgx_compute_primitive_set, behind libint2_build_eri*): one synchronous
+    call per contracted shell set, host records in, host sets out, through
+    the Python binding; the oracle's contracted quartet of the same shells
+    (one host thread) beside it."""
+    import libint_gb300 as lg
+    from oracle import oracle
+    oracle.build()
+    ctx = lg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    rng = np.random.default_rng(2024)
+    rows = []
+    for ls, depth, deriv in (((1, 1, 1, 1), 3, 0), ((2, 2, 2, 2), 1, 0), ((3, 3, 3, 3), 1, 0),
+                             ((2, 1, 2, 1), 2, 1), ((1, 1, 1, 1), 1, 2)):
+        sh, prims, AB, CD = _prim_inputs(rng, ls, depth, deriv, lg._lgx.PRIM_DTYPE)
+        n = 200
+        for _ in range(5):
+            ctx.compute_primitive_set(ls, prims, AB, CD, deriv)
+        t0 = time.perf_counter()
+        for _ in range(n):
+            out = ctx.compute_primitive_set(ls, prims, AB, CD, deriv)
+        t_gpu = (time.perf_counter() - t0) / n
+        ob = oracle.OracleBasis(np.array(ls, np.int32), np.zeros(4, np.int32),
+                                np.full(4, depth, np.int32), np.concatenate([s[3] for s in sh]),
+                                np.concatenate([s[1] for s in sh]),
+                                np.concatenate([s[2] for s in sh]))
+        t0 = time.perf_counter()
+        for _ in range(n):
+            oracle.compute_quartet(ob, 0, 1, 2, 3, deriv=deriv, precision=0.0)
+        t_cpu = (time.perf_counter() - t0) / n
+        nint = sum(x.size for x in out)
+        rows.append({"class": "(%d%d|%d%d)" % ls, "deriv": deriv, "prim_quartets": len(prims),
+                     "integrals": nint, "us_per_call": 1e6 * t_gpu,
+                     "eri_per_s": nint / t_gpu, "oracle_us_per_call": 1e6 * t_cpu})
+    ctx.close()
+    print(json.dumps({"metric": "generated-library entry latency (libint2_build_eri*)",
+                      "unit": "us/call", "data": "synthetic", "calls": 200,
+                      "note": "synchronous: host records -> GPU -> host sets, Python binding",
+                      "classes": rows}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -447,7 +527,11 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-budget", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--primitive-api", action="store_true",
+                    help="time the generated-library entry (libint2_build_eri*) instead")
     args = ap.parse_args()
+    if args.primitive_api:
+        return run_primitive_api(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

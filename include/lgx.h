@@ -114,6 +114,51 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4],
                                 double* out, size_t out_capacity, int* nsets,
                                 int* nvalues, int* is_null);
 
+/* ------------------------------------ generated-library entry (Libint_t) */
+
+/* One primitive quartet of caller-computed VRR inputs, the per-primitive
+ * prefactors a libint caller writes into Libint_t before
+ * libint2_build_eri* (engine.impl.h:1389-1757; prep_libint2.h of the
+ * reference's test_eri), for shells 1..4 = A, B, C, D in caller order with
+ * primitive exponents a1..a4, zeta = a1 + a2, eta = a3 + a4,
+ * rho = zeta eta / (zeta + eta), P, Q the bra / ket centres and
+ * W = (zeta P + eta Q) / (zeta + eta). */
+#define LGX_PRIM_MAX_M 15
+typedef struct lgx_prim_quartet {
+  double PA[3];        /* P - A                                              */
+  double QC[3];        /* Q - C                                              */
+  double WP[3];        /* W - P                                              */
+  double WQ[3];        /* W - Q                                              */
+  double oo2z;         /* 1 / (2 zeta)                                       */
+  double oo2e;         /* 1 / (2 eta)                                        */
+  double oo2ze;        /* 1 / (2 (zeta + eta))                               */
+  double roz;          /* rho / zeta                                         */
+  double roe;          /* rho / eta                                          */
+  double two_alpha[4]; /* 2 a1 .. 2 a4 (read for derivatives only)           */
+  /* (00|00)^(m) = pfac F_m(rho |PQ|^2), m = 0..l1+l2+l3+l4+deriv, with pfac
+   * = 2 pi^{5/2} K_AB K_CD / (zeta eta sqrt(zeta + eta)) times the four
+   * contraction coefficients (libint's LIBINT_T_SS_EREP_SS(m)) */
+  double ss[LGX_PRIM_MAX_M + 1];
+} lgx_prim_quartet;
+
+/* The contracted Cartesian shell set (l1 l2|l3 l4) over `nprim` primitive
+ * quartets (libint2_build_eri / libint2_build_eri1 with
+ * Libint_t::contrdepth = nprim, dg.cc:1177-1189), computed on the GPU with
+ * the class's VRR / HRR programs.  AB = A - B, CD = C - D.  deriv 0: one
+ * set; deriv 1: 12 sets ordered A_x..D_z (all four centres; centre C by
+ * translational invariance as libint's generated code does).  Sets are
+ * row-major ncart(l1) ncart(l2) ncart(l3) ncart(l4) in the caller's shell
+ * order and Cartesian (no solid-harmonic transform, no renormalisation:
+ * the caller's (00|00)^(m) carry it), written to the HOST buffer `out`.
+ * deriv 2 (libint2_build_eri2, shells up to l = 2): the 78 sets in
+ * libint's CartesianDerivIterator order, composed from the first-derivative
+ * sets of the quartets with one shell raised (its primitives weighted by
+ * 2 a_X) and lowered, which requires ss[] up to m = l1+..+l4+2. */
+lgx_status lgx_compute_primitive_set(lgx_context* ctx, int l1, int l2, int l3, int l4,
+                                     int deriv, const lgx_prim_quartet* prims, int nprim,
+                                     const double AB[3], const double CD[3], double* out,
+                                     size_t out_capacity, int* nsets, int* nvalues);
+
 /* ----------------------------------------------------------- basis state */
 
 /* Uploads a basis (a libint2::BasisSet, basis.h.in:134-182, flattened):

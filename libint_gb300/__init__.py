@@ -305,6 +305,29 @@ class Context:
         shape = tuple(s.size() for s in shells)
         return [out[i * nv:(i + 1) * nv].reshape(shape) for i in range(ns.value)]
 
+    def compute_primitive_set(self, ls, prims, AB, CD, deriv=0):
+        """Contracted Cartesian shell set(s) (l1 l2|l3 l4) from caller-computed
+        primitive quartets (libint2_build_eri / _eri1 / _eri2 with Libint_t
+        prefactors): `prims` is an array of dtype PRIM_DTYPE, AB = A - B,
+        CD = C - D.  Returns the 1 / 12 / 78 sets in the caller's shell
+        order, each shaped (ncart(l1), ncart(l2), ncart(l3), ncart(l4))."""
+        ls = [int(x) for x in ls]
+        prims = np.ascontiguousarray(prims, dtype=_lgx.PRIM_DTYPE)
+        nsets = {0: 1, 1: 12, 2: 78}[int(deriv)]
+        shape = tuple((l + 1) * (l + 2) // 2 for l in ls)
+        nv = int(np.prod(shape))
+        out = np.zeros(nsets * nv)
+        AB = np.ascontiguousarray(AB, dtype=float)
+        CD = np.ascontiguousarray(CD, dtype=float)
+        ns, nvals = ctypes.c_int(), ctypes.c_int()
+        st = self._lib.lgx_compute_primitive_set(
+            self._h, ls[0], ls[1], ls[2], ls[3], int(deriv),
+            prims.ctypes.data_as(ctypes.POINTER(_lgx.LgxPrimQuartet)), len(prims),
+            _lgx.ptr(AB), _lgx.ptr(CD), _lgx.ptr(out), out.size, ctypes.byref(ns),
+            ctypes.byref(nvals))
+        self._check(st, "lgx_compute_primitive_set")
+        return [out[i * nv:(i + 1) * nv].reshape(shape) for i in range(ns.value)]
+
     # ------------------------------------------------------------- basis
     def set_basis(self, basis: BasisSet):
         I = ctypes.c_int32

@@ -57,6 +57,32 @@ class LgxLaunchStats(ctypes.Structure):
                 ("ms", ctypes.c_double)]
 
 
+LGX_PRIM_MAX_M = 15
+
+
+class LgxPrimQuartet(ctypes.Structure):
+    """lgx_prim_quartet: one primitive quartet of caller-computed VRR inputs."""
+    _fields_ = [("PA", ctypes.c_double * 3), ("QC", ctypes.c_double * 3),
+                ("WP", ctypes.c_double * 3), ("WQ", ctypes.c_double * 3),
+                ("oo2z", ctypes.c_double), ("oo2e", ctypes.c_double),
+                ("oo2ze", ctypes.c_double), ("roz", ctypes.c_double), ("roe", ctypes.c_double),
+                ("two_alpha", ctypes.c_double * 4),
+                ("ss", ctypes.c_double * (LGX_PRIM_MAX_M + 1))]
+
+
+# numpy view of an lgx_prim_quartet array (same field order, all doubles)
+PRIM_DTYPE = None
+try:
+    import numpy as _np
+    PRIM_DTYPE = _np.dtype([("PA", "f8", 3), ("QC", "f8", 3), ("WP", "f8", 3), ("WQ", "f8", 3),
+                            ("oo2z", "f8"), ("oo2e", "f8"), ("oo2ze", "f8"), ("roz", "f8"),
+                            ("roe", "f8"), ("two_alpha", "f8", 4),
+                            ("ss", "f8", LGX_PRIM_MAX_M + 1)])
+    assert PRIM_DTYPE.itemsize == ctypes.sizeof(LgxPrimQuartet)
+except ImportError:  # numpy is optional for the bare ctypes binding
+    pass
+
+
 # Every symbol include/lgx.h declares, with its ctypes signature.
 SIGNATURES = {
     "lgx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
@@ -70,6 +96,12 @@ SIGNATURES = {
                                             ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int)]),
+    "lgx_compute_primitive_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(LgxPrimQuartet), ctypes.c_int,
+                                                 _dp, _dp, _dp, ctypes.c_size_t,
+                                                 ctypes.POINTER(ctypes.c_int),
+                                                 ctypes.POINTER(ctypes.c_int)]),
     "lgx_set_basis": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip, _ip,
                                      _dp, _dp, _dp]),
     "lgx_basis_nbf": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),

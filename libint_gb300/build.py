@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(PKG_DIR, "liblgx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu"]
-CXX_SOURCES = ["lgx_program.cpp", "lgx_host.cpp"]
+CXX_SOURCES = ["lgx_program.cpp", "lgx_host.cpp", "lgx_libint_c.cpp"]
 
 
 def _nvcc() -> str:

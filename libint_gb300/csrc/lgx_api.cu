@@ -28,6 +28,7 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
 size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
+cudaError_t launch_prim_set(const PrimSetArgs& a, size_t smem, cudaStream_t st);
 cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
                       long long work, int nsm, cudaStream_t st);
 bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
@@ -246,6 +247,7 @@ struct lgx_context {
   DBuf gscratch, counter, errflag, primcount;
   DBuf items, out, isnull;
   DBuf Jacc, Kacc, Dd, Jd, Kd, gJ, gK;
+  DBuf prim_rows, prim_slots;  // lgx_compute_primitive_set
   PinnedBuf pin_in, pin_out;
   BinCache bins;
   std::mutex mu;
@@ -1436,6 +1438,76 @@ void cart_exp(int l, int c, int* e) {
   e[2] = l - e[0] - e[1];
 }
 
+// The 78 second-derivative sets (libint's CartesianDerivIterator<4>(2)
+// order) from the first-derivative sets d1 of the quartets with shell X
+// raised (12 sets of su[X] values at offu[X]) and lowered (sd[X] values at
+// offd[X]; l = 0 has none):
+//   d/dY_j d/dX_i (..x..) = d/dY_j (..X'(x+1_i)..) - x_i d/dY_j (..X_(x-1_i)..)
+// composed in Cartesian components, then transformed to solid harmonics
+// for the pure shell X.  n[] are the caller's set dimensions, nv their
+// product; the raised / lowered shells are Cartesian.
+void compose_deriv2(const int lx[4], const int n[4], const int pure[4], const double* d1,
+                    const int64_t offu[4], const int64_t offd[4], const size_t su[4],
+                    const size_t sd[4], size_t nv, double* out) {
+  std::vector<double> cart;
+  int set = 0;
+  for (int c1 = 0; c1 < 12; ++c1)
+    for (int c2 = c1; c2 < 12; ++c2, ++set) {
+      const int X = c1 / 3, i = c1 % 3;
+      int dc[4] = {n[0], n[1], n[2], n[3]}, du[4] = {n[0], n[1], n[2], n[3]},
+          dd[4] = {n[0], n[1], n[2], n[3]};
+      dc[X] = ncart(lx[X]);
+      du[X] = ncart(lx[X] + 1);
+      dd[X] = lx[X] > 0 ? ncart(lx[X] - 1) : 0;
+      const double* U = d1 + offu[X] + size_t(c2) * su[X];
+      const double* Dn = lx[X] > 0 ? d1 + offd[X] + size_t(c2) * sd[X] : nullptr;
+      cart.assign(size_t(dc[0]) * dc[1] * dc[2] * dc[3], 0.0);
+      int ix[4];
+      size_t o = 0;
+      for (ix[0] = 0; ix[0] < dc[0]; ++ix[0])
+        for (ix[1] = 0; ix[1] < dc[1]; ++ix[1])
+          for (ix[2] = 0; ix[2] < dc[2]; ++ix[2])
+            for (ix[3] = 0; ix[3] < dc[3]; ++ix[3], ++o) {
+              int e[3];
+              cart_exp(lx[X], ix[X], e);
+              int iu[4] = {ix[0], ix[1], ix[2], ix[3]};
+              int eu[3] = {e[0], e[1], e[2]};
+              ++eu[i];
+              iu[X] = cart_idx(lx[X] + 1, eu[0], eu[1]);
+              double v = U[((size_t(iu[0]) * du[1] + iu[1]) * du[2] + iu[2]) * du[3] + iu[3]];
+              if (e[i] > 0) {
+                int id[4] = {ix[0], ix[1], ix[2], ix[3]};
+                int ed[3] = {e[0], e[1], e[2]};
+                --ed[i];
+                id[X] = cart_idx(lx[X] - 1, ed[0], ed[1]);
+                v -= e[i] * Dn[((size_t(id[0]) * dd[1] + id[1]) * dd[2] + id[2]) * dd[3] + id[3]];
+              }
+              cart[o] = v;
+            }
+      double* dst = out + size_t(set) * nv;
+      if (!pure[X]) {
+        std::memcpy(dst, cart.data(), nv * sizeof(double));
+        continue;
+      }
+      size_t outer = 1, inner = 1;
+      for (int t = 0; t < X; ++t) outer *= size_t(dc[t]);
+      for (int t = X + 1; t < 4; ++t) inner *= size_t(dc[t]);
+      const int ncx = dc[X], npx = 2 * lx[X] + 1;
+      std::fill(dst, dst + nv, 0.0);
+      for (size_t a = 0; a < outer; ++a)
+        for (int p = 0; p < npx; ++p)
+          for (int c = 0; c < ncx; ++c) {
+            int e[3];
+            cart_exp(lx[X], c, e);
+            const double coef = solid_coeff(lx[X], p - lx[X], e[0], e[1], e[2]);
+            if (coef == 0.0) continue;
+            const double* src = &cart[(a * ncx + c) * inner];
+            double* d = &dst[(a * npx + p) * inner];
+            for (size_t b = 0; b < inner; ++b) d[b] += coef * src[b];
+          }
+    }
+}
+
 // deriv_order = 2 (Engine::compute2<coulomb, xx_xx, 2>): the 78 second-
 // derivative shell sets, composed from first-derivative sets that the GPU
 // computes in one batched launch.  With X' = shell X raised by one angular
@@ -1534,63 +1606,181 @@ lgx_status shellset_deriv2(lgx_context* ctx, const lgx_shell shells[4], double p
   for (int v : nul) all_null = all_null && v != 0;
   *is_null = all_null ? 1 : 0;
   if (all_null) return LGX_OK;
-  std::vector<double> cart;
-  int set = 0;
-  for (int c1 = 0; c1 < 12; ++c1)
-    for (int c2 = c1; c2 < 12; ++c2, ++set) {
-      const int X = c1 / 3, i = c1 % 3;
-      int dc[4] = {n[0], n[1], n[2], n[3]}, du[4] = {n[0], n[1], n[2], n[3]},
-          dd[4] = {n[0], n[1], n[2], n[3]};
-      dc[X] = ncart(lx[X]);
-      du[X] = ncart(lx[X] + 1);
-      dd[X] = lx[X] > 0 ? ncart(lx[X] - 1) : 0;
-      const double* U = d1.data() + offu[X] + size_t(c2) * su[X];
-      const double* Dn = lx[X] > 0 ? d1.data() + offd[X] + size_t(c2) * sd[X] : nullptr;
-      cart.assign(size_t(dc[0]) * dc[1] * dc[2] * dc[3], 0.0);
-      int ix[4];
-      size_t o = 0;
-      for (ix[0] = 0; ix[0] < dc[0]; ++ix[0])
-        for (ix[1] = 0; ix[1] < dc[1]; ++ix[1])
-          for (ix[2] = 0; ix[2] < dc[2]; ++ix[2])
-            for (ix[3] = 0; ix[3] < dc[3]; ++ix[3], ++o) {
-              int e[3];
-              cart_exp(lx[X], ix[X], e);
-              int iu[4] = {ix[0], ix[1], ix[2], ix[3]};
-              int eu[3] = {e[0], e[1], e[2]};
-              ++eu[i];
-              iu[X] = cart_idx(lx[X] + 1, eu[0], eu[1]);
-              double v = U[((size_t(iu[0]) * du[1] + iu[1]) * du[2] + iu[2]) * du[3] + iu[3]];
-              if (e[i] > 0) {
-                int id[4] = {ix[0], ix[1], ix[2], ix[3]};
-                int ed[3] = {e[0], e[1], e[2]};
-                --ed[i];
-                id[X] = cart_idx(lx[X] - 1, ed[0], ed[1]);
-                v -= e[i] * Dn[((size_t(id[0]) * dd[1] + id[1]) * dd[2] + id[2]) * dd[3] + id[3]];
-              }
-              cart[o] = v;
-            }
-      double* dst = out + size_t(set) * nv;
-      if (!shells[X].pure) {
-        std::memcpy(dst, cart.data(), nv * sizeof(double));
-        continue;
-      }
-      size_t outer = 1, inner = 1;
-      for (int t = 0; t < X; ++t) outer *= size_t(dc[t]);
-      for (int t = X + 1; t < 4; ++t) inner *= size_t(dc[t]);
-      const int ncx = dc[X], npx = 2 * lx[X] + 1;
-      std::fill(dst, dst + nv, 0.0);
-      for (size_t a = 0; a < outer; ++a)
-        for (int p = 0; p < npx; ++p)
-          for (int c = 0; c < ncx; ++c) {
-            int e[3];
-            cart_exp(lx[X], c, e);
-            const double coef = solid_coeff(lx[X], p - lx[X], e[0], e[1], e[2]);
-            if (coef == 0.0) continue;
-            const double* src = &cart[(a * ncx + c) * inner];
-            double* d = &dst[(a * npx + p) * inner];
-            for (size_t b = 0; b < inner; ++b) d[b] += coef * src[b];
-          }
+  int pure4[4];
+  for (int k = 0; k < 4; ++k) pure4[k] = shells[k].pure ? 1 : 0;
+  compose_deriv2(lx, n, pure4, d1.data(), offu, offd, su, sd, nv, out);
+  return LGX_OK;
+}
+
+
+// Caller position of canonical shell k for shells of angular momenta l[]
+// (la >= lb, lc >= ld, la + lb <= lc + ld; the same rule as canonicalize).
+void canonical_perm(const int l[4], int perm[4], bool* stb, bool* stk, bool* sbk) {
+  *stb = l[0] < l[1];
+  *stk = l[2] < l[3];
+  *sbk = l[0] + l[1] > l[2] + l[3];
+  perm[0] = *sbk ? (*stk ? 3 : 2) : (*stb ? 1 : 0);
+  perm[1] = *sbk ? (*stk ? 2 : 3) : (*stb ? 0 : 1);
+  perm[2] = *sbk ? (*stb ? 1 : 0) : (*stk ? 3 : 2);
+  perm[3] = *sbk ? (*stb ? 0 : 1) : (*stk ? 2 : 3);
+}
+
+// Enqueues one prim_set_kernel launch for (l[0] l[1]|l[2] l[3]) on
+// ctx->stream: packs the caller's primitive quartets into staging rows in
+// the canonical orientation (bra pair swap: P - B = PA + AB and B - A;
+// ket pair swap likewise; bra-ket swap exchanges PA/QC, WP/WQ, zeta/eta
+// factors and AB/CD), every (00|00)^(m) times the 2 alpha of caller
+// centre `scale_ctr` when >= 0, and writes the sets to the device buffer
+// d_out.  Returns the program's set count through *nsets_out.
+lgx_status prim_set_launch(lgx_context* ctx, const int l[4], int deriv,
+                           const lgx_prim_quartet* prims, int nprim, const double AB[3],
+                           const double CD[3], int scale_ctr, double* d_out) {
+  int perm[4];
+  bool stb, stk, sbk;
+  canonical_perm(l, perm, &stb, &stk, &sbk);
+  ProgDev* P = nullptr;
+  lgx_status s = get_prog(ctx, l[perm[0]], l[perm[1]], l[perm[2]], l[perm[3]], deriv, &P);
+  if (s != LGX_OK) return s;
+  const int mmax = l[0] + l[1] + l[2] + l[3] + deriv;
+  if (mmax > kStMaxM) return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "(00|00)^(m) beyond m = 15");
+  double ab[3], cd[3];
+  for (int x = 0; x < 3; ++x) {
+    ab[x] = stb ? -AB[x] : AB[x];
+    cd[x] = stk ? -CD[x] : CD[x];
+  }
+  std::vector<double> rows(size_t(nprim) * kStage, 0.0);
+  for (int p = 0; p < nprim; ++p) {
+    const lgx_prim_quartet& q = prims[p];
+    double* st = &rows[size_t(p) * kStage];
+    double pa[3], qc[3], wp[3], wq[3];
+    for (int x = 0; x < 3; ++x) {
+      pa[x] = stb ? q.PA[x] + AB[x] : q.PA[x];
+      qc[x] = stk ? q.QC[x] + CD[x] : q.QC[x];
+      wp[x] = q.WP[x];
+      wq[x] = q.WQ[x];
     }
+    double z = q.oo2z, e = q.oo2e, rz = q.roz, re = q.roe;
+    if (sbk) {
+      for (int x = 0; x < 3; ++x) {
+        std::swap(pa[x], qc[x]);
+        std::swap(wp[x], wq[x]);
+      }
+      std::swap(z, e);
+      std::swap(rz, re);
+    }
+    const double w = scale_ctr >= 0 ? q.two_alpha[scale_ctr] : 1.0;
+    for (int m = 0; m <= mmax; ++m) st[kStF + m] = w * q.ss[m];
+    for (int x = 0; x < 3; ++x) {
+      st[kStPA + x] = pa[x];
+      st[kStWP + x] = wp[x];
+      st[kStQC + x] = qc[x];
+      st[kStWQ + x] = wq[x];
+    }
+    st[kStOo2z] = z;
+    st[kStRoz] = rz;
+    st[kStOo2e] = e;
+    st[kStRoe] = re;
+    st[kStOo2ze] = q.oo2ze;
+    st[kStW + 0] = q.two_alpha[perm[0]];
+    st[kStW + 1] = q.two_alpha[perm[1]];
+    st[kStW + 2] = q.two_alpha[perm[3]];
+  }
+  if (sbk)
+    for (int x = 0; x < 3; ++x) std::swap(ab[x], cd[x]);
+  PrimSetArgs a{};
+  a.prog = P->dev;
+  a.nrows = nprim;
+  a.stage_rows = 32;
+  for (int x = 0; x < 3; ++x) {
+    a.AB[x] = ab[x];
+    a.CD[x] = cd[x];
+  }
+  for (int k = 0; k < 4; ++k) a.perm[k] = perm[k];
+  a.out = d_out;
+  CK(ctx->prim_rows.ensure(std::max<size_t>(rows.size(), 1) * sizeof(double)));
+  // pageable source: the copy has read `rows` when cudaMemcpyAsync returns
+  CK(cudaMemcpyAsync(ctx->prim_rows.p, rows.data(), rows.size() * sizeof(double),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  a.rows = ctx->prim_rows.as<double>();
+  const size_t stage = stage_bytes_per_warp(false, a.stage_rows);
+  const size_t slot_bytes = size_t((P->host.total_slots() + 1) & ~1) * sizeof(double);
+  const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
+  size_t smem = stage + slot_bytes;
+  if (smem > smem_cap) {  // slots in global memory (L1/L2 resident)
+    CK(ctx->prim_slots.ensure(slot_bytes));
+    a.slots = ctx->prim_slots.as<double>();
+    smem = stage;
+  }
+  CK(launch_prim_set(a, smem, ctx->stream));
+  return LGX_OK;
+}
+
+// lgx_compute_primitive_set: one launch (deriv 0/1), or the first-
+// derivative sets of the raised / lowered quartets and the composition
+// (deriv 2).
+lgx_status primitive_set(lgx_context* ctx, const int l[4], int deriv,
+                         const lgx_prim_quartet* prims, int nprim, const double AB[3],
+                         const double CD[3], double* out, size_t out_capacity, int* nsets,
+                         int* nvalues) {
+  int n[4];
+  size_t nv = 1;
+  for (int k = 0; k < 4; ++k) {
+    const int lmax = deriv == 2 ? kMaxL - 1 : kMaxL;
+    if (l[k] < 0 || l[k] > lmax)
+      return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "shell angular momentum beyond the build's limit");
+    n[k] = ncart(l[k]);
+    nv *= size_t(n[k]);
+  }
+  const int ns = deriv == 0 ? 1 : (deriv == 1 ? 12 : 78);
+  if (nv * ns > out_capacity) return fail(ctx, LGX_ERR_TOO_LARGE, "output buffer too small");
+  *nsets = ns;
+  *nvalues = int(nv);
+  if (nprim == 0) {
+    std::fill(out, out + nv * ns, 0.0);
+    return LGX_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  if (deriv < 2) {
+    CK(ctx->out.ensure(nv * ns * sizeof(double)));
+    lgx_status s = prim_set_launch(ctx, l, deriv, prims, nprim, AB, CD, -1, ctx->out.as<double>());
+    if (s != LGX_OK) return s;
+    CK(cudaMemcpyAsync(out, ctx->out.p, nv * ns * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return LGX_OK;
+  }
+  // deriv 2: raised (weights 2 a_X) and lowered quartets, first derivatives
+  int64_t offu[4] = {0, 0, 0, 0}, offd[4] = {0, 0, 0, 0};
+  size_t su[4] = {0, 0, 0, 0}, sd[4] = {0, 0, 0, 0}, total = 0;
+  for (int X = 0; X < 4; ++X) {
+    su[X] = nv / size_t(n[X]) * size_t(ncart(l[X] + 1));
+    offu[X] = int64_t(total);
+    total += 12 * su[X];
+    if (l[X] > 0) {
+      sd[X] = nv / size_t(n[X]) * size_t(ncart(l[X] - 1));
+      offd[X] = int64_t(total);
+      total += 12 * sd[X];
+    }
+  }
+  CK(ctx->out.ensure(total * sizeof(double)));
+  double* d1 = ctx->out.as<double>();
+  for (int X = 0; X < 4; ++X) {
+    int lu[4] = {l[0], l[1], l[2], l[3]};
+    ++lu[X];
+    lgx_status s = prim_set_launch(ctx, lu, 1, prims, nprim, AB, CD, X, d1 + offu[X]);
+    if (s != LGX_OK) return s;
+    if (l[X] > 0) {
+      int ld[4] = {l[0], l[1], l[2], l[3]};
+      --ld[X];
+      s = prim_set_launch(ctx, ld, 1, prims, nprim, AB, CD, -1, d1 + offd[X]);
+      if (s != LGX_OK) return s;
+    }
+  }
+  std::vector<double> h(total);
+  CK(cudaMemcpyAsync(h.data(), d1, total * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const int pure[4] = {0, 0, 0, 0};
+  compose_deriv2(l, n, pure, h.data(), offu, offd, su, sd, nv, out);
   return LGX_OK;
 }
 
@@ -1796,6 +1986,20 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int
   *nvalues = int(nv);
   *is_null = nul;
   return LGX_OK;
+}
+
+lgx_status lgx_compute_primitive_set(lgx_context* ctx, int l1, int l2, int l3, int l4,
+                                     int deriv, const lgx_prim_quartet* prims, int nprim,
+                                     const double AB[3], const double CD[3], double* out,
+                                     size_t out_capacity, int* nsets, int* nvalues) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!AB || !CD || !out || !nsets || !nvalues || nprim < 0 || (nprim > 0 && !prims))
+    return fail(ctx, LGX_ERR_INVALID_ARG, "null argument or negative primitive count");
+  if (deriv < 0 || deriv > 2)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "deriv must be 0, 1 or 2");
+  const int l[4] = {l1, l2, l3, l4};
+  return primitive_set(ctx, l, deriv, prims, nprim, AB, CD, out, out_capacity, nsets, nvalues);
 }
 
 lgx_status lgx_set_basis(lgx_context* ctx, int nshell, const int32_t* l, const int32_t* pure,

@@ -185,6 +185,83 @@ cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t 
   return cudaGetLastError();
 }
 
+// One contracted Cartesian shell set from caller-supplied primitive data
+// (libint's generated per-quartet entry libint2_build_eri / _eri1: the
+// caller fills the Libint_t prefactors and (00|00)^(m) of every primitive
+// quartet, engine.impl.h:1389-1757, and the library contracts them,
+// dg.cc:1177-1189).  The host packs the rows in the canonical orientation;
+// one warp stages them in batches, runs the class's VRR program and post
+// program, and stores the Cartesian sets in the caller's shell order, the
+// derivative sets of centre C by translational invariance.
+__global__ void __launch_bounds__(32) prim_set_kernel(PrimSetArgs a) {
+  extern __shared__ double smem_d[];
+  const int lane = threadIdx.x & 31;
+  const DevProg& P = a.prog;
+  const int R = a.stage_rows;
+  double* stage = smem_d;
+  double* ktab = stage + R * kStage;
+  double* slots = a.slots ? a.slots : smem_d + ((R * kStage + kKtab + 3) & ~3);
+  for (int i = lane; i < P.nacc; i += 32) slots[i] = 0.0;
+  __syncwarp();
+  for (int base = 0; base < a.nrows; base += R) {
+    const int n = min(R, a.nrows - base);
+    const double* src = a.rows + (size_t)base * kStage;
+    for (int i = lane; i < n * kStage; i += 32) stage[i] = src[i];
+    __syncwarp();
+    const unsigned ballot = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+    vrr_consume<double>(P, stage, ballot, slots, ktab, lane);
+    __syncwarp();
+  }
+  QuartetGeom<double> g;
+  for (int x = 0; x < 3; ++x) {
+    g.AB[x] = a.AB[x];
+    g.CD[x] = a.CD[x];
+  }
+  const int dims[4] = {ncart_of(P.la), ncart_of(P.lb), ncart_of(P.lc), ncart_of(P.ld)};
+  int tn[4];
+  for (int t = 0; t < 4; ++t) tn[a.perm[t]] = dims[t];
+  const int n4 = P.ncart4;
+  auto caller_index = [&](int e) {
+    int ci[4];
+    int r = e;
+    ci[3] = r % dims[3]; r /= dims[3];
+    ci[2] = r % dims[2]; r /= dims[2];
+    ci[1] = r % dims[1]; ci[0] = r / dims[1];
+    int it[4];
+    for (int t = 0; t < 4; ++t) it[a.perm[t]] = ci[t];
+    return ((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3];
+  };
+  for (int ph = 0; ph < P.nphases; ++ph) {
+    run_post_phase<double>(P, ph, g, slots, lane);
+    const int ctr = P.deriv ? (ph == 0 ? 0 : (ph == 1 ? 1 : 3)) : 0;
+    for (int s = 0; s < P.sets_per_phase; ++s) {
+      const double* cart = slots + P.cart_out + s * n4;
+      double* cb = slots + P.cbuf + s * n4;
+      double* o = a.out + (size_t)(P.deriv ? a.perm[ctr] * 3 + s : 0) * n4;
+      for (int e = lane; e < n4; e += 32) {
+        o[caller_index(e)] = cart[e];
+        if (P.deriv) cb[e] = (ph == 0 ? 0.0 : cb[e]) - cart[e];
+      }
+      __syncwarp();
+      if (P.deriv && ph == P.nphases - 1) {
+        double* oc = a.out + (size_t)(a.perm[2] * 3 + s) * n4;
+        for (int e = lane; e < n4; e += 32) oc[caller_index(e)] = cb[e];
+        __syncwarp();
+      }
+    }
+  }
+}
+
+// One warp; smem = staging (stage_bytes_per_warp) + the slots when they
+// live in shared memory (a.slots == nullptr).
+cudaError_t launch_prim_set(const PrimSetArgs& a, size_t smem, cudaStream_t st) {
+  cudaError_t e =
+      cudaFuncSetAttribute(prim_set_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  prim_set_kernel<<<1, 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem) {
   if (!fp32) {

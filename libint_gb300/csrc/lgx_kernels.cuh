@@ -50,6 +50,29 @@ __device__ __forceinline__ int bin_segment(const BinWork& b, long long q) {
   return lo;
 }
 
+// Staging row of one primitive quartet (the VRR inputs, libint's Libint_t
+// prefactors: engine.impl.h:1389-1757), written by the kernels' prologue or,
+// for caller-supplied primitive data, packed on the host.
+constexpr int kStage = 36;        // values staged per primitive quartet
+constexpr int kStF = 0;           // (00|00)^(m) = F_m * pfac, m <= 15
+constexpr int kStMaxM = 15;
+constexpr int kStPA = 16, kStWP = 19, kStQC = 22, kStWQ = 25;
+constexpr int kStOo2z = 28, kStRoz = 29, kStOo2e = 30, kStRoe = 31, kStOo2ze = 32;
+constexpr int kStW = 33;          // 2 alpha_A, 2 alpha_B, 2 alpha_D
+
+// One contracted Cartesian shell set from staged primitive quartets in the
+// canonical orientation (prim_set_kernel).
+struct PrimSetArgs {
+  DevProg prog;
+  const double* rows;   // [nrows][kStage]
+  int nrows;
+  int stage_rows;       // rows staged in shared memory per batch
+  double AB[3], CD[3];  // canonical A - B, C - D
+  int perm[4];          // canonical position k -> caller position perm[k]
+  double* slots;        // global slot scratch, or nullptr for shared memory
+  double* out;          // nsets x ncart(l1) ncart(l2) ncart(l3) ncart(l4), caller order
+};
+
 struct EriArgs {
   DevBasis basis;
   const PairRec* pairs;

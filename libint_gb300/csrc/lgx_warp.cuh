@@ -28,12 +28,6 @@
 
 namespace lgx {
 
-
-constexpr int kStage = 36;        // values staged per primitive quartet
-constexpr int kStF = 0;           // F_m * pfac, m <= 15
-constexpr int kStPA = 16, kStWP = 19, kStQC = 22, kStWQ = 25;
-constexpr int kStOo2z = 28, kStRoz = 29, kStOo2e = 30, kStRoe = 31, kStOo2ze = 32;
-constexpr int kStW = 33;          // 2 alpha_A, 2 alpha_B, 2 alpha_D
 // Per-warp table of the integer-weighted recurrence factors of the current
 // primitive quartet: k/(2 zeta), k/(2 eta), k/(2(zeta+eta)) for k = 0..7.
 constexpr int kKtab = 24;
@@ -351,6 +345,81 @@ __device__ __forceinline__ PostOp load_post_op(const DevProg& P, int op) {
   return o;
 }
 
+// Step 2 for the staged primitive quartets of `ballot` (rows of `stage`):
+// the class's VRR program, level by level, and the accumulation of its
+// (e0|f0) targets into the contracted slots.
+template <typename T>
+__device__ __forceinline__ void vrr_consume(const DevProg& P, const T* __restrict__ stage,
+                                            unsigned ballot, T* __restrict__ slots,
+                                            T* __restrict__ ktab, int lane) {
+  while (ballot) {
+    const T* st = stage + (__ffs(ballot) - 1) * kStage;
+    ballot &= ballot - 1u;
+    const T PAx = st[kStPA], PAy = st[kStPA + 1], PAz = st[kStPA + 2];
+    const T WPx = st[kStWP], WPy = st[kStWP + 1], WPz = st[kStWP + 2];
+    const T QCx = st[kStQC], QCy = st[kStQC + 1], QCz = st[kStQC + 2];
+    const T WQx = st[kStWQ], WQy = st[kStWQ + 1], WQz = st[kStWQ + 2];
+    const T oo2z = st[kStOo2z], roz = st[kStRoz];
+    const T oo2e = st[kStOo2e], roe = st[kStRoe];
+    const T oo2ze = st[kStOo2ze];
+    const T w1 = st[kStW], w2 = st[kStW + 1], w3 = st[kStW + 2];
+    for (int m = lane; m <= P.mmax; m += 32) slots[P.leaf_slot0 + m] = st[kStF + m];
+    if (lane < kKtab)
+      ktab[lane] = small_int<T>(lane & 7) * (lane < 8 ? oo2z : (lane < 16 ? oo2e : oo2ze));
+    __syncwarp();
+    // one VRR op: slots[d] = c1*s1 + c2*s2 [+ k1*(s3 - c4*s4)] [+ k5*s5]
+    auto eval = [&](const VrrOp& o) -> T {
+      const unsigned fl = o.fl;
+      const int dir = (fl >> 1) & 3;
+      const int n1 = (fl >> 3) & 31;
+      const int ne = (fl >> 8) & 31;
+      T c1, c2, c4;
+      if ((fl & 1u) == 0) {
+        c1 = sel3(dir, PAx, PAy, PAz);
+        c2 = sel3(dir, WPx, WPy, WPz);
+        c4 = roz;
+      } else {
+        c1 = sel3(dir, QCx, QCy, QCz);
+        c2 = sel3(dir, WQx, WQy, WQz);
+        c4 = roe;
+      }
+      T val = c1 * slots[o.s1];
+      val = fma(c2, slots[o.s2], val);
+      if (n1) val = fma(ktab[((fl & 1u) << 3) + n1], fma(-c4, slots[o.s4], slots[o.s3]), val);
+      if (ne) val = fma(ktab[16 + ne], slots[o.s5], val);
+      return val;
+    };
+    for (int k = 0; k < P.nlev; ++k) {
+      if (k > 0) {
+        // two ops per lane per step, loads first: ops of a level are
+        // independent, so both may be evaluated before either is stored
+        const int o1 = P.vrr_lev[k + 1];
+        for (int op = P.vrr_lev[k] + lane; op < o1; op += 64) {
+          const bool two = op + 32 < o1;
+          const VrrOp x = load_vrr_op(P, op);
+          VrrOp y = x;
+          if (two) y = load_vrr_op(P, op + 32);
+          const T vx = eval(x);
+          T vy = T(0);
+          if (two) vy = eval(y);
+          slots[x.d] = vx;
+          if (two) slots[y.d] = vy;
+        }
+        __syncwarp();
+      }
+      const int a1 = P.acc_lev[k + 1];
+      for (int op = P.acc_lev[k] + lane; op < a1; op += 32) {
+        const uint2 u = __ldg(P.acc_ops + op);
+        const unsigned src = u.y & 0x3FFFFFFFu;
+        const unsigned w = u.y >> 30;
+        const T wt = w == 0 ? T(1) : (w == 1 ? w1 : (w == 2 ? w2 : w3));
+        slots[u.x] = fma(wt, slots[src], slots[u.x]);
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // Steps 1-2: contracted (e0|f0) accumulators in slots[0, nacc).  Returns the
 // number of primitive quartets that survived screening.
 template <typename T, bool ATT = false>
@@ -368,75 +437,10 @@ __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __
     const int idx = base + lane;
     bool keep = false;
     if (lane < R && idx < nq) keep = prologue<ATT>(a, g, idx, npbraket, stage + lane * kStage);
-    unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    const unsigned ballot = __ballot_sync(0xffffffffu, keep);
     __syncwarp();
     kept += __popc(ballot);
-    while (ballot) {
-      const T* st = stage + (__ffs(ballot) - 1) * kStage;
-      ballot &= ballot - 1u;
-      const T PAx = st[kStPA], PAy = st[kStPA + 1], PAz = st[kStPA + 2];
-      const T WPx = st[kStWP], WPy = st[kStWP + 1], WPz = st[kStWP + 2];
-      const T QCx = st[kStQC], QCy = st[kStQC + 1], QCz = st[kStQC + 2];
-      const T WQx = st[kStWQ], WQy = st[kStWQ + 1], WQz = st[kStWQ + 2];
-      const T oo2z = st[kStOo2z], roz = st[kStRoz];
-      const T oo2e = st[kStOo2e], roe = st[kStRoe];
-      const T oo2ze = st[kStOo2ze];
-      const T w1 = st[kStW], w2 = st[kStW + 1], w3 = st[kStW + 2];
-      for (int m = lane; m <= P.mmax; m += 32) slots[P.leaf_slot0 + m] = st[kStF + m];
-      if (lane < kKtab)
-        ktab[lane] = small_int<T>(lane & 7) * (lane < 8 ? oo2z : (lane < 16 ? oo2e : oo2ze));
-      __syncwarp();
-      // one VRR op: slots[d] = c1*s1 + c2*s2 [+ k1*(s3 - c4*s4)] [+ k5*s5]
-      auto eval = [&](const VrrOp& o) -> T {
-        const unsigned fl = o.fl;
-        const int dir = (fl >> 1) & 3;
-        const int n1 = (fl >> 3) & 31;
-        const int ne = (fl >> 8) & 31;
-        T c1, c2, c4;
-        if ((fl & 1u) == 0) {
-          c1 = sel3(dir, PAx, PAy, PAz);
-          c2 = sel3(dir, WPx, WPy, WPz);
-          c4 = roz;
-        } else {
-          c1 = sel3(dir, QCx, QCy, QCz);
-          c2 = sel3(dir, WQx, WQy, WQz);
-          c4 = roe;
-        }
-        T val = c1 * slots[o.s1];
-        val = fma(c2, slots[o.s2], val);
-        if (n1) val = fma(ktab[((fl & 1u) << 3) + n1], fma(-c4, slots[o.s4], slots[o.s3]), val);
-        if (ne) val = fma(ktab[16 + ne], slots[o.s5], val);
-        return val;
-      };
-      for (int k = 0; k < P.nlev; ++k) {
-        if (k > 0) {
-          // two ops per lane per step, loads first: ops of a level are
-          // independent, so both may be evaluated before either is stored
-          const int o1 = P.vrr_lev[k + 1];
-          for (int op = P.vrr_lev[k] + lane; op < o1; op += 64) {
-            const bool two = op + 32 < o1;
-            const VrrOp x = load_vrr_op(P, op);
-            VrrOp y = x;
-            if (two) y = load_vrr_op(P, op + 32);
-            const T vx = eval(x);
-            T vy = T(0);
-            if (two) vy = eval(y);
-            slots[x.d] = vx;
-            if (two) slots[y.d] = vy;
-          }
-          __syncwarp();
-        }
-        const int a1 = P.acc_lev[k + 1];
-        for (int op = P.acc_lev[k] + lane; op < a1; op += 32) {
-          const uint2 u = __ldg(P.acc_ops + op);
-          const unsigned src = u.y & 0x3FFFFFFFu;
-          const unsigned w = u.y >> 30;
-          const T wt = w == 0 ? T(1) : (w == 1 ? w1 : (w == 2 ? w2 : w3));
-          slots[u.x] = fma(wt, slots[src], slots[u.x]);
-        }
-        __syncwarp();
-      }
-    }
+    vrr_consume<T>(P, stage, ballot, slots, ktab, lane);
     __syncwarp();
   }
   return kept;

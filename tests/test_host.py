@@ -77,3 +77,61 @@ def test_random_density_is_psd(lgx):
     assert np.allclose(D, D.T)
     w = np.linalg.eigvalsh(D)
     assert w.min() > -1e-12 and np.sum(w > 1e-10) == 7
+
+
+LIBINT2_C_PROBE = r"""
+#include <libint2.h>
+#include <stdio.h>
+#include <stdlib.h>
+#if !LIBINT2_DEFINED(eri, LIBINT_T_SS_EREP_SS(3)) || !LIBINT2_DEFINED(eri, two_alpha1_ket)
+#error members of Libint_t not reported by LIBINT2_DEFINED
+#endif
+#if LIBINT2_DEFINED(eri, no_such_member)
+#error LIBINT2_DEFINED reports a member that does not exist
+#endif
+int main(void) {
+  Libint_t e[2];
+  double* buf = (double*)malloc(libint2_need_memory_eri1(2) * sizeof(double));
+  e[0].LIBINT_T_SS_EREP_SS(14)[0] = 1.0;
+  if (libint2_need_memory_eri(3) != 10000 || libint2_need_memory_eri2(1) != 78 * 81) return 1;
+  libint2_init_eri1(&e[0], 2, buf);
+  if (e[0].stack != buf || e[0].contrdepth != 1 || e[0].targets[0] != 0) return 2;
+  libint2_cleanup_eri1(&e[0]);
+  libint2_init_eri(&e[1], 3, 0);
+  if (!e[1].stack) return 3;
+  libint2_cleanup_eri(&e[1]);
+  if (LIBINT2_PREFIXED_NAME(libint2_build_eri)[3][0][1][2] == 0) return 4;
+  if (libint2_build_eri2[2][2][2][2] == 0 || libint2_build_eri1[0][3][0][3] == 0) return 5;
+  free(buf);
+  printf("ok\n");
+  return 0;
+}
+"""
+
+
+def test_libint2_c_header_and_exports(lgx, tmp_path):
+    # libint's generated-library C API (include/libint2.h): compiles as C99
+    # and C++17, LIBINT2_DEFINED / LIBINT_T_SS_EREP_SS behave as in libint,
+    # the library exports every declared entry, and init / need_memory /
+    # cleanup keep the stack bookkeeping (no build call: those need a GPU)
+    import subprocess
+    lib = lgx._lgx.load()
+    header = open(os.path.join(ROOT, "include", "libint2.h")).read()
+    names = set(re.findall(r"\b(libint2_[a-z0-9_]+)\s*[\(\[]", header))
+    names |= set(re.findall(r"\(\*(libint2_[a-z0-9_]+)\[", header))
+    assert {"libint2_build_eri", "libint2_build_eri1", "libint2_build_eri2",
+            "libint2_init_eri", "libint2_static_init"} <= names
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+    src = tmp_path / "probe.c"
+    src.write_text(LIBINT2_C_PROBE)
+    libdir = os.path.join(ROOT, "libint_gb300")
+    for cc, std, out in (("gcc", "-std=c99", "probe_c"), ("g++", "-std=c++17", "probe_cxx")):
+        exe = str(tmp_path / out)
+        cmd = [cc, std, "-Wall", "-Werror", "-I", os.path.join(ROOT, "include")]
+        if cc == "g++":
+            cmd += ["-x", "c++"]
+        subprocess.check_call(cmd + [str(src), "-x", "none", "-L", libdir, "-llgx",
+                                     "-Wl,-rpath," + libdir, "-o", exe])
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0 and r.stdout.strip() == "ok", (cc, r.returncode, r.stderr)
