@@ -41,7 +41,8 @@ typedef int lgx_status;
 #define LGX_ERR_NO_DEVICE 7     /* no CUDA device / wrong architecture       */
 
 /* Largest angular momentum per shell and derivative order supported
- * (deriv_order 2 through lgx_compute_shellset for shells up to l = 2). */
+ * (deriv_order 2 through lgx_compute_shellset and
+ * lgx_compute_primitive_set). */
 #define LGX_MAX_L 3
 #define LGX_MAX_DERIV 2
 #define LGX_MAX_NPRIM 16
@@ -108,7 +109,8 @@ const char* lgx_version(void);
 /* deriv 2 (compute2<coulomb, xx_xx, 2>): 78 second-derivative sets in
  * libint's order (coordinate pairs c1 <= c2 over A_x..D_z, row-major,
  * CartesianDerivIterator<4>(2) of include/libint2/deriv_iter.h), for shells
- * up to l = 2 (LGX_ERR_LMAX_EXCEEDED above). */
+ * up to LGX_MAX_L (the raised Cartesian copies of the composition reach
+ * LGX_MAX_L + 1 internally). */
 lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4],
                                 int deriv, double precision, int screening,
                                 double* out, size_t out_capacity, int* nsets,
@@ -150,7 +152,7 @@ typedef struct lgx_prim_quartet {
  * row-major ncart(l1) ncart(l2) ncart(l3) ncart(l4) in the caller's shell
  * order and Cartesian (no solid-harmonic transform, no renormalisation:
  * the caller's (00|00)^(m) carry it), written to the HOST buffer `out`.
- * deriv 2 (libint2_build_eri2, shells up to l = 2): the 78 sets in
+ * deriv 2 (libint2_build_eri2): the 78 sets in
  * libint's CartesianDerivIterator order, composed from the first-derivative
  * sets of the quartets with one shell raised (its primitives weighted by
  * 2 a_X) and lowered, which requires ss[] up to m = l1+..+l4+2. */

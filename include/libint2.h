@@ -45,7 +45,7 @@
 #define LIBINT2_SUPPORT_ERI 1
 #define LIBINT2_MAX_AM_eri 3
 #define LIBINT2_MAX_AM_eri1 3
-#define LIBINT2_MAX_AM_eri2 2
+#define LIBINT2_MAX_AM_eri2 3
 #define LIBINT2_MAX_AM 3
 #define LIBINT_MAX_AM 4
 #define LIBINT2_DERIV_ERI_ORDER 2

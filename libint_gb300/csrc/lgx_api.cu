@@ -437,9 +437,12 @@ lgx_status get_prog(lgx_context* ctx, int la, int lb, int lc, int ld, int deriv,
 }
 
 // ---------------------------------------------------------------- basis
+// lmax: LGX_MAX_L for callers' bases; one more for the Cartesian raised
+// shells of the second-derivative composition.
 lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t* l,
                         const int32_t* pure, const int32_t* nprim, const int32_t* atom,
-                        const double* origins, const double* alpha, const double* coeff) {
+                        const double* origins, const double* alpha, const double* coeff,
+                        int lmax = kMaxL) {
   if (nshell <= 0 || !l || !pure || !nprim || !origins || !alpha || !coeff)
     return fail(ctx, LGX_ERR_INVALID_ARG, "lgx_set_basis: null array or empty basis");
   B.nshell = nshell;
@@ -452,7 +455,7 @@ lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t
   B.bf_off.resize(nshell);
   int np = 0, nbf = 0, natoms = 0;
   for (int s = 0; s < nshell; ++s) {
-    if (l[s] < 0 || l[s] > kMaxL)
+    if (l[s] < 0 || l[s] > lmax || (pure[s] && l[s] > kMaxL))
       return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "shell angular momentum exceeds LGX_MAX_L");
     if (nprim[s] <= 0 || nprim[s] > kMaxNprim)
       return fail(ctx, LGX_ERR_TOO_LARGE, "shell contraction depth exceeds LGX_MAX_NPRIM");
@@ -1520,7 +1523,8 @@ void compose_deriv2(const int lx[4], const int n[4], const int pure[4], const do
 // include/libint2/deriv_iter.h: coordinate pairs c1 <= c2, row-major over
 // A_x..D_z) and in the caller's shell order, so no derivative remap is
 // needed; pure shells are transformed after the Cartesian composition.
-// Shells up to l = 2: the raised copies reach LGX_MAX_L.
+// Shells up to LGX_MAX_L: the raised copies reach LGX_MAX_L + 1 (Cartesian
+// class programs of kMaxLInternal).
 lgx_status shellset_deriv2(lgx_context* ctx, const lgx_shell shells[4], double precision,
                            int screening, double* out, size_t out_capacity, int* nsets,
                            int* nvalues, int* is_null) {
@@ -1531,9 +1535,8 @@ lgx_status shellset_deriv2(lgx_context* ctx, const lgx_shell shells[4], double p
   for (int k = 0; k < 4; ++k) {
     if (!shells[k].alpha || !shells[k].coeff) return fail(ctx, LGX_ERR_INVALID_ARG, "null shell data");
     lx[k] = shells[k].l;
-    if (lx[k] < 0 || lx[k] > kMaxL - 1)
-      return fail(ctx, LGX_ERR_LMAX_EXCEEDED,
-                  "deriv_order 2: shell angular momentum above LGX_MAX_L - 1");
+    if (lx[k] < 0 || lx[k] > kMaxL)
+      return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "shell angular momentum exceeds LGX_MAX_L");
     n[k] = nfunc(lx[k], shells[k].pure ? 1 : 0);
     nv *= size_t(n[k]);
   }
@@ -1560,7 +1563,8 @@ lgx_status shellset_deriv2(lgx_context* ctx, const lgx_shell shells[4], double p
   for (int X = 0; X < 4; ++X) push(X, X, 0, false);
   for (int X = 0; X < 4; ++X) push(4 + X, X, +1, true);
   for (int X = 0; X < 4; ++X) push(8 + X, X, lx[X] > 0 ? -1 : 0, false);
-  lgx_status s = upload_basis(ctx, ctx->small, 12, l, pure, np, atom, O, al.data(), co.data());
+  lgx_status s =
+      upload_basis(ctx, ctx->small, 12, l, pure, np, atom, O, al.data(), co.data(), kMaxLInternal);
   if (s != LGX_OK) return s;
   const double ln_prec =
       precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
@@ -1725,8 +1729,7 @@ lgx_status primitive_set(lgx_context* ctx, const int l[4], int deriv,
   int n[4];
   size_t nv = 1;
   for (int k = 0; k < 4; ++k) {
-    const int lmax = deriv == 2 ? kMaxL - 1 : kMaxL;
-    if (l[k] < 0 || l[k] > lmax)
+    if (l[k] < 0 || l[k] > kMaxL)
       return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "shell angular momentum beyond the build's limit");
     n[k] = ncart(l[k]);
     nv *= size_t(n[k]);

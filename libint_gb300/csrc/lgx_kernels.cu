@@ -47,8 +47,9 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, P
       mPB = fmax(mPB, fabs(r.P[x] - B[x]));
     }
     const int l1 = b.l[s1], l2 = b.l[s2];
-    const double fl1 = l1 < 2 ? 1.0 : (l1 == 2 ? 2.0 : 6.0);
-    const double fl2 = l2 < 2 ? 1.0 : (l2 == 2 ? 2.0 : 6.0);
+    // l! (l <= 4: the Cartesian raised shells of deriv 2 reach g)
+    const double fl1 = l1 < 2 ? 1.0 : (l1 == 2 ? 2.0 : (l1 == 3 ? 6.0 : 24.0));
+    const double fl2 = l2 < 2 ? 1.0 : (l2 == 2 ? 2.0 : (l2 == 3 ? 6.0 : 24.0));
     const double t1 = pow(mPA, l1) * pow(mPB, l2);
     const double t2 = fl1 * fl2 * pow(oog, l1 + l2);
     nonsph = fmax(t1, t2);

@@ -134,10 +134,6 @@ void build_fn(const Libint_t* inteval) {
 #define LGX_B3(D, a, b) { LGX_B4(D, a, b, 0), LGX_B4(D, a, b, 1), LGX_B4(D, a, b, 2), LGX_B4(D, a, b, 3) }
 #define LGX_B2(D, a) { LGX_B3(D, a, 0), LGX_B3(D, a, 1), LGX_B3(D, a, 2), LGX_B3(D, a, 3) }
 #define LGX_B1(D) { LGX_B2(D, 0), LGX_B2(D, 1), LGX_B2(D, 2), LGX_B2(D, 3) }
-#define LGX_C4(D, a, b, c) { &build_fn<a, b, c, 0, D>, &build_fn<a, b, c, 1, D>, &build_fn<a, b, c, 2, D> }
-#define LGX_C3(D, a, b) { LGX_C4(D, a, b, 0), LGX_C4(D, a, b, 1), LGX_C4(D, a, b, 2) }
-#define LGX_C2(D, a) { LGX_C3(D, a, 0), LGX_C3(D, a, 1), LGX_C3(D, a, 2) }
-#define LGX_C1(D) { LGX_C2(D, 0), LGX_C2(D, 1), LGX_C2(D, 2) }
 
 extern "C" {
 
@@ -146,7 +142,7 @@ void (*libint2_build_eri[LIBINT2_MAX_AM_eri + 1][LIBINT2_MAX_AM_eri + 1][LIBINT2
 void (*libint2_build_eri1[LIBINT2_MAX_AM_eri1 + 1][LIBINT2_MAX_AM_eri1 + 1][LIBINT2_MAX_AM_eri1 + 1]
                          [LIBINT2_MAX_AM_eri1 + 1])(const Libint_t*) = LGX_B1(1);
 void (*libint2_build_eri2[LIBINT2_MAX_AM_eri2 + 1][LIBINT2_MAX_AM_eri2 + 1][LIBINT2_MAX_AM_eri2 + 1]
-                         [LIBINT2_MAX_AM_eri2 + 1])(const Libint_t*) = LGX_C1(2);
+                         [LIBINT2_MAX_AM_eri2 + 1])(const Libint_t*) = LGX_B1(2);
 
 void libint2_static_init(void) {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -200,9 +200,9 @@ int asap_levels(std::vector<N>& nodes) {
 
 int num_classes() {
   int n = 0;
-  for (int la = 0; la <= kMaxL; ++la)
+  for (int la = 0; la <= kMaxLInternal; ++la)
     for (int lb = 0; lb <= la; ++lb)
-      for (int lc = 0; lc <= kMaxL; ++lc)
+      for (int lc = 0; lc <= kMaxLInternal; ++lc)
         for (int ld = 0; ld <= lc; ++ld)
           if (la + lb <= lc + ld) ++n;
   return n;
@@ -210,9 +210,9 @@ int num_classes() {
 
 int class_index(int la, int lb, int lc, int ld) {
   int n = 0;
-  for (int a = 0; a <= kMaxL; ++a)
+  for (int a = 0; a <= kMaxLInternal; ++a)
     for (int b = 0; b <= a; ++b)
-      for (int c = 0; c <= kMaxL; ++c)
+      for (int c = 0; c <= kMaxLInternal; ++c)
         for (int d = 0; d <= c; ++d)
           if (a + b <= c + d) {
             if (a == la && b == lb && c == lc && d == ld) return n;
@@ -222,7 +222,7 @@ int class_index(int la, int lb, int lc, int ld) {
 }
 
 ClassProgramHost build_class_program(int la, int lb, int lc, int ld, int deriv) {
-  if (la < lb || lc < ld || la + lb > lc + ld || la > kMaxL || lc > kMaxL ||
+  if (la < lb || lc < ld || la + lb > lc + ld || la > kMaxLInternal || lc > kMaxLInternal ||
       deriv < 0 || deriv > kMaxDeriv)
     throw std::runtime_error("lgx: non-canonical class");
   ClassProgramHost P;

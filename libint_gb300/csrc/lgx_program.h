@@ -24,8 +24,10 @@
 namespace lgx {
 
 constexpr int kMaxL = 3;
+// Class programs also serve one more angular momentum quantum: the
+// Cartesian raised shells of the second-derivative composition.
+constexpr int kMaxLInternal = kMaxL + 1;
 constexpr int kMaxDeriv = 1;
-constexpr int kMaxM = 4 * kMaxL + kMaxDeriv;  // highest Boys order needed
 constexpr int kMaxNprim = 16;
 
 // Slots are 32-bit indices into a per-warp array of T.

@@ -891,7 +891,7 @@ int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
   const int tgt[4] = {s1, s2, s3, s4};
   if (deriv == 2) {
     for (int k = 0; k < 4; ++k)
-      if (bs->l[tgt[k]] > 2) return -1;
+      if (bs->l[tgt[k]] > 3) return -1;  // raised copies up to g
     return compute_quartet_d2(bs, tgt, precision, method, w, out);
   }
   return compute_quartet(bs, tgt, deriv, precision, method, w, out);

@@ -85,7 +85,7 @@ int main(int argc, char** argv) {
     const auto& r2 = e2.compute(obs[t[0]], obs[t[1]]);
     for (size_t i = 0; i < obs[t[0]].size() * obs[t[1]].size(); ++i) put(r2[0][i]);
   }
-  // second derivatives: compute2<coulomb, xx_xx, 2>, 78 sets (shells up to d)
+  // second derivatives: compute2<coulomb, xx_xx, 2>, 78 sets
   libint2::Engine d2(libint2::Operator::coulomb, obs.max_nprim(), 2, 2);
   const size_t q2[][4] = {{5, 3, 8, 0}, {3, 0, 1, 9}};
   for (const auto& q : q2) {

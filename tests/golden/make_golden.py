@@ -19,7 +19,7 @@ Outputs (numpy .npz, committed):
                   as eri.npz plus the braket rank
   eri_d2.npz      brute-force second-derivative (deriv_order 2) shell sets, 78
                   per quartet in libint's order (CartesianDerivIterator<4>(2)),
-                  shells up to d, with that order as coordinate pairs
+                  shells up to f, with that order as coordinate pairs
   hf.npz          system-level golden values of the reference's Hartree-Fock
                   tests, read as text: the rotated-water geometry
                   (tests/hartree-fock/h2o_rotated.xyz) with the aug-cc-pVDZ
@@ -229,7 +229,9 @@ def eri_d2_fixtures():
     c1, c2 = oracle.ref_deriv_order2(ref)
     cases = [(0, 0, 0, 0), (1, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 0), (0, 0, 0, 1), (1, 1, 0, 0),
              (1, 0, 1, 0), (0, 1, 0, 1), (1, 1, 1, 1), (2, 0, 0, 0), (0, 2, 1, 0), (2, 1, 0, 1),
-             (1, 0, 2, 1), (2, 2, 0, 0), (0, 0, 2, 2), (2, 1, 1, 2)]
+             (1, 0, 2, 1), (2, 2, 0, 0), (0, 0, 2, 2), (2, 1, 1, 2),
+             # f shells (the composition raises them to g)
+             (3, 0, 0, 0), (0, 1, 3, 0), (3, 1, 0, 2), (2, 3, 3, 1)]
     recs = {"l": [], "pure": [], "nprim": [], "alpha": [], "coeff": [], "O": [], "offset": []}
     off, vals = 0, []
     for t, ls in enumerate(cases):

@@ -21,10 +21,10 @@ def test_lmax_exceeded(lgx):
     with pytest.raises(lgx.LgxError) as e:
         ctx.compute_shellset([g, s, s, s])
     assert e.value.status == lgx._lgx.LGX_ERR_LMAX_EXCEEDED
-    # second derivatives: shells up to d
-    f = _shell(lgx, 3, pure=True)
+    # second derivatives: shells up to f (the composition raises them to g
+    # internally), g refused
     with pytest.raises(lgx.LgxError) as e:
-        ctx.compute_shellset([f, s, s, s], deriv=2)
+        ctx.compute_shellset([s, g, s, s], deriv=2)
     assert e.value.status == lgx._lgx.LGX_ERR_LMAX_EXCEEDED
     # Engine raises for max_l above the build, like Engine::lmax_exceeded
     with pytest.raises(lgx.LgxError):

@@ -30,7 +30,7 @@ def test_engine_vs_reference_bruteforce(lgx):
 
 
 def test_engine_deriv2_vs_reference_bruteforce(lgx):
-    # deriv_order 2 (78 sets per quartet, shells up to d) through Engine
+    # deriv_order 2 (78 sets per quartet, shells up to f) through Engine
     from golden_util import eri_d2_cases
     worst = 0.0
     for l, pure, nprim, alpha, coeff, O, vals in eri_d2_cases():
@@ -41,7 +41,7 @@ def test_engine_deriv2_vs_reference_bruteforce(lgx):
                                                     coeff[off:off + n], O[3 * k:3 * k + 3],
                                                     bool(pure[k])))
             off += n
-        eng = lgx.Engine(lgx.Operator.coulomb, 4, 2, 2, precision=0.0)
+        eng = lgx.Engine(lgx.Operator.coulomb, 4, 3, 2, precision=0.0)
         assert eng.nshellsets() == 78
         r = eng.compute(*shells)
         got = np.concatenate([x.reshape(-1) for x in r])

@@ -35,9 +35,10 @@ def _cases(rng, deriv):
         every = list(itertools.product(range(4), repeat=4))
         pick = rng.choice(len(every), 48, replace=False)
         return [every[i] for i in pick] + [(3, 3, 3, 3), (0, 3, 1, 2), (3, 0, 0, 0)]
-    every = list(itertools.product(range(3), repeat=4))
+    every = list(itertools.product(range(4), repeat=4))
     pick = rng.choice(len(every), 24, replace=False)
-    return [every[i] for i in pick] + [(2, 2, 2, 2), (0, 2, 1, 0), (1, 1, 1, 1)]
+    return [every[i] for i in pick] + [(2, 2, 2, 2), (0, 2, 1, 0), (1, 1, 1, 1), (3, 3, 3, 3),
+                                       (3, 0, 1, 2)]
 
 
 @pytest.mark.parametrize("deriv", [0, 1, 2])
@@ -67,7 +68,7 @@ def test_primitive_set_errors(lgx):
         ctx.compute_primitive_set((4, 0, 0, 0), prims, AB, CD)
     assert e.value.status == lgx._lgx.LGX_ERR_LMAX_EXCEEDED
     with pytest.raises(lgx.LgxError) as e:
-        ctx.compute_primitive_set((3, 0, 0, 0), prims, AB, CD, deriv=2)
+        ctx.compute_primitive_set((0, 0, 4, 0), prims, AB, CD, deriv=2)
     assert e.value.status == lgx._lgx.LGX_ERR_LMAX_EXCEEDED
     # no primitive quartets: zero sets
     z = ctx.compute_primitive_set((1, 0, 0, 0), prims[:0], AB, CD)
@@ -165,7 +166,8 @@ def test_libint2_c_api_vs_oracle(lgx, tmp_path):
     for deriv, lss in ((0, [(0, 0, 0, 0), (1, 0, 1, 0), (0, 1, 2, 3), (3, 2, 1, 0), (2, 2, 2, 2),
                             (3, 3, 3, 3), (1, 1, 0, 0)]),
                        (1, [(1, 0, 0, 0), (0, 0, 1, 1), (2, 1, 0, 3), (3, 3, 2, 2)]),
-                       (2, [(1, 0, 0, 0), (0, 1, 1, 0), (2, 1, 0, 2), (2, 2, 2, 2)])):
+                       (2, [(1, 0, 0, 0), (0, 1, 1, 0), (2, 1, 0, 2), (2, 2, 2, 2),
+                            (3, 1, 0, 3)])):
         for i, ls in enumerate(lss):
             sh = random_shells(rng, ls, max_depth=2)
             prims, AB, CD = prim_quartets(sh, deriv, lgx._lgx.PRIM_DTYPE)
