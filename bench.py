@@ -517,6 +517,113 @@ def run_primitive_api(args):
     return 0
 
 
+def run_rows(args):
+    """--rows: the widened rows of the path, each timed end to end through
+    the public API on the GPU with the oracle beside it on the host cores:
+    density-fitting tensors (BraKet xs_xx / xs_xs through lgx_compute_batch),
+    second-derivative shell sets (deriv_order 2, per call) and a
+    range-separated J/K pass (erfc, omega = 0.4)."""
+    import torch
+    import libint_gb300 as lg
+    from oracle import oracle
+    oracle.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rows = {}
+    cores = os.cpu_count()
+
+    # density fitting: (P|ab) and (P|Q) of (H2O)8 cc-pVDZ / cc-pVDZ-jkfit
+    atoms = lg.water_cluster(2, 2, 2, spacing=3.0, jitter=0.2, seed=SEED)
+    obs = lg.BasisSet("cc-pVDZ", atoms)
+    dfbs = lg.BasisSet("cc-pVDZ-jkfit", atoms)
+    full = lg.BasisSet(list(obs) + list(dfbs) + [lg.Shell.unit()])
+    full.atom_of_shell = obs.atom_of_shell + dfbs.atom_of_shell + [0]
+    ns, na, u = len(obs), len(dfbs), len(obs) + len(dfbs)
+    a, b = np.tril_indices(ns)
+    P = np.arange(ns, ns + na)
+    q3 = np.stack(np.broadcast_arrays(P[:, None], u, a[None, :], b[None, :]), -1).reshape(-1, 4)
+    r1, r2 = np.tril_indices(na)
+    q2 = np.stack([P[r1], np.full_like(r1, u), P[r2], np.full_like(r1, u)], -1)
+    q = np.ascontiguousarray(np.concatenate([q3, q2]), np.int32)
+    ctx = lg.Context(local)
+    ctx.set_basis(full)
+    ctx.compute_batch(q)
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out, offs, _ = ctx.compute_batch(q)
+    t_gpu = (time.perf_counter() - t0) / reps
+    sz = np.array([sh.size() for sh in full], np.int64)
+    nint = int((sz[q[:, 0]] * sz[q[:, 2]] * sz[q[:, 3]]).sum())
+    ob = oracle.OracleBasis.from_basis(full)
+    t0 = time.perf_counter()
+    oracle.compute_batch(ob, q, offs, int(offs[-1] + nint), nthreads=0)
+    t_cpu = time.perf_counter() - t0
+    rows["f2_df_tensors"] = {
+        "workload": "(H2O)8 cc-pVDZ / cc-pVDZ-jkfit: every (P|ab) and (P|Q)",
+        "quartets": len(q), "integrals": nint, "ms": 1e3 * t_gpu, "eri_per_s": nint / t_gpu,
+        "oracle_ms": 1e3 * t_cpu, "oracle_eri_per_s": nint / t_cpu, "oracle_cores": cores,
+        "note": "lgx_compute_batch, FP64, host output buffer (copy timed)"}
+    ctx.close()
+
+    # second derivatives: per-call shell sets through the Engine entry
+    rng = np.random.default_rng(SEED)
+    d2 = []
+    ctx = lg.Context(local)
+    for ls in ((1, 1, 1, 1), (2, 1, 2, 0), (2, 2, 2, 2), (3, 2, 1, 0)):
+        sh = [lg.Shell(l, [(float(x), 1.0) for x in np.sort(rng.uniform(0.3, 3.0, 2))[::-1]],
+                       tuple(rng.uniform(-1.2, 1.2, 3)), pure=l >= 2) for l in ls]
+        for _ in range(3):
+            ctx.compute_shellset(sh, deriv=2)
+        n = 50
+        t0 = time.perf_counter()
+        for _ in range(n):
+            r = ctx.compute_shellset(sh, deriv=2)
+        tg = (time.perf_counter() - t0) / n
+        ob = oracle.OracleBasis.from_basis(lg.BasisSet(sh))
+        t0 = time.perf_counter()
+        for _ in range(n):
+            oracle.compute_quartet(ob, 0, 1, 2, 3, deriv=2)
+        tc = (time.perf_counter() - t0) / n
+        nint = sum(x.size for x in r)
+        d2.append({"class": "(%d%d|%d%d)" % ls, "integrals": nint, "us_per_call": 1e6 * tg,
+                   "oracle_us_per_call": 1e6 * tc})
+    rows["f3_deriv2_shellsets"] = {"classes": d2, "note": "78 sets per call, 2 primitives per "
+                                   "shell, pure d/f; oracle on one host core"}
+    ctx.close()
+
+    # range-separated J/K: erfc(0.4 r)/r pass vs the Coulomb pass, (H2O)16 cc-pVDZ
+    atoms, bs, D, thresh, _ = build_inputs("h2o16_cc-pvdz")
+    res = {}
+    for name, op in (("coulomb", lg.Operator.coulomb), ("erfc", lg.Operator.erfc_coulomb)):
+        ctx = lg.Context(local)
+        ctx.set_basis(bs)
+        ctx.set_operator(op, 0.4)
+        dD = torch.tensor(D, device="cuda")
+        dJ, dK = torch.empty_like(dD), torch.empty_like(dD)
+        for _ in range(2):
+            ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, lg._lgx.LGX_FP64)
+        ms = []
+        for _ in range(3):
+            st = ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh,
+                               lg._lgx.LGX_FP64)
+            ms.append(st.pass_ms)
+        Kq = ctx.schwarz()
+        oracle.set_operator(oracle.OP_ERFC_COULOMB if name == "erfc" else oracle.OP_COULOMB, 0.4)
+        v, nsamp, tsamp, npair = cpu_baseline(bs, D, Kq, thresh, 8.0)
+        res[name] = {"pass_ms": statistics.median(ms), "integrals": int(st.integrals),
+                     "eri_per_s": st.integrals / (statistics.median(ms) * 1e-3),
+                     "oracle_eri_per_s": v, "oracle_sample_integrals": int(nsamp)}
+        ctx.close()
+    oracle.set_operator(oracle.OP_COULOMB, 0.0)
+    rows["f4_erfc_jk"] = dict(res, workload="(H2O)16 cc-pVDZ, Schwarz 1e-12, FP64, omega 0.4",
+                             note="device-resident D/J/K, pass time from CUDA events; oracle "
+                                  "on a bounded sample of bra pairs, all host threads")
+    print(json.dumps({"metric": "widened rows: GPU vs oracle", "data": "synthetic",
+                      "cores": cores, "rows": rows}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -529,9 +636,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--primitive-api", action="store_true",
                     help="time the generated-library entry (libint2_build_eri*) instead")
+    ap.add_argument("--rows", action="store_true",
+                    help="time the widened rows (DF tensors, deriv 2, erfc J/K) instead")
     args = ap.parse_args()
     if args.primitive_api:
         return run_primitive_api(args)
+    if args.rows:
+        return run_rows(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

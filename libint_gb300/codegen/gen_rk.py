@@ -31,10 +31,13 @@ OUT_DEFAULT = os.path.join(os.path.dirname(HERE), "csrc", "gen", "rk_classes.cuh
 RK_MAX_L = 6
 RK_MAX_L_STORE = 4
 LMAX = 3
-# (precision, mode) variants and the class limit of each
-VARIANTS = [("double", "kModeJK", RK_MAX_L), ("float", "kModeJK", RK_MAX_L),
-            ("double", "kModeStore", RK_MAX_L_STORE), ("double", "kModeSchwarz", RK_MAX_L_STORE),
-            ("float", "kModeStore", RK_MAX_L_STORE)]
+# (precision, mode, class limit, attenuated operator) variants; the
+# attenuated (erf / erfc) register kernels serve the J/K passes only
+VARIANTS = [("double", "kModeJK", RK_MAX_L, False), ("float", "kModeJK", RK_MAX_L, False),
+            ("double", "kModeStore", RK_MAX_L_STORE, False),
+            ("double", "kModeSchwarz", RK_MAX_L_STORE, False),
+            ("float", "kModeStore", RK_MAX_L_STORE, False),
+            ("double", "kModeJK", RK_MAX_L, True), ("float", "kModeJK", RK_MAX_L, True)]
 N_UNITS = 24  # instantiation translation units (compiled in parallel)
 
 
@@ -310,16 +313,16 @@ def write_units(gen_dir):
     (precision, mode, class) kernels; rk_dispatch.cu maps run-time
     (precision, mode, class) to them.  Returns the unit file names."""
     items = []
-    for prec, mode, lmax in VARIANTS:
+    for prec, mode, lmax, att in VARIANTS:
         for c in rk_classes(lmax):
-            items.append((prec, mode, c))
-    items.sort(key=lambda it: -_cost(it[2]))
+            items.append((prec, mode, att, c))
+    items.sort(key=lambda it: -_cost(it[3]))
     units = [[] for _ in range(N_UNITS)]
     load = [0] * N_UNITS
     for it in items:  # greedy balance by estimated code size
         k = load.index(min(load))
         units[k].append(it)
-        load[k] += _cost(it[2])
+        load[k] += _cost(it[3])
     names = []
     decls = []
     for k, u in enumerate(units):
@@ -327,38 +330,42 @@ def write_units(gen_dir):
         names.append(name)
         lines = ["// GENERATED by libint_gb300/codegen/gen_rk.py -- do not edit.",
                  '#include "../lgx_rk.cuh"', "", "namespace lgx {"]
-        for prec, mode, c in u:
-            fn = "rk_launch_%s_%s_%d%d%d%d" % (prec[0], mode[5:].lower(), *c)
-            decls.append((prec, mode, c, fn))
+        for prec, mode, att, c in u:
+            fn = "rk_launch_%s_%s%s_%d%d%d%d" % (prec[0], mode[5:].lower(), "_att" if att else "",
+                                                 *c)
+            decls.append((prec, mode, att, c, fn))
             lines.append("cudaError_t %s(const EriArgs& a, long long work, int nsm, "
                          "cudaStream_t st) {" % fn)
-            lines.append("  return rk_launch_one<%s, %d, %d, %d, %d, %s>(a, work, nsm, st);" %
-                         (prec, *c, mode))
+            lines.append("  return rk_launch_one<%s, %d, %d, %d, %d, %s, %s>(a, work, nsm, st);" %
+                         (prec, *c, mode, "true" if att else "false"))
             lines.append("}")
         lines.append("}  // namespace lgx")
         _write_if_changed(os.path.join(gen_dir, name), "\n".join(lines) + "\n")
     d = ["// GENERATED by libint_gb300/codegen/gen_rk.py -- do not edit.",
          "// Run-time dispatch of the register kernels.", '#include "../lgx_rk.cuh"', "",
          "namespace lgx {"]
-    for prec, mode, c, fn in decls:
+    for prec, mode, att, c, fn in decls:
         d.append("cudaError_t %s(const EriArgs& a, long long work, int nsm, cudaStream_t st);" % fn)
     d.append("")
-    d.append("// Launches the register kernel of (precision, mode, class); returns")
-    d.append("// cudaErrorNotSupported when that kernel is not compiled.")
-    d.append("cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, "
+    d.append("// Launches the register kernel of (precision, mode, operator, class);")
+    d.append("// returns cudaErrorNotSupported when that kernel is not compiled.")
+    d.append("cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int ld, "
              "const EriArgs& a, long long work, int nsm, cudaStream_t st) {")
-    d.append("  const int key = (((fp32 ? 1 : 0) * 8 + mode) * 4096) + ((la * 8 + lb) * 8 + lc) * 8 + ld;")
+    d.append("  const int key = ((((att ? 1 : 0) * 2 + (fp32 ? 1 : 0)) * 8 + mode) * 4096) + "
+             "((la * 8 + lb) * 8 + lc) * 8 + ld;")
     d.append("  switch (key) {")
-    for prec, mode, c, fn in sorted(decls, key=lambda x: x[3]):
+    for prec, mode, att, c, fn in sorted(decls, key=lambda x: x[4]):
         mode_id = {"kModeStore": 0, "kModeSchwarz": 1, "kModeJK": 2}[mode]
-        key = (((1 if prec == "float" else 0) * 8 + mode_id) * 4096) + ((c[0] * 8 + c[1]) * 8 + c[2]) * 8 + c[3]
+        key = ((((1 if att else 0) * 2 + (1 if prec == "float" else 0)) * 8 + mode_id) * 4096) + \
+            ((c[0] * 8 + c[1]) * 8 + c[2]) * 8 + c[3]
         d.append("    case %d: return %s(a, work, nsm, st);" % (key, fn))
     d.append("  }")
     d.append("  return cudaErrorNotSupported;")
     d.append("}")
     d.append("")
-    d.append("bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld) {")
+    d.append("bool rk_available(bool fp32, int mode, bool att, int la, int lb, int lc, int ld) {")
     d.append("  const int L = la + lb + lc + ld;")
+    d.append("  if (att) return mode == kModeJK && L <= %d;" % RK_MAX_L)
     d.append("  if (mode == kModeJK) return L <= %d;" % RK_MAX_L)
     d.append("  if (mode == kModeStore) return L <= %d;" % RK_MAX_L_STORE)
     d.append("  if (mode == kModeSchwarz) return !fp32 && L <= %d;" % RK_MAX_L_STORE)

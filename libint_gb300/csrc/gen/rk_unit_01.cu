@@ -3,15 +3,18 @@
 
 namespace lgx {
 cudaError_t rk_launch_d_jk_1032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 3, 2, kModeJK>(a, work, nsm, st);
+  return rk_launch_one<double, 1, 0, 3, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_1031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 3, 1, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_2031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_store_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 2, 0, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_1010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 1, 0, kModeSchwarz>(a, work, nsm, st);
+cudaError_t rk_launch_d_schwarz_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 2, 0, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

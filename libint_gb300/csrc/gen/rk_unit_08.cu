@@ -3,15 +3,30 @@
 
 namespace lgx {
 cudaError_t rk_launch_d_jk_3021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 3, 0, 2, 1, kModeJK>(a, work, nsm, st);
+  return rk_launch_one<double, 3, 0, 2, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_1021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 2, 1, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_att_1122(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 2, 2, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_store_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 1, 1, 1, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_att_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 2, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 1, 1, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_f_store_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 1, 1, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 1, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_store_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 0, 0, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_store_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 0, 0, kModeStore, false>(a, work, nsm, st);
 }
 }  // namespace lgx

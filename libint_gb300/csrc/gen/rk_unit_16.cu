@@ -3,21 +3,27 @@
 
 namespace lgx {
 cudaError_t rk_launch_f_jk_2121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 1, 2, 1, kModeJK>(a, work, nsm, st);
+  return rk_launch_one<float, 2, 1, 2, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_1021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 2, 1, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_0032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 1, 1, 1, kModeSchwarz>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 2, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 1, 1, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 1, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_store_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 1, 1, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_0022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 2, kModeStore, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 0, 0, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_0022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 2, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_store_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 1, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

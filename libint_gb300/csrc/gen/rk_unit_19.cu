@@ -3,18 +3,27 @@
 
 namespace lgx {
 cudaError_t rk_launch_f_jk_3030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 3, 0, 3, 0, kModeJK>(a, work, nsm, st);
+  return rk_launch_one<float, 3, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 1, 2, 0, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 0, 2, 0, kModeSchwarz>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_1130(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_store_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 3, 0, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 2, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 1, 1, kModeSchwarz>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 3, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_store_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 2, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 2, 0, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

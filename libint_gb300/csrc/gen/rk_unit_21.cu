@@ -2,19 +2,34 @@
 #include "../lgx_rk.cuh"
 
 namespace lgx {
-cudaError_t rk_launch_d_jk_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 2, 2, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 3, 2, kModeJK, true>(a, work, nsm, st);
 }
 cudaError_t rk_launch_d_jk_2021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 0, 2, 1, kModeJK>(a, work, nsm, st);
+  return rk_launch_one<double, 2, 0, 2, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 2, 0, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_2030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 2, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_0031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 3, 1, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_0031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 3, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 3, 0, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 0, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_schwarz_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 0, kModeSchwarz, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 0, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_1010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 1, 0, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_1010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 1, 0, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

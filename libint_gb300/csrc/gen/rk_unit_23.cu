@@ -2,19 +2,34 @@
 #include "../lgx_rk.cuh"
 
 namespace lgx {
-cudaError_t rk_launch_d_jk_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 1, 2, 1, kModeJK>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1131(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 3, 1, kModeJK, true>(a, work, nsm, st);
 }
 cudaError_t rk_launch_f_jk_0032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 3, 2, kModeJK>(a, work, nsm, st);
+  return rk_launch_one<float, 0, 0, 3, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_store_0031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 3, 1, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 2, 2, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 3, 0, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 2, 0, kModeStore>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 2, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 2, 0, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_schwarz_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 1, 1, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_store_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 0, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

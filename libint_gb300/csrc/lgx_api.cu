@@ -29,9 +29,9 @@ size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
 cudaError_t launch_prim_set(const PrimSetArgs& a, size_t smem, cudaStream_t st);
-cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
+cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int ld, const EriArgs& a,
                       long long work, int nsm, cudaStream_t st);
-bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
+bool rk_available(bool fp32, int mode, bool att, int la, int lb, int lc, int ld);
 cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
                               PrimPairJK32* out, cudaStream_t st);
 cudaError_t post_launch(bool fp32, int la, int lb, int lc, int ld, const EriArgs& a, int grid,
@@ -672,8 +672,9 @@ void fill_common(const lgx_context* ctx, const BasisDev& B, EriArgs& a) {
 
 bool rk_eligible(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode,
                  bool fp32) {
-  if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0 || ctx->op != LGX_OP_COULOMB) return false;
-  return rk_available(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld);
+  if (!ctx->use_rk || !B.std_pure || P.host.deriv != 0) return false;
+  const bool att = ctx->op != LGX_OP_COULOMB;  // attenuated: J/K register kernels only
+  return rk_available(fp32, mode, att, P.host.la, P.host.lb, P.host.lc, P.host.ld);
 }
 
 int choose_group(double nq_avg) {
@@ -706,7 +707,8 @@ lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, boo
                   EriArgs a, long long nwork, int group) {
   fill_common(ctx, B, a);
   a.group = group;
-  CK(rk_launch(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, nwork, ctx->nsm,
+  CK(rk_launch(fp32, mode, a.op != LGX_OP_COULOMB, P.host.la, P.host.lb, P.host.lc, P.host.ld, a,
+               nwork, ctx->nsm,
                ctx->launch_stream ? ctx->launch_stream : ctx->stream));
   return LGX_OK;
 }

@@ -121,6 +121,49 @@ __device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, 
   }
 }
 
+// Attenuated operators (register kernels of the J/K passes): F holds
+// pfac F_m(T) on entry; with s = omega^2 / (omega^2 + rho) the core
+// integrals become (libint's erf_coulomb_gm_eval / erfc_coulomb_gm_eval,
+// include/libint2/boys.h:1913-1980)
+//   erf(omega r)/r :  s^{m+1/2} F_m(s T)
+//   erfc(omega r)/r:  F_m(T) - s^{m+1/2} F_m(s T)
+// (s T <= T, so the same Taylor grid serves).  omega = 0 gives zero (erf)
+// and the Coulomb integrals (erfc).
+template <int MMAX>
+__device__ __forceinline__ void rk_attenuate(const EriArgs& a, double T, double rho, double pfac,
+                                             double* F) {
+  if (!(a.omega2 > 0.0)) {
+    if (a.op == 1)
+#pragma unroll
+      for (int m = 0; m <= MMAX; ++m) F[m] = 0.0;
+    return;
+  }
+  const double s = a.omega2 / (a.omega2 + rho);
+  double G[MMAX + 1];
+  rk_boys<MMAX>(a.boys_tay, T * s, pfac, G);
+  double f = sqrt(s);
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m, f *= s) F[m] = a.op == 1 ? f * G[m] : F[m] - f * G[m];
+}
+
+template <int MMAX>
+__device__ __forceinline__ void rk_attenuate(const EriArgs& a, float T, float rho, float pfac,
+                                             float* F) {
+  const float w2 = float(a.omega2);
+  if (!(w2 > 0.0f)) {
+    if (a.op == 1)
+#pragma unroll
+      for (int m = 0; m <= MMAX; ++m) F[m] = 0.0f;
+    return;
+  }
+  const float s = w2 / (w2 + rho);
+  float G[MMAX + 1];
+  rk_boys<MMAX>(a.boys32, T * s, pfac, G);
+  float f = sqrtf(s);
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m, f *= s) F[m] = a.op == 1 ? f * G[m] : F[m] - f * G[m];
+}
+
 template <typename T>
 struct RkQuartet {
   int sh[4];
@@ -176,7 +219,7 @@ __device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, 
 // The ln-screen runs on the FP32 copies (it only decides whether a
 // primitive quartet below ~1e-16 contributes) and the pfac screen compares
 // the IEEE bit patterns, so neither costs an FP64 instruction.
-template <class C>
+template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double>& q, int ib,
                                         int ik, double* acc) {
   const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
@@ -194,6 +237,7 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double
   const double T = rho * fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
   double F[C::kMmax + 1];
   rk_boys<C::kMmax>(a.boys_tay, T, pfac, F);
+  if constexpr (ATT) rk_attenuate<C::kMmax>(a, T, rho, pfac, F);
   rk::Geo<double> g;
   const double ez = eta * oogpq, zz = zeta * oogpq;
   g.PAx = bp.P[0] - q.A[0]; g.PAy = bp.P[1] - q.A[1]; g.PAz = bp.P[2] - q.A[2];
@@ -234,7 +278,7 @@ __device__ __forceinline__ PrimF32 rk_pp32(const PrimPairRec& r, bool sw) {
 }
 
 // One primitive quartet into acc (FP32).  AC = A - C of the quartet.
-template <class C>
+template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>& q,
                                         const PrimF32& bp, const PrimF32& kp, float* acc) {
   if (!(bp.k.w + kp.k.w > a.fln_prec)) return false;
@@ -252,6 +296,7 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
   const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
   float F[C::kMmax + 1];
   rk_boys<C::kMmax>(a.boys32, T, pfac, F);
+  if constexpr (ATT) rk_attenuate<C::kMmax>(a, T, rho, pfac, F);
   rk::Geo<float> g;
   const float ez = eta * oogpq, zz = zeta * oogpq;
   g.PAx = PA[0]; g.PAy = PA[1]; g.PAz = PA[2];
@@ -286,7 +331,9 @@ __device__ __forceinline__ float rk_D(const EriArgs& a, size_t i, float*) {
   return __ldg(a.Df + i);
 }
 
-template <typename T, int LA, int LB, int LC, int LD, int MODE>
+// ATT: attenuated operator (erf / erfc, EriArgs::op), J/K mode only; the
+// Coulomb instances (ATT = false) carry none of its code.
+template <typename T, int LA, int LB, int LC, int LD, int MODE, bool ATT = false>
 __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
   using C = rk::Cls<LA, LB, LC, LD>;
   constexpr int N0 = C::kN0, N1 = C::kN1, N2 = C::kN2, N3 = C::kN3;
@@ -357,9 +404,9 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
                                : rk_pp32(a.pprims[q.bra_pp + ib], q.bsw);
         const PrimF32 kp = rec ? rk_rec32(a.jk32 + krec.x + ik * krec.y)
                                : rk_pp32(a.pprims[q.ket_pp + ik], q.ksw);
-        kept += rk_prim<C>(a, q, bp, kp, acc) ? 1 : 0;
+        kept += rk_prim<C, ATT>(a, q, bp, kp, acc) ? 1 : 0;
       } else {
-        kept += rk_prim<C>(a, q, ib, ik, acc) ? 1 : 0;
+        kept += rk_prim<C, ATT>(a, q, ib, ik, acc) ? 1 : 0;
       }
       ib += gb;
       ik += gk;
@@ -534,10 +581,10 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
 }
 
 // Launch of one register kernel: occupancy-sized grid, capped by the work.
-template <typename T, int LA, int LB, int LC, int LD, int MODE>
+template <typename T, int LA, int LB, int LC, int LD, int MODE, bool ATT = false>
 cudaError_t rk_launch_one(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   const int block = 128;
-  auto k = rk_kernel<T, LA, LB, LC, LD, MODE>;
+  auto k = rk_kernel<T, LA, LB, LC, LD, MODE, ATT>;
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, block, 0) != cudaSuccess || occ < 1)
     occ = 1;
@@ -549,8 +596,8 @@ cudaError_t rk_launch_one(const EriArgs& a, long long work, int nsm, cudaStream_
   return cudaGetLastError();
 }
 
-cudaError_t rk_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
-                      long long work, int nsm, cudaStream_t st);
-bool rk_available(bool fp32, int mode, int la, int lb, int lc, int ld);
+cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int ld,
+                      const EriArgs& a, long long work, int nsm, cudaStream_t st);
+bool rk_available(bool fp32, int mode, bool att, int la, int lb, int lc, int ld);
 
 }  // namespace lgx

@@ -2,7 +2,9 @@
 (Operator::erf_coulomb / erfc_coulomb with omega as params) on the CUDA
 path against the oracle's restatement of libint's core integrals:
 shell sets at deriv 0 and 1 through Engine, the identity erf + erfc =
-coulomb, and Schwarz-screened J/K builds (FP64 and mixed) with erfc."""
+coulomb, and Schwarz-screened J/K builds (FP64 and mixed) with erf and erfc
+(their small classes on the attenuated register kernels, the rest on the
+attenuated program kernel)."""
 import numpy as np
 import pytest
 
@@ -47,16 +49,19 @@ def test_engine_erf_erfc_vs_oracle(lgx, oracle_op):
             assert np.max(np.abs(a + b - c)) < 1e-12
 
 
-def test_jk_erfc_vs_oracle(lgx, oracle_op):
+@pytest.mark.parametrize("oper", ["erf", "erfc"])
+def test_jk_attenuated_vs_oracle(lgx, oracle_op, oper):
     atoms = lgx.water_cluster(2, 1, 1, spacing=3.0, jitter=0.2, seed=1)
     bs = lgx.BasisSet("cc-pVDZ", atoms)
     ob = oracle_op.OracleBasis.from_basis(bs)
     D = lgx.random_density(bs.nbf, 10, seed=2)
     ctx = lgx.Context(0)
     ctx.set_basis(bs)
-    ctx.set_operator(lgx.Operator.erfc_coulomb, OMEGA)
+    op, code = ((lgx.Operator.erf_coulomb, 1) if oper == "erf"
+                else (lgx.Operator.erfc_coulomb, 2))
+    ctx.set_operator(op, OMEGA)
     Kq = ctx.schwarz()
-    oracle_op.set_operator(2, OMEGA)
+    oracle_op.set_operator(code, OMEGA)
     assert np.max(np.abs(Kq - oracle_op.schwarz(ob))) < 1e-12
     J, K, st = ctx.jk(D, 1e-12)
     Jr, Kr, nq = oracle_op.jk(ob, D, Kq, 1e-12)
