@@ -555,6 +555,13 @@ def run_rows(args):
     t_gpu = (time.perf_counter() - t0) / reps
     sz = np.array([sh.size() for sh in full], np.int64)
     nint = int((sz[q[:, 0]] * sz[q[:, 2]] * sz[q[:, 3]]).sum())
+    # the same tensors left in HBM (lgx_compute_batch_device)
+    dout = torch.empty(int(offs[-1]) + nint, dtype=torch.float64, device="cuda")
+    ctx.compute_batch_device(q, dout.data_ptr(), dout.numel(), offsets=offs)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.compute_batch_device(q, dout.data_ptr(), dout.numel(), offsets=offs)
+    t_dev = (time.perf_counter() - t0) / reps
     ob = oracle.OracleBasis.from_basis(full)
     t0 = time.perf_counter()
     oracle.compute_batch(ob, q, offs, int(offs[-1] + nint), nthreads=0)
@@ -562,8 +569,11 @@ def run_rows(args):
     rows["f2_df_tensors"] = {
         "workload": "(H2O)8 cc-pVDZ / cc-pVDZ-jkfit: every (P|ab) and (P|Q)",
         "quartets": len(q), "integrals": nint, "ms": 1e3 * t_gpu, "eri_per_s": nint / t_gpu,
+        "device_ms": 1e3 * t_dev, "device_eri_per_s": nint / t_dev,
         "oracle_ms": 1e3 * t_cpu, "oracle_eri_per_s": nint / t_cpu, "oracle_cores": cores,
-        "note": "lgx_compute_batch, FP64, host output buffer (copy timed)"}
+        "note": "lgx_compute_batch, FP64: ms with the host output buffer (copy timed), "
+                "device_ms with the tensors left in HBM (lgx_compute_batch_device); "
+                "oracle output in host memory"}
     ctx.close()
 
     # second derivatives: per-call shell sets through the Engine entry

@@ -191,6 +191,16 @@ lgx_status lgx_compute_batch(lgx_context* ctx, const int32_t* quartets,
                              double mixed_thresh, const int64_t* offsets,
                              double* out, size_t out_capacity,
                              int32_t* is_null);
+/* lgx_compute_batch with the sets left in HBM: `d_out` (out_capacity
+ * doubles) and `d_is_null` (optional, n ints) are DEVICE memory of the
+ * context's GPU; quartets and offsets stay host arrays.  For callers that
+ * contract the integrals on the GPU next (density fitting: the 3-centre
+ * tensor and the metric), so no host copy is made.  Returns after the
+ * kernels have finished. */
+lgx_status lgx_compute_batch_device(lgx_context* ctx, const int32_t* quartets, int64_t n,
+                                    int deriv, int mode, double mixed_thresh,
+                                    const int64_t* offsets, double* d_out, size_t out_capacity,
+                                    int32_t* d_is_null);
 
 /* Statistics of one J/K (or gradient) pass. */
 typedef struct {

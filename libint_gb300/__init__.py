@@ -364,6 +364,32 @@ class Context:
         self._check(st, "lgx_compute_batch")
         return out, offs, isnull[:len(q)]
 
+    def compute_batch_device(self, quartets, d_out, out_capacity, deriv=0, mode=_lgx.LGX_FP64,
+                             mixed_thresh=1e-4, offsets=None, d_is_null=0):
+        """compute_batch with the sets left in device memory: d_out is the
+        address of out_capacity doubles on the context's GPU (e.g. a torch
+        tensor's data_ptr()), d_is_null optionally that of len(quartets)
+        int32.  Returns the offsets (computed as in compute_batch when not
+        given)."""
+        q = np.ascontiguousarray(quartets, dtype=np.int32).reshape(-1, 4)
+        if q.size and (q.min() < 0 or q.max() >= len(self.basis)):
+            raise LgxError(_lgx.LGX_ERR_INVALID_ARG, "quartet shell index out of range")
+        if offsets is None:
+            sizes = np.array([s.size() for s in self.basis], np.int64)
+            nv = (sizes[q[:, 0]] * sizes[q[:, 1]] * sizes[q[:, 2]] * sizes[q[:, 3]] *
+                  (12 if deriv else 1))
+            offsets = np.zeros(len(q), np.int64)
+            if len(q):
+                offsets[1:] = np.cumsum(nv)[:-1]
+        offsets = np.ascontiguousarray(offsets, np.int64)
+        st = self._lib.lgx_compute_batch_device(self._h, _lgx.ptr(q, ctypes.c_int32), len(q),
+                                                int(deriv), int(mode), float(mixed_thresh),
+                                                _lgx.ptr(offsets, ctypes.c_int64),
+                                                ctypes.c_void_p(int(d_out)), int(out_capacity),
+                                                ctypes.c_void_p(int(d_is_null) or None))
+        self._check(st, "lgx_compute_batch_device")
+        return offsets
+
     def jk(self, D, schwarz_thresh=1e-12, mode=_lgx.LGX_FP64, mixed_thresh=1e-4):
         n = self.basis.nbf
         D = np.ascontiguousarray(D, dtype=float)

@@ -109,6 +109,10 @@ SIGNATURES = {
     "lgx_compute_batch": (ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.c_int64, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_double, _i64p, _dp,
                                          ctypes.c_size_t, _ip]),
+    "lgx_compute_batch_device": (ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.c_int64, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_double, _i64p,
+                                                ctypes.c_void_p, ctypes.c_size_t,
+                                                ctypes.c_void_p]),
     "lgx_jk": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int,
                               ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
     "lgx_jk_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -248,6 +248,7 @@ struct lgx_context {
   DBuf items, out, isnull;
   DBuf Jacc, Kacc, Dd, Jd, Kd, gJ, gK;
   DBuf prim_rows, prim_slots;  // lgx_compute_primitive_set
+  DBuf xcounters;              // explicit lists: one work counter per class launch
   PinnedBuf pin_in, pin_out;
   BinCache bins;
   std::mutex mu;
@@ -836,13 +837,44 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
   }
   CK(cudaMemcpyAsync(ctx->items.p, all.data(), total * sizeof(QuartetItem),
                      cudaMemcpyHostToDevice, ctx->stream));
+  // the class launches run on parallel branches (streams forked from and
+  // joined back into ctx->stream, one work counter and one program-kernel
+  // slot scratch per launch / branch): a short list, such as the raised and
+  // lowered quartets of a second-derivative set, then costs its slowest
+  // class rather than the sum of its classes
+  const int ng = int(groups.size());
+  const int nbr = std::min(ng, lgx_context::kMaxBranches);
+  const bool split = ctx->overlap && nbr > 1;
+  CK(ctx->xcounters.ensure(size_t(ng) * sizeof(unsigned long long)));
+  CK(cudaMemsetAsync(ctx->xcounters.p, 0, size_t(ng) * sizeof(unsigned long long), ctx->stream));
+  if (split) {
+    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+    for (int b = 0; b < nbr; ++b) {
+      CK(cudaStreamWaitEvent(ctx->s64[b], ctx->ev_fork, 0));
+      CK(cudaStreamWaitEvent(ctx->s32[b], ctx->ev_fork, 0));
+    }
+  }
+  struct Restore {  // launch stream / scratch back to the context defaults
+    lgx_context* c;
+    ~Restore() {
+      c->launch_stream = nullptr;
+      c->scratch = nullptr;
+    }
+  } restore{ctx};
   size_t gi = 0;
+  lgx_status s = LGX_OK;
   for (auto& kv : groups) {
     ProgDev* P = nullptr;
-    lgx_status s = get_prog(ctx, kv.second.la, kv.second.lb, kv.second.lc, kv.second.ld,
-                            deriv, &P);
-    if (s != LGX_OK) return s;
+    s = get_prog(ctx, kv.second.la, kv.second.lb, kv.second.lc, kv.second.ld, deriv, &P);
+    if (s != LGX_OK) break;
+    const bool fp32 = kv.second.fp32;
+    if (split) {
+      const int b = int(gi) % nbr;
+      ctx->launch_stream = fp32 ? ctx->s32[b] : ctx->s64[b];
+      ctx->scratch = (fp32 || b > 0) ? &ctx->gscratch_br[(fp32 ? nbr : 0) + b] : &ctx->gscratch;
+    }
     EriArgs a{};
+    a.counter = ctx->xcounters.as<unsigned long long>() + gi;
     a.precision = precision;
     a.ln_prec = precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
     a.screening = screening;
@@ -856,11 +888,19 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
     for (const auto& it : kv.second.items)
       nq += double(B.hpairs[it.bra_pair].npp) * double(B.hpairs[it.ket_pair].npp);
     nq /= std::max<size_t>(1, kv.second.items.size());
-    s = run_eri(ctx, B, *P, mode, kv.second.fp32, a, a.nitems, nq);
-    if (s != LGX_OK) return s;
+    s = run_eri(ctx, B, *P, mode, fp32, a, a.nitems, nq);
+    if (s != LGX_OK) break;
     ++gi;
   }
-  return LGX_OK;
+  if (split) {  // joined on every path, so ctx->stream orders after all branch work
+    for (int b = 0; b < nbr; ++b) {
+      CK(cudaEventRecord(ctx->ev_join[2 * b], ctx->s64[b]));
+      CK(cudaEventRecord(ctx->ev_join[2 * b + 1], ctx->s32[b]));
+      CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[2 * b], 0));
+      CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[2 * b + 1], 0));
+    }
+  }
+  return s;
 }
 
 lgx_status ensure_schwarz(lgx_context* ctx, BasisDev& B) {
@@ -2042,9 +2082,13 @@ lgx_status lgx_schwarz(lgx_context* ctx, double* K) {
   return LGX_OK;
 }
 
-lgx_status lgx_compute_batch(lgx_context* ctx, const int32_t* quartets, int64_t n, int deriv,
-                             int mode, double mixed_thresh, const int64_t* offsets, double* out,
-                             size_t out_capacity, int32_t* is_null) {
+// lgx_compute_batch / lgx_compute_batch_device: `out` / `is_null` are host
+// memory (copied from the context's buffers) or, for `device_out`, device
+// memory the kernels write directly.
+static lgx_status compute_batch(lgx_context* ctx, const int32_t* quartets, int64_t n,
+                                int deriv, int mode, double mixed_thresh, const int64_t* offsets,
+                                double* out, size_t out_capacity, int32_t* is_null,
+                                bool device_out) {
   if (!ctx) return LGX_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!quartets || n < 0 || !out) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
@@ -2075,20 +2119,43 @@ lgx_status lgx_compute_batch(lgx_context* ctx, const int32_t* quartets, int64_t 
   const double eps = std::numeric_limits<double>::epsilon();
   s = ensure_pairs(ctx, B, std::log(eps), 0);
   if (s != LGX_OK) return s;
-  CK(ctx->out.ensure(std::max<size_t>(need, 1) * sizeof(double)));
-  CK(ctx->isnull.ensure(std::max<int64_t>(n, 1) * sizeof(int)));
-  CK(cudaMemsetAsync(ctx->out.p, 0, std::max<size_t>(need, 1) * sizeof(double), ctx->stream));
+  double* d_out = out;
+  int* d_isnull = reinterpret_cast<int*>(is_null);
+  if (!device_out) {
+    CK(ctx->out.ensure(std::max<size_t>(need, 1) * sizeof(double)));
+    d_out = ctx->out.as<double>();
+  }
+  if (!device_out || !is_null) {
+    CK(ctx->isnull.ensure(std::max<int64_t>(n, 1) * sizeof(int)));
+    d_isnull = ctx->isnull.as<int>();
+  }
+  CK(cudaMemsetAsync(d_out, 0, std::max<size_t>(need, 1) * sizeof(double), ctx->stream));
   s = run_explicit(ctx, B, quartets, n, deriv, kModeStore,
-                   mode == LGX_MIXED ? mixed_thresh : 0.0, offsets, ctx->out.as<double>(),
-                   ctx->isnull.as<int>(), eps, 0, nullptr);
+                   mode == LGX_MIXED ? mixed_thresh : 0.0, offsets, d_out, d_isnull, eps, 0,
+                   nullptr);
   if (s != LGX_OK) return s;
-  CK(cudaMemcpyAsync(out, ctx->out.p, need * sizeof(double), cudaMemcpyDeviceToHost,
-                     ctx->stream));
-  if (is_null)
-    CK(cudaMemcpyAsync(is_null, ctx->isnull.p, n * sizeof(int), cudaMemcpyDeviceToHost,
-                       ctx->stream));
+  if (!device_out) {
+    CK(cudaMemcpyAsync(out, d_out, need * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (is_null)
+      CK(cudaMemcpyAsync(is_null, d_isnull, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   return check_errflag(ctx);
+}
+
+lgx_status lgx_compute_batch(lgx_context* ctx, const int32_t* quartets, int64_t n, int deriv,
+                             int mode, double mixed_thresh, const int64_t* offsets, double* out,
+                             size_t out_capacity, int32_t* is_null) {
+  return compute_batch(ctx, quartets, n, deriv, mode, mixed_thresh, offsets, out, out_capacity,
+                       is_null, false);
+}
+
+lgx_status lgx_compute_batch_device(lgx_context* ctx, const int32_t* quartets, int64_t n,
+                                    int deriv, int mode, double mixed_thresh,
+                                    const int64_t* offsets, double* d_out, size_t out_capacity,
+                                    int32_t* d_is_null) {
+  return compute_batch(ctx, quartets, n, deriv, mode, mixed_thresh, offsets, d_out, out_capacity,
+                       d_is_null, true);
 }
 
 lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double* dK,

@@ -66,12 +66,20 @@ def test_df_tensors_batched_vs_oracle(lgx, oracle_mod):
     q2 = np.array([(p, u, r, u) for p in P for r in P if r <= p], np.int32)
     ob = oracle_mod.OracleBasis.from_basis(full)
     sz = np.array([s.size() for s in full], np.int64)
+    import torch
     for q in (q3, q2):
         out, offs, isnull = ctx.compute_batch(q)
         nv = sz[q[:, 0]] * sz[q[:, 1]] * sz[q[:, 2]] * sz[q[:, 3]]
         ref, risnull = oracle_mod.compute_batch(ob, q, offs, int(nv.sum()))
         assert np.array_equal(isnull, risnull)
         assert np.max(np.abs(out[:nv.sum()] - ref[:nv.sum()])) < 1e-12
+        # the same sets left in HBM (lgx_compute_batch_device): bit-identical
+        d = torch.full((int(nv.sum()),), float("nan"), dtype=torch.float64, device="cuda")
+        dn = torch.full((len(q),), -1, dtype=torch.int32, device="cuda")
+        offs_d = ctx.compute_batch_device(q, d.data_ptr(), d.numel(), d_is_null=dn.data_ptr())
+        assert np.array_equal(offs_d, offs)
+        assert np.array_equal(d.cpu().numpy(), out[:nv.sum()])
+        assert np.array_equal(dn.cpu().numpy(), isnull)
     # assemble (P|ab) and (P|Q); DF Coulomb energy vs the exact one
     nbf, naux = obs.nbf, dfbs.nbf
     off_o, off_a = obs.shell2bf(), dfbs.shell2bf()
