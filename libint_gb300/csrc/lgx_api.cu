@@ -29,6 +29,7 @@ size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
 cudaError_t launch_prim_set(const PrimSetArgs& a, size_t smem, cudaStream_t st);
+cudaError_t launch_eri_block_store(const EriArgs& a, int grid, size_t smem, cudaStream_t st);
 cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int ld, const EriArgs& a,
                       long long work, int nsm, cudaStream_t st);
 bool rk_available(bool fp32, int mode, bool att, int la, int lb, int lc, int ld);
@@ -714,11 +715,41 @@ lgx_status run_rk(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, boo
   return LGX_OK;
 }
 
+// Short explicit FP64 store lists (at most one quartet per SM): one block
+// of kBlockThreads per quartet (eri_block_store_kernel), the slots in shared
+// memory when they fit, else in per-block global scratch.
+lgx_status run_block_store(lgx_context* ctx, BasisDev& B, const ProgDev& P, EriArgs a,
+                           long long nwork) {
+  fill_common(ctx, B, a);
+  a.prog = P.dev;
+  a.stage_rows = 32;
+  a.slot_stride = (P.host.total_slots() + 1) & ~1;
+  const size_t stage = stage_bytes_per_warp(false, a.stage_rows);
+  const size_t slot_bytes = size_t(a.slot_stride) * sizeof(double);
+  const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
+  const int grid = int(std::max<long long>(1, nwork));
+  size_t smem = stage + slot_bytes;
+  a.global_slots = 0;
+  if (smem > smem_cap) {
+    DBuf& scr = ctx->scratch ? *ctx->scratch : ctx->gscratch;
+    if (ctx->noalloc && scr.n < size_t(grid) * slot_bytes)
+      return fail(ctx, LGX_ERR_INVALID_ARG, "slot scratch not prepared");
+    if (!ctx->noalloc) CK(scr.ensure(size_t(grid) * slot_bytes));
+    a.gscratch = scr.p;
+    a.global_slots = 1;
+    smem = stage;
+  }
+  CK(launch_eri_block_store(a, grid, smem, ctx->launch_stream ? ctx->launch_stream : ctx->stream));
+  return LGX_OK;
+}
+
 lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bool fp32,
                    EriArgs a, long long nwork, double nq_avg = 1.0,
                    const Variant* var = nullptr) {
   const Variant v = var ? *var : default_variant(ctx, B, P, mode, fp32, a.implicit, nq_avg);
   if (v.kind == 0) return run_rk(ctx, B, P, mode, fp32, a, nwork, v.group);
+  if (v.kind == 1 && mode == kModeStore && !fp32 && !a.implicit && nwork <= ctx->nsm)
+    return run_block_store(ctx, B, P, a, nwork);
   const bool gen = v.kind == 2;
   Launch L;
   lgx_status s = plan_launch(ctx, P, mode, fp32, nwork, nq_avg, v.rows, gen, L);

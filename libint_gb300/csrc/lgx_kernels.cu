@@ -191,27 +191,28 @@ cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t 
 // caller fills the Libint_t prefactors and (00|00)^(m) of every primitive
 // quartet, engine.impl.h:1389-1757, and the library contracts them,
 // dg.cc:1177-1189).  The host packs the rows in the canonical orientation;
-// one warp stages them in batches, runs the class's VRR program and post
-// program, and stores the Cartesian sets in the caller's shell order, the
+// the block stages them in batches of stage_rows (<= 32), runs the class's
+// VRR program and post program with every level spread over all its
+// threads, and stores the Cartesian sets in the caller's shell order, the
 // derivative sets of centre C by translational invariance.
-__global__ void __launch_bounds__(32) prim_set_kernel(PrimSetArgs a) {
+__global__ void __launch_bounds__(kBlockThreads) prim_set_kernel(PrimSetArgs a) {
   extern __shared__ double smem_d[];
-  const int lane = threadIdx.x & 31;
+  const int tid = threadIdx.x, nt = blockDim.x;
   const DevProg& P = a.prog;
   const int R = a.stage_rows;
   double* stage = smem_d;
   double* ktab = stage + R * kStage;
   double* slots = a.slots ? a.slots : smem_d + ((R * kStage + kKtab + 3) & ~3);
-  for (int i = lane; i < P.nacc; i += 32) slots[i] = 0.0;
-  __syncwarp();
+  for (int i = tid; i < P.nacc; i += nt) slots[i] = 0.0;
+  __syncthreads();
   for (int base = 0; base < a.nrows; base += R) {
     const int n = min(R, a.nrows - base);
     const double* src = a.rows + (size_t)base * kStage;
-    for (int i = lane; i < n * kStage; i += 32) stage[i] = src[i];
-    __syncwarp();
+    for (int i = tid; i < n * kStage; i += nt) stage[i] = src[i];
+    __syncthreads();
     const unsigned ballot = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
-    vrr_consume<double>(P, stage, ballot, slots, ktab, lane);
-    __syncwarp();
+    vrr_consume<double, BlockGrp>(P, stage, ballot, slots, ktab, tid);
+    __syncthreads();
   }
   QuartetGeom<double> g;
   for (int x = 0; x < 3; ++x) {
@@ -233,33 +234,137 @@ __global__ void __launch_bounds__(32) prim_set_kernel(PrimSetArgs a) {
     return ((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3];
   };
   for (int ph = 0; ph < P.nphases; ++ph) {
-    run_post_phase<double>(P, ph, g, slots, lane);
+    run_post_phase<double, BlockGrp>(P, ph, g, slots, tid);
     const int ctr = P.deriv ? (ph == 0 ? 0 : (ph == 1 ? 1 : 3)) : 0;
     for (int s = 0; s < P.sets_per_phase; ++s) {
       const double* cart = slots + P.cart_out + s * n4;
       double* cb = slots + P.cbuf + s * n4;
       double* o = a.out + (size_t)(P.deriv ? a.perm[ctr] * 3 + s : 0) * n4;
-      for (int e = lane; e < n4; e += 32) {
+      for (int e = tid; e < n4; e += nt) {
         o[caller_index(e)] = cart[e];
         if (P.deriv) cb[e] = (ph == 0 ? 0.0 : cb[e]) - cart[e];
       }
-      __syncwarp();
+      __syncthreads();
       if (P.deriv && ph == P.nphases - 1) {
         double* oc = a.out + (size_t)(a.perm[2] * 3 + s) * n4;
-        for (int e = lane; e < n4; e += 32) oc[caller_index(e)] = cb[e];
-        __syncwarp();
+        for (int e = tid; e < n4; e += nt) oc[caller_index(e)] = cb[e];
+        __syncthreads();
       }
     }
   }
 }
 
-// One warp; smem = staging (stage_bytes_per_warp) + the slots when they
-// live in shared memory (a.slots == nullptr).
+// Store mode for short explicit lists (a few quartets, e.g. one shell set
+// or the raised / lowered quartets of a second-derivative set): one block
+// per contracted quartet instead of one warp, so a single quartet's VRR
+// and post-program levels, transform and store are spread over all the
+// block's threads.  Warp 0 runs the primitive-quartet prologues (<= 32
+// staged rows per batch, ballot-compacted as in the warp kernel).  FP64;
+// ATT: attenuated operator.  Same output layout as eri_warp_kernel's store.
+template <bool ATT>
+__global__ void __launch_bounds__(kBlockThreads) eri_block_store_kernel(EriArgs a) {
+  extern __shared__ double smem_d[];
+  __shared__ unsigned s_ballot;
+  __shared__ int s_kept;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const DevProg& P = a.prog;
+  const int R = a.stage_rows;
+  double* stage = smem_d;
+  double* ktab = stage + R * kStage;
+  double* slots = a.global_slots
+                      ? reinterpret_cast<double*>(a.gscratch) + size_t(blockIdx.x) * a.slot_stride
+                      : smem_d + ((R * kStage + kKtab + 3) & ~3);
+  for (long long q = blockIdx.x; q < a.nitems; q += gridDim.x) {
+    const QuartetItem it = a.items[q];
+    QuartetGeom<double> g;
+    load_geom<double>(a, it.bra_pair, it.ket_pair, it.flags & 1, (it.flags >> 1) & 1, g);
+    for (int i = tid; i < P.nacc; i += nt) slots[i] = 0.0;
+    if (tid == 0) s_kept = 0;
+    __syncthreads();
+    const int nq = g.nbpp * g.nkpp;
+    const double npbraket = double(nq);
+    for (int base = 0; base < nq; base += R) {
+      if (tid < 32) {
+        bool keep = false;
+        if (tid < R && base + tid < nq)
+          keep = prologue<ATT>(a, g, base + tid, npbraket, stage + tid * kStage);
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if (tid == 0) {
+          s_ballot = b;
+          s_kept += __popc(b);
+        }
+      }
+      __syncthreads();
+      vrr_consume<double, BlockGrp>(P, stage, s_ballot, slots, ktab, tid);
+      __syncthreads();
+    }
+    const int kept = s_kept;
+    if (a.is_null && tid == 0) a.is_null[it.pad] = kept == 0 ? 1 : 0;
+    if (kept == 0) continue;  // block-uniform
+    const int lsh[4] = {P.la, P.lb, P.lc, P.ld};
+    int pure[4];
+    for (int t = 0; t < 4; ++t) pure[t] = a.basis.pure[g.sh[t]];
+    const int fl = it.flags >> 2;
+    const bool sbk = fl & 1, stb = (fl >> 1) & 1, stk = (fl >> 2) & 1;
+    int perm[4];
+    perm[0] = sbk ? (stk ? 3 : 2) : (stb ? 1 : 0);
+    perm[1] = sbk ? (stk ? 2 : 3) : (stb ? 0 : 1);
+    perm[2] = sbk ? (stb ? 1 : 0) : (stk ? 3 : 2);
+    perm[3] = sbk ? (stb ? 0 : 1) : (stk ? 2 : 3);
+    for (int ph = 0; ph < P.nphases; ++ph) {
+      run_post_phase<double, BlockGrp>(P, ph, g, slots, tid);
+      const int ctr = P.deriv ? (ph == 0 ? 0 : (ph == 1 ? 1 : 3)) : 0;
+      for (int s = 0; s < P.sets_per_phase; ++s) {
+        int dims[4] = {ncart_of(P.la), ncart_of(P.lb), ncart_of(P.lc), ncart_of(P.ld)};
+        double* cart = slots + P.cart_out + s * P.ncart4;
+        const double* V =
+            sph_transform<double, BlockGrp>(a, lsh, pure, dims, cart, slots + P.sph_tmp, tid);
+        const int nsph4 = dims[0] * dims[1] * dims[2] * dims[3];
+        int tn[4];
+        for (int t = 0; t < 4; ++t) tn[perm[t]] = dims[t];
+        auto caller_index = [&](int e) {
+          int ci[4];
+          int r = e;
+          ci[3] = r % dims[3]; r /= dims[3];
+          ci[2] = r % dims[2]; r /= dims[2];
+          ci[1] = r % dims[1]; ci[0] = r / dims[1];
+          int ix[4];
+          for (int t = 0; t < 4; ++t) ix[perm[t]] = ci[t];
+          return ((ix[0] * tn[1] + ix[1]) * tn[2] + ix[2]) * tn[3] + ix[3];
+        };
+        const int ts = P.deriv ? perm[ctr] * 3 + s : 0;
+        double* o = a.out + it.out + (size_t)ts * nsph4;
+        double* cb = slots + P.cbuf + s * P.ncart4;
+        for (int e = tid; e < nsph4; e += nt) {
+          o[caller_index(e)] = V[e];
+          if (P.deriv) cb[e] = (ph == 0 ? 0.0 : cb[e]) - V[e];
+        }
+        __syncthreads();
+        if (P.deriv && ph == P.nphases - 1) {
+          double* oc = a.out + it.out + (size_t)(perm[2] * 3 + s) * nsph4;
+          for (int e = tid; e < nsph4; e += nt) oc[caller_index(e)] = cb[e];
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+cudaError_t launch_eri_block_store(const EriArgs& a, int grid, size_t smem, cudaStream_t st) {
+  auto k = a.op != 0 ? eri_block_store_kernel<true> : eri_block_store_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, kBlockThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// One block of kBlockThreads; smem = staging (stage_bytes_per_warp) + the
+// slots when they live in shared memory (a.slots == nullptr).
 cudaError_t launch_prim_set(const PrimSetArgs& a, size_t smem, cudaStream_t st) {
   cudaError_t e =
       cudaFuncSetAttribute(prim_set_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  prim_set_kernel<<<1, 32, smem, st>>>(a);
+  prim_set_kernel<<<1, kBlockThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 

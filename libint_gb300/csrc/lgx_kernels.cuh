@@ -60,6 +60,10 @@ constexpr int kStPA = 16, kStWP = 19, kStQC = 22, kStWQ = 25;
 constexpr int kStOo2z = 28, kStRoz = 29, kStOo2e = 30, kStRoe = 31, kStOo2ze = 32;
 constexpr int kStW = 33;          // 2 alpha_A, 2 alpha_B, 2 alpha_D
 
+// Threads of the block-cooperative single-quartet kernels (prim_set_kernel,
+// eri_block_store_kernel).
+constexpr int kBlockThreads = 256;
+
 // One contracted Cartesian shell set from staged primitive quartets in the
 // canonical orientation (prim_set_kernel).
 struct PrimSetArgs {
@@ -96,7 +100,7 @@ struct EriArgs {
   float fprecision, fln_prec;
   int screening;  // 0 Original, 1 Conservative
   // two-body operator: 0 coulomb 1/r, 1 erf(omega r)/r, 2 erfc(omega r)/r
-  // (program kernel only; the register kernels serve coulomb)
+  // (attenuated: program kernel instantiations and the ATT register kernels)
   int op;
   double omega2;  // omega^2
   // work

@@ -345,10 +345,24 @@ __device__ __forceinline__ PostOp load_post_op(const DevProg& P, int op) {
   return o;
 }
 
+// Thread-group policies of the program-execution helpers below: one warp
+// (the program kernel runs a quartet per warp) or the whole block (the
+// single-quartet kernels of short explicit lists and caller-supplied
+// primitive data, which spread one quartet's program levels over all the
+// block's threads).  `lane` is the thread's rank in the group.
+struct WarpGrp {
+  static __device__ __forceinline__ constexpr int size() { return 32; }
+  static __device__ __forceinline__ void sync() { __syncwarp(); }
+};
+struct BlockGrp {
+  static __device__ __forceinline__ int size() { return int(blockDim.x); }
+  static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+
 // Step 2 for the staged primitive quartets of `ballot` (rows of `stage`):
 // the class's VRR program, level by level, and the accumulation of its
 // (e0|f0) targets into the contracted slots.
-template <typename T>
+template <typename T, class Grp = WarpGrp>
 __device__ __forceinline__ void vrr_consume(const DevProg& P, const T* __restrict__ stage,
                                             unsigned ballot, T* __restrict__ slots,
                                             T* __restrict__ ktab, int lane) {
@@ -363,10 +377,10 @@ __device__ __forceinline__ void vrr_consume(const DevProg& P, const T* __restric
     const T oo2e = st[kStOo2e], roe = st[kStRoe];
     const T oo2ze = st[kStOo2ze];
     const T w1 = st[kStW], w2 = st[kStW + 1], w3 = st[kStW + 2];
-    for (int m = lane; m <= P.mmax; m += 32) slots[P.leaf_slot0 + m] = st[kStF + m];
+    for (int m = lane; m <= P.mmax; m += Grp::size()) slots[P.leaf_slot0 + m] = st[kStF + m];
     if (lane < kKtab)
       ktab[lane] = small_int<T>(lane & 7) * (lane < 8 ? oo2z : (lane < 16 ? oo2e : oo2ze));
-    __syncwarp();
+    Grp::sync();
     // one VRR op: slots[d] = c1*s1 + c2*s2 [+ k1*(s3 - c4*s4)] [+ k5*s5]
     auto eval = [&](const VrrOp& o) -> T {
       const unsigned fl = o.fl;
@@ -394,28 +408,28 @@ __device__ __forceinline__ void vrr_consume(const DevProg& P, const T* __restric
         // two ops per lane per step, loads first: ops of a level are
         // independent, so both may be evaluated before either is stored
         const int o1 = P.vrr_lev[k + 1];
-        for (int op = P.vrr_lev[k] + lane; op < o1; op += 64) {
-          const bool two = op + 32 < o1;
+        for (int op = P.vrr_lev[k] + lane; op < o1; op += 2 * Grp::size()) {
+          const bool two = op + Grp::size() < o1;
           const VrrOp x = load_vrr_op(P, op);
           VrrOp y = x;
-          if (two) y = load_vrr_op(P, op + 32);
+          if (two) y = load_vrr_op(P, op + Grp::size());
           const T vx = eval(x);
           T vy = T(0);
           if (two) vy = eval(y);
           slots[x.d] = vx;
           if (two) slots[y.d] = vy;
         }
-        __syncwarp();
+        Grp::sync();
       }
       const int a1 = P.acc_lev[k + 1];
-      for (int op = P.acc_lev[k] + lane; op < a1; op += 32) {
+      for (int op = P.acc_lev[k] + lane; op < a1; op += Grp::size()) {
         const uint2 u = __ldg(P.acc_ops + op);
         const unsigned src = u.y & 0x3FFFFFFFu;
         const unsigned w = u.y >> 30;
         const T wt = w == 0 ? T(1) : (w == 1 ? w1 : (w == 2 ? w2 : w3));
         slots[u.x] = fma(wt, slots[src], slots[u.x]);
       }
-      __syncwarp();
+      Grp::sync();
     }
   }
 }
@@ -447,7 +461,7 @@ __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __
 }
 
 // Step 3 for one phase.
-template <typename T>
+template <typename T, class Grp = WarpGrp>
 __device__ void run_post_phase(const DevProg& P, int ph, const QuartetGeom<T>& g,
                                T* __restrict__ slots, int lane) {
   const T ABx = g.AB[0], ABy = g.AB[1], ABz = g.AB[2];
@@ -472,18 +486,18 @@ __device__ void run_post_phase(const DevProg& P, int ph, const QuartetGeom<T>& g
   };
   for (int k = l0; k < l1; ++k) {
     const int o1 = P.post_lev[k + 1];
-    for (int op = P.post_lev[k] + lane; op < o1; op += 64) {
-      const bool two = op + 32 < o1;
+    for (int op = P.post_lev[k] + lane; op < o1; op += 2 * Grp::size()) {
+      const bool two = op + Grp::size() < o1;
       const PostOp x = load_post_op(P, op);
       PostOp y = x;
-      if (two) y = load_post_op(P, op + 32);
+      if (two) y = load_post_op(P, op + Grp::size());
       const T vx = eval(x);
       T vy = T(0);
       if (two) vy = eval(y);
       slots[x.d] = vx;
       if (two) slots[y.d] = vy;
     }
-    __syncwarp();
+    Grp::sync();
   }
 }
 
@@ -498,7 +512,7 @@ __device__ __forceinline__ float sph_coef(const EriArgs& a, int t, float*) {
 // between `cart` and `tmp`.  Each lane owns whole columns (all indices but
 // the transformed one), so the row loops and coefficient reads are
 // warp-uniform (broadcast loads).  Returns the result buffer.
-template <typename T>
+template <typename T, class Grp = WarpGrp>
 __device__ T* sph_transform(const EriArgs& a, const int* l, const int* pure, int* dims, T* cart,
                             T* tmp, int lane) {
   T* src = cart;
@@ -511,7 +525,7 @@ __device__ T* sph_transform(const EriArgs& a, const int* l, const int* pure, int
     for (int t = 0; t < k; ++t) outer *= dims[t];
     for (int t = k + 1; t < 4; ++t) inner *= dims[t];
     const int ncol = outer * inner;
-    for (int c = lane; c < ncol; c += 32) {
+    for (int c = lane; c < ncol; c += Grp::size()) {
       const int o = c / inner, i = c - o * inner;
       const T* sp = src + (size_t)o * nc * inner + i;
       T* dp = dst + (size_t)o * np * inner + i;
@@ -523,7 +537,7 @@ __device__ T* sph_transform(const EriArgs& a, const int* l, const int* pure, int
         dp[p * inner] = v;
       }
     }
-    __syncwarp();
+    Grp::sync();
     T* x = src;
     src = dst;
     dst = x;
