@@ -819,12 +819,29 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
                         int deriv, int mode, double mixed_thresh, const int64_t* offsets,
                         double* d_out, int* d_isnull, double precision, int screening,
                         double* d_kschwarz) {
+  // class key of each quartet from a (la, lb, lc, ld) table, counting
+  // passes, and a stable scatter of the work items into one array grouped by
+  // key (ascending key order, as the launches below go)
+  static const std::vector<int> kClassKey = [] {
+    constexpr int L = kMaxLInternal + 1;
+    std::vector<int> t(L * L * L * L, -1);
+    for (int la = 0; la < L; ++la)
+      for (int lb = 0; lb < L; ++lb)
+        for (int lc = 0; lc < L; ++lc)
+          for (int ld = 0; ld < L; ++ld) t[((la * L + lb) * L + lc) * L + ld] = class_index(la, lb, lc, ld);
+    return t;
+  }();
+  constexpr int LK = kMaxLInternal + 1;
+  const int nkeys = 2 * num_classes();
   struct G {
-    std::vector<QuartetItem> items;
-    int la, lb, lc, ld;
-    bool fp32;
+    size_t count = 0, begin = 0, fill = 0;
+    double nq = 0;
+    int la = 0, lb = 0, lc = 0, ld = 0;
+    bool fp32 = false;
   };
-  std::map<int, G> groups;
+  std::vector<G> gk(nkeys);
+  std::vector<QuartetItem> items(size_t(std::max<long long>(n, 0)));
+  std::vector<int> keys(items.size());
   long long run_off = 0;
   for (long long q = 0; q < n; ++q) {
     const int* s = quartets + 4 * q;
@@ -832,7 +849,7 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
       if (s[k] < 0 || s[k] >= B.nshell)
         return fail(ctx, LGX_ERR_INVALID_ARG, "quartet shell index out of range");
     const Canon c = canonicalize(B, s);
-    QuartetItem it;
+    QuartetItem& it = items[size_t(q)];
     it.bra_pair = int(pidx(std::max(c.c[0], c.c[1]), std::min(c.c[0], c.c[1])));
     it.ket_pair = int(pidx(std::max(c.c[2], c.c[3]), std::min(c.c[2], c.c[3])));
     it.flags = c.flags;
@@ -851,21 +868,27 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
       const double bound = B.Kpair[it.bra_pair] * B.Kpair[it.ket_pair];
       fp32 = bound < mixed_thresh;
     }
-    const int key = class_index(c.la, c.lb, c.lc, c.ld) * 2 + (fp32 ? 1 : 0);
-    G& g = groups[key];
-    g.la = c.la; g.lb = c.lb; g.lc = c.lc; g.ld = c.ld; g.fp32 = fp32;
-    g.items.push_back(it);
+    const int ci = kClassKey[((c.la * LK + c.lb) * LK + c.lc) * LK + c.ld];
+    if (ci < 0) return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "angular momentum beyond LGX_MAX_L");
+    const int key = ci * 2 + (fp32 ? 1 : 0);
+    keys[size_t(q)] = key;
+    G& g = gk[key];
+    if (g.count++ == 0) {
+      g.la = c.la; g.lb = c.lb; g.lc = c.lc; g.ld = c.ld; g.fp32 = fp32;
+    }
+    g.nq += double(B.hpairs[it.bra_pair].npp) * double(B.hpairs[it.ket_pair].npp);
   }
   size_t total = 0;
-  for (auto& kv : groups) total += kv.second.items.size();
-  CK(ctx->items.ensure(total * sizeof(QuartetItem)));
-  std::vector<QuartetItem> all;
-  all.reserve(total);
-  std::vector<std::pair<size_t, size_t>> ranges;
-  for (auto& kv : groups) {
-    ranges.push_back({all.size(), kv.second.items.size()});
-    all.insert(all.end(), kv.second.items.begin(), kv.second.items.end());
-  }
+  std::vector<int> order;  // keys with work, ascending
+  for (int k = 0; k < nkeys; ++k)
+    if (gk[k].count) {
+      gk[k].begin = gk[k].fill = total;
+      total += gk[k].count;
+      order.push_back(k);
+    }
+  CK(ctx->items.ensure(std::max<size_t>(total, 1) * sizeof(QuartetItem)));
+  std::vector<QuartetItem> all(total);
+  for (size_t q = 0; q < items.size(); ++q) all[gk[keys[q]].fill++] = items[q];
   CK(cudaMemcpyAsync(ctx->items.p, all.data(), total * sizeof(QuartetItem),
                      cudaMemcpyHostToDevice, ctx->stream));
   // the class launches run on parallel branches (streams forked from and
@@ -873,7 +896,7 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
   // slot scratch per launch / branch): a short list, such as the raised and
   // lowered quartets of a second-derivative set, then costs its slowest
   // class rather than the sum of its classes
-  const int ng = int(groups.size());
+  const int ng = int(order.size());
   const int nbr = std::min(ng, lgx_context::kMaxBranches);
   const bool split = ctx->overlap && nbr > 1;
   CK(ctx->xcounters.ensure(size_t(ng) * sizeof(unsigned long long)));
@@ -894,11 +917,12 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
   } restore{ctx};
   size_t gi = 0;
   lgx_status s = LGX_OK;
-  for (auto& kv : groups) {
+  for (const int key : order) {
+    const G& grp = gk[key];
     ProgDev* P = nullptr;
-    s = get_prog(ctx, kv.second.la, kv.second.lb, kv.second.lc, kv.second.ld, deriv, &P);
+    s = get_prog(ctx, grp.la, grp.lb, grp.lc, grp.ld, deriv, &P);
     if (s != LGX_OK) break;
-    const bool fp32 = kv.second.fp32;
+    const bool fp32 = grp.fp32;
     if (split) {
       const int b = int(gi) % nbr;
       ctx->launch_stream = fp32 ? ctx->s32[b] : ctx->s64[b];
@@ -909,16 +933,13 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
     a.precision = precision;
     a.ln_prec = precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
     a.screening = screening;
-    a.items = ctx->items.as<QuartetItem>() + ranges[gi].first;
-    a.nitems = (long long)ranges[gi].second;
+    a.items = ctx->items.as<QuartetItem>() + grp.begin;
+    a.nitems = (long long)grp.count;
     a.implicit = 0;
     a.out = d_out;
     a.is_null = d_isnull;
     a.kschwarz = d_kschwarz;
-    double nq = 0;
-    for (const auto& it : kv.second.items)
-      nq += double(B.hpairs[it.bra_pair].npp) * double(B.hpairs[it.ket_pair].npp);
-    nq /= std::max<size_t>(1, kv.second.items.size());
+    const double nq = grp.nq / double(std::max<size_t>(1, grp.count));
     s = run_eri(ctx, B, *P, mode, fp32, a, a.nitems, nq);
     if (s != LGX_OK) break;
     ++gi;
