@@ -69,22 +69,6 @@ struct DBuf {
   T* as() const { return reinterpret_cast<T*>(p); }
 };
 
-struct PinnedBuf {
-  void* p = nullptr;
-  size_t n = 0;
-  ~PinnedBuf() {
-    if (p) cudaFreeHost(p);
-  }
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= n && p) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    n = 0;
-    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(bytes, 256));
-    if (e == cudaSuccess) n = std::max<size_t>(bytes, 256);
-    return e;
-  }
-};
 
 struct ProgDev {
   ClassProgramHost host;
@@ -250,7 +234,6 @@ struct lgx_context {
   DBuf Jacc, Kacc, Dd, Jd, Kd, gJ, gK;
   DBuf prim_rows, prim_slots;  // lgx_compute_primitive_set
   DBuf xcounters;              // explicit lists: one work counter per class launch
-  PinnedBuf pin_in, pin_out;
   BinCache bins;
   std::mutex mu;
 };
