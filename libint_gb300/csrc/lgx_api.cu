@@ -1783,14 +1783,26 @@ lgx_status prim_set_launch(lgx_context* ctx, const int l[4], int deriv,
   CK(cudaMemcpyAsync(ctx->prim_rows.p, rows.data(), rows.size() * sizeof(double),
                      cudaMemcpyHostToDevice, ctx->stream));
   a.rows = ctx->prim_rows.as<double>();
-  const size_t stage = stage_bytes_per_warp(false, a.stage_rows);
-  const size_t slot_bytes = size_t((P->host.total_slots() + 1) & ~1) * sizeof(double);
+  a.slot_stride = (P->host.total_slots() + 1) & ~1;
+  const size_t slot_bytes = size_t(a.slot_stride) * sizeof(double);
   const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
-  size_t smem = stage + slot_bytes;
-  if (smem > smem_cap) {  // slots in global memory (L1/L2 resident)
-    CK(ctx->prim_slots.ensure(slot_bytes));
-    a.slots = ctx->prim_slots.as<double>();
-    smem = stage;
+  // many rows of a small class: whole rows per warp (8 staged rows each),
+  // no block-wide barrier per recurrence level
+  const size_t per_warp = stage_bytes_per_warp(false, 8) + slot_bytes;
+  size_t smem;
+  if (nprim >= 8 && (kBlockThreads / 32) * per_warp <= smem_cap) {
+    a.warp_rows = 1;
+    a.stage_rows = 8;
+    smem = (kBlockThreads / 32) * per_warp;
+  } else {
+    a.warp_rows = 0;
+    const size_t stage = stage_bytes_per_warp(false, a.stage_rows);
+    smem = stage + slot_bytes;
+    if (smem > smem_cap) {  // slots in global memory (L1/L2 resident)
+      CK(ctx->prim_slots.ensure(slot_bytes));
+      a.slots = ctx->prim_slots.as<double>();
+      smem = stage;
+    }
   }
   CK(launch_prim_set(a, smem, ctx->stream));
   return LGX_OK;

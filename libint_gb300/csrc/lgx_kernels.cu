@@ -200,19 +200,51 @@ __global__ void __launch_bounds__(kBlockThreads) prim_set_kernel(PrimSetArgs a) 
   const int tid = threadIdx.x, nt = blockDim.x;
   const DevProg& P = a.prog;
   const int R = a.stage_rows;
-  double* stage = smem_d;
-  double* ktab = stage + R * kStage;
-  double* slots = a.slots ? a.slots : smem_d + ((R * kStage + kKtab + 3) & ~3);
-  for (int i = tid; i < P.nacc; i += nt) slots[i] = 0.0;
-  __syncthreads();
-  for (int base = 0; base < a.nrows; base += R) {
-    const int n = min(R, a.nrows - base);
-    const double* src = a.rows + (size_t)base * kStage;
-    for (int i = tid; i < n * kStage; i += nt) stage[i] = src[i];
+  const int stage_per = (R * kStage + kKtab + 3) & ~3;
+  double* slots;
+  if (a.warp_rows) {
+    // warp w: stage at w * (stage_per + slot_stride), its accumulators after it;
+    // rows w, w + nwarps, ... in batches of up to R per warp
+    const int w = tid >> 5, lane = tid & 31, nw = nt >> 5;
+    double* wstage = smem_d + size_t(w) * (stage_per + a.slot_stride);
+    double* wslots = wstage + stage_per;
+    for (int i = lane; i < P.nacc; i += 32) wslots[i] = 0.0;
+    __syncwarp();
+    const int mine = a.nrows > w ? (a.nrows - w + nw - 1) / nw : 0;  // rows of this warp
+    for (int base = 0; base < mine; base += R) {
+      const int n = min(R, mine - base);
+      for (int i = lane; i < n * kStage; i += 32) {
+        const int r = i / kStage, c = i - r * kStage;
+        wstage[i] = a.rows[(size_t)(w + (base + r) * nw) * kStage + c];
+      }
+      __syncwarp();
+      const unsigned ballot = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+      vrr_consume<double, WarpGrp>(P, wstage, ballot, wslots, wstage + R * kStage, lane);
+      __syncwarp();
+    }
     __syncthreads();
-    const unsigned ballot = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
-    vrr_consume<double, BlockGrp>(P, stage, ballot, slots, ktab, tid);
+    slots = smem_d + stage_per;  // warp 0's accumulators receive the sum
+    for (int i = tid; i < P.nacc; i += nt) {
+      double v = slots[i];
+      for (int u = 1; u < nw; ++u) v += smem_d[size_t(u) * (stage_per + a.slot_stride) + stage_per + i];
+      slots[i] = v;
+    }
     __syncthreads();
+  } else {
+    double* stage = smem_d;
+    double* ktab = stage + R * kStage;
+    slots = a.slots ? a.slots : smem_d + stage_per;
+    for (int i = tid; i < P.nacc; i += nt) slots[i] = 0.0;
+    __syncthreads();
+    for (int base = 0; base < a.nrows; base += R) {
+      const int n = min(R, a.nrows - base);
+      const double* src = a.rows + (size_t)base * kStage;
+      for (int i = tid; i < n * kStage; i += nt) stage[i] = src[i];
+      __syncthreads();
+      const unsigned ballot = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+      vrr_consume<double, BlockGrp>(P, stage, ballot, slots, ktab, tid);
+      __syncthreads();
+    }
   }
   QuartetGeom<double> g;
   for (int x = 0; x < 3; ++x) {

@@ -75,6 +75,11 @@ struct PrimSetArgs {
   int perm[4];          // canonical position k -> caller position perm[k]
   double* slots;        // global slot scratch, or nullptr for shared memory
   double* out;          // nsets x ncart(l1) ncart(l2) ncart(l3) ncart(l4), caller order
+  // warp_rows: each warp contracts its own rows into its own accumulators
+  // (stage and slot_stride slots per warp in shared memory), summed into
+  // warp 0's before the post program; for small classes with many rows
+  int warp_rows;
+  int slot_stride;
 };
 
 struct EriArgs {
