@@ -705,14 +705,26 @@ lgx_status run_block_store(lgx_context* ctx, BasisDev& B, const ProgDev& P, EriA
                            long long nwork) {
   fill_common(ctx, B, a);
   a.prog = P.dev;
-  a.stage_rows = 32;
   a.slot_stride = (P.host.total_slots() + 1) & ~1;
-  const size_t stage = stage_bytes_per_warp(false, a.stage_rows);
   const size_t slot_bytes = size_t(a.slot_stride) * sizeof(double);
   const size_t smem_cap = std::min<size_t>(ctx->smem_optin, 200 * 1024);
   const int grid = int(std::max<long long>(1, nwork));
-  size_t smem = stage + slot_bytes;
   a.global_slots = 0;
+  // small classes: each warp contracts its own primitive quartets (8 staged
+  // rows and the accumulators per warp in shared memory), no block-wide
+  // barrier per recurrence level
+  const size_t per_warp = stage_bytes_per_warp(false, 8) + slot_bytes;
+  if ((kBlockThreads / 32) * per_warp <= smem_cap) {
+    a.warp_rows = 1;
+    a.stage_rows = 8;
+    CK(launch_eri_block_store(a, grid, (kBlockThreads / 32) * per_warp,
+                              ctx->launch_stream ? ctx->launch_stream : ctx->stream));
+    return LGX_OK;
+  }
+  a.warp_rows = 0;
+  a.stage_rows = 32;
+  const size_t stage = stage_bytes_per_warp(false, a.stage_rows);
+  size_t smem = stage + slot_bytes;
   if (smem > smem_cap) {
     DBuf& scr = ctx->scratch ? *ctx->scratch : ctx->gscratch;
     if (ctx->noalloc && scr.n < size_t(grid) * slot_bytes)

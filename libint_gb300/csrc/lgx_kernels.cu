@@ -301,34 +301,67 @@ __global__ void __launch_bounds__(kBlockThreads) eri_block_store_kernel(EriArgs 
   const int tid = threadIdx.x, nt = blockDim.x;
   const DevProg& P = a.prog;
   const int R = a.stage_rows;
+  const int stage_per = (R * kStage + kKtab + 3) & ~3;
   double* stage = smem_d;
   double* ktab = stage + R * kStage;
+  // warp_rows: warp w owns the shared-memory region w * (stage_per +
+  // slot_stride) (its staging rows, then its accumulators); the post program
+  // runs on warp 0's region after the accumulators are summed into it
   double* slots = a.global_slots
                       ? reinterpret_cast<double*>(a.gscratch) + size_t(blockIdx.x) * a.slot_stride
-                      : smem_d + ((R * kStage + kKtab + 3) & ~3);
+                      : smem_d + stage_per;
+  const int w = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  double* wstage = smem_d + size_t(w) * (stage_per + a.slot_stride);
+  double* wslots = wstage + stage_per;
   for (long long q = blockIdx.x; q < a.nitems; q += gridDim.x) {
     const QuartetItem it = a.items[q];
     QuartetGeom<double> g;
     load_geom<double>(a, it.bra_pair, it.ket_pair, it.flags & 1, (it.flags >> 1) & 1, g);
-    for (int i = tid; i < P.nacc; i += nt) slots[i] = 0.0;
-    if (tid == 0) s_kept = 0;
-    __syncthreads();
     const int nq = g.nbpp * g.nkpp;
     const double npbraket = double(nq);
-    for (int base = 0; base < nq; base += R) {
-      if (tid < 32) {
+    if (a.warp_rows) {
+      for (int i = lane; i < P.nacc; i += 32) wslots[i] = 0.0;
+      if (tid == 0) s_kept = 0;
+      __syncthreads();
+      const int mine = nq > w ? (nq - w + nw - 1) / nw : 0;  // primitive quartets w + k nw
+      int kept_w = 0;
+      for (int base = 0; base < mine; base += R) {
         bool keep = false;
-        if (tid < R && base + tid < nq)
-          keep = prologue<ATT>(a, g, base + tid, npbraket, stage + tid * kStage);
+        if (lane < R && base + lane < mine)
+          keep = prologue<ATT>(a, g, w + (base + lane) * nw, npbraket, wstage + lane * kStage);
         const unsigned b = __ballot_sync(0xffffffffu, keep);
-        if (tid == 0) {
-          s_ballot = b;
-          s_kept += __popc(b);
-        }
+        kept_w += __popc(b);
+        __syncwarp();
+        vrr_consume<double, WarpGrp>(P, wstage, b, wslots, wstage + R * kStage, lane);
+        __syncwarp();
+      }
+      if (lane == 0) atomicAdd(&s_kept, kept_w);
+      __syncthreads();
+      for (int i = tid; i < P.nacc; i += nt) {
+        double v = slots[i];
+        for (int u = 1; u < nw; ++u) v += smem_d[size_t(u) * (stage_per + a.slot_stride) + stage_per + i];
+        slots[i] = v;
       }
       __syncthreads();
-      vrr_consume<double, BlockGrp>(P, stage, s_ballot, slots, ktab, tid);
+    } else {
+      for (int i = tid; i < P.nacc; i += nt) slots[i] = 0.0;
+      if (tid == 0) s_kept = 0;
       __syncthreads();
+      for (int base = 0; base < nq; base += R) {
+        if (tid < 32) {
+          bool keep = false;
+          if (tid < R && base + tid < nq)
+            keep = prologue<ATT>(a, g, base + tid, npbraket, stage + tid * kStage);
+          const unsigned b = __ballot_sync(0xffffffffu, keep);
+          if (tid == 0) {
+            s_ballot = b;
+            s_kept += __popc(b);
+          }
+        }
+        __syncthreads();
+        vrr_consume<double, BlockGrp>(P, stage, s_ballot, slots, ktab, tid);
+        __syncthreads();
+      }
     }
     const int kept = s_kept;
     if (a.is_null && tid == 0) a.is_null[it.pad] = kept == 0 ? 1 : 0;

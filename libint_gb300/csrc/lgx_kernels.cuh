@@ -121,6 +121,7 @@ struct EriArgs {
   int slot_stride;     // slots per warp (elements of T)
   int stage_rows;      // program kernel: primitive quartets staged per batch (8, 16 or 32)
   int global_slots;    // 1: slots live in gscratch
+  int warp_rows;       // block store kernel: each warp contracts its own primitive quartets
   void* gscratch;      // [nwarps_total][slot_stride] of T
   // outputs
   double* out;         // kModeStore
