@@ -604,6 +604,7 @@ def run_rows(args):
 
     # range-separated J/K: erfc(0.4 r)/r pass vs the Coulomb pass, (H2O)16 cc-pVDZ
     atoms, bs, D, thresh, _ = build_inputs("h2o16_cc-pvdz")
+    peaks = measure_peaks(torch)
     res = {}
     for name, op in (("coulomb", lg.Operator.coulomb), ("erfc", lg.Operator.erfc_coulomb)):
         ctx = lg.Context(local)
@@ -618,11 +619,25 @@ def run_rows(args):
             st = ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh,
                                lg._lgx.LGX_FP64)
             ms.append(st.pass_ms)
+        launches = ctx.last_pass_launches()
+        for r in launches:
+            r["ms_avg"] = r["ms"]
+        roof = kernel_roofline(launches, peaks, "h2o16_cc-pvdz", "fp64")
+        if roof:
+            roof["note"] = ("dominant class launch of the last pass (concurrent branches: its "
+                            "time includes sharing the GPU); FLOPs counted as for the Coulomb "
+                            "operator (the attenuation's second Boys evaluation not included)")
         Kq = ctx.schwarz()
         oracle.set_operator(oracle.OP_ERFC_COULOMB if name == "erfc" else oracle.OP_COULOMB, 0.4)
         v, nsamp, tsamp, npair = cpu_baseline(bs, D, Kq, thresh, 8.0)
         res[name] = {"pass_ms": statistics.median(ms), "integrals": int(st.integrals),
                      "eri_per_s": st.integrals / (statistics.median(ms) * 1e-3),
+                     "roofline_pass": {"bound": "fp64-pipe", "unit": "TFLOP/s",
+                                       "achieved": st.flops_fp64 / (st.pass_ms * 1e-3) / 1e12,
+                                       "peak": peaks["fp64"],
+                                       "frac": st.flops_fp64 / (st.pass_ms * 1e-3) / 1e12
+                                       / peaks["fp64"]},
+                     "roofline": roof,
                      "oracle_eri_per_s": v, "oracle_sample_integrals": int(nsamp)}
         ctx.close()
     oracle.set_operator(oracle.OP_COULOMB, 0.0)
