@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -11,6 +12,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/lgx.h"
@@ -816,74 +818,141 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
                         double* d_kschwarz) {
   // class key of each quartet from a (la, lb, lc, ld) table, counting
   // passes, and a stable scatter of the work items into one array grouped by
-  // key (ascending key order, as the launches below go)
-  static const std::vector<int> kClassKey = [] {
-    constexpr int L = kMaxLInternal + 1;
-    std::vector<int> t(L * L * L * L, -1);
-    for (int la = 0; la < L; ++la)
-      for (int lb = 0; lb < L; ++lb)
-        for (int lc = 0; lc < L; ++lc)
-          for (int ld = 0; ld < L; ++ld) t[((la * L + lb) * L + lc) * L + ld] = class_index(la, lb, lc, ld);
+  // key (ascending key order, as the launches below go); long lists split
+  // both passes over the host threads (per-thread counts merged so that the
+  // items of a class keep the list order, packed offsets fixed up by the
+  // chunks' prefix sums)
+  constexpr int LK = kMaxLInternal + 1;
+  struct ClassTables {
+    std::vector<int> key;          // (la, lb, lc, ld) -> class index
+    std::vector<std::array<int, 4>> shape;  // class index -> (la, lb, lc, ld)
+  };
+  static const ClassTables kTab = [] {
+    ClassTables t;
+    t.key.assign(LK * LK * LK * LK, -1);
+    t.shape.resize(num_classes());
+    for (int la = 0; la < LK; ++la)
+      for (int lb = 0; lb < LK; ++lb)
+        for (int lc = 0; lc < LK; ++lc)
+          for (int ld = 0; ld < LK; ++ld) {
+            const int ci = class_index(la, lb, lc, ld);
+            t.key[((la * LK + lb) * LK + lc) * LK + ld] = ci;
+            if (ci >= 0) t.shape[ci] = {la, lb, lc, ld};
+          }
     return t;
   }();
-  constexpr int LK = kMaxLInternal + 1;
   const int nkeys = 2 * num_classes();
   struct G {
-    size_t count = 0, begin = 0, fill = 0;
+    size_t count = 0, begin = 0;
     double nq = 0;
     int la = 0, lb = 0, lc = 0, ld = 0;
     bool fp32 = false;
   };
-  std::vector<G> gk(nkeys);
-  std::vector<QuartetItem> items(size_t(std::max<long long>(n, 0)));
-  std::vector<int> keys(items.size());
-  long long run_off = 0;
-  for (long long q = 0; q < n; ++q) {
-    const int* s = quartets + 4 * q;
-    for (int k = 0; k < 4; ++k)
-      if (s[k] < 0 || s[k] >= B.nshell)
-        return fail(ctx, LGX_ERR_INVALID_ARG, "quartet shell index out of range");
-    const Canon c = canonicalize(B, s);
-    QuartetItem& it = items[size_t(q)];
-    it.bra_pair = int(pidx(std::max(c.c[0], c.c[1]), std::min(c.c[0], c.c[1])));
-    it.ket_pair = int(pidx(std::max(c.c[2], c.c[3]), std::min(c.c[2], c.c[3])));
-    it.flags = c.flags;
-    it.pad = int(q);
-    long long nv = 1;
-    for (int k = 0; k < 4; ++k) nv *= nfunc(B.l[s[k]], B.pure[s[k]]);
-    const long long nsets = deriv ? 12 : 1;
-    if (mode == kModeSchwarz) {
-      it.out = offsets ? offsets[q] : q;
-    } else {
-      it.out = offsets ? offsets[q] : run_off;
-      run_off += nv * nsets;
+  const size_t nn = size_t(std::max<long long>(n, 0));
+  std::vector<QuartetItem> items(nn);
+  std::vector<int> keys(nn);
+  const int nthr = nn >= 65536 ? int(std::max(1u, std::min(16u, std::thread::hardware_concurrency())))
+                               : 1;
+  const size_t chunk = (nn + nthr - 1) / std::max(1, nthr);
+  std::vector<std::vector<size_t>> cnt(nthr, std::vector<size_t>(nkeys, 0));
+  std::vector<std::vector<double>> nqs(nthr, std::vector<double>(nkeys, 0.0));
+  std::vector<long long> span(nthr, 0);  // packed output length of each chunk
+  std::vector<int> bad(nthr, 0);          // 1: shell index out of range, 2: l beyond the build
+  const long long nsets = deriv ? 12 : 1;
+  auto pass1 = [&](int t) {
+    const size_t q0 = std::min(nn, size_t(t) * chunk), q1 = std::min(nn, q0 + chunk);
+    long long run_off = 0;
+    for (size_t q = q0; q < q1; ++q) {
+      const int* s = quartets + 4 * q;
+      for (int k = 0; k < 4; ++k)
+        if (s[k] < 0 || s[k] >= B.nshell) {
+          bad[t] = 1;
+          return;
+        }
+      const Canon c = canonicalize(B, s);
+      QuartetItem& it = items[q];
+      it.bra_pair = int(pidx(std::max(c.c[0], c.c[1]), std::min(c.c[0], c.c[1])));
+      it.ket_pair = int(pidx(std::max(c.c[2], c.c[3]), std::min(c.c[2], c.c[3])));
+      it.flags = c.flags;
+      it.pad = int(q);
+      if (mode == kModeSchwarz) {
+        it.out = offsets ? offsets[q] : (long long)q;
+      } else if (offsets) {
+        it.out = offsets[q];
+      } else {
+        long long nv = 1;
+        for (int k = 0; k < 4; ++k) nv *= nfunc(B.l[s[k]], B.pure[s[k]]);
+        it.out = run_off;  // chunk-relative; the chunk's base is added in the scatter
+        run_off += nv * nsets;
+      }
+      bool fp32 = false;
+      if (mode == kModeStore && mixed_thresh > 0 && B.schwarz_ok) {
+        const double bound = B.Kpair[it.bra_pair] * B.Kpair[it.ket_pair];
+        fp32 = bound < mixed_thresh;
+      }
+      const int ci = kTab.key[((c.la * LK + c.lb) * LK + c.lc) * LK + c.ld];
+      if (ci < 0) {
+        bad[t] = 2;
+        return;
+      }
+      const int key = ci * 2 + (fp32 ? 1 : 0);
+      keys[q] = key;
+      ++cnt[t][key];
+      nqs[t][key] += double(B.hpairs[it.bra_pair].npp) * double(B.hpairs[it.ket_pair].npp);
     }
-    bool fp32 = false;
-    if (mode == kModeStore && mixed_thresh > 0 && B.schwarz_ok) {
-      const double bound = B.Kpair[it.bra_pair] * B.Kpair[it.ket_pair];
-      fp32 = bound < mixed_thresh;
+    span[t] = run_off;
+  };
+  auto run_threads = [&](auto&& fn) {
+    if (nthr == 1) {
+      fn(0);
+      return;
     }
-    const int ci = kClassKey[((c.la * LK + c.lb) * LK + c.lc) * LK + c.ld];
-    if (ci < 0) return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "angular momentum beyond LGX_MAX_L");
-    const int key = ci * 2 + (fp32 ? 1 : 0);
-    keys[size_t(q)] = key;
-    G& g = gk[key];
-    if (g.count++ == 0) {
-      g.la = c.la; g.lb = c.lb; g.lc = c.lc; g.ld = c.ld; g.fp32 = fp32;
-    }
-    g.nq += double(B.hpairs[it.bra_pair].npp) * double(B.hpairs[it.ket_pair].npp);
+    std::vector<std::thread> th;
+    th.reserve(nthr);
+    for (int t = 0; t < nthr; ++t) th.emplace_back(fn, t);
+    for (auto& x : th) x.join();
+  };
+  run_threads(pass1);
+  for (int t = 0; t < nthr; ++t) {
+    if (bad[t] == 1) return fail(ctx, LGX_ERR_INVALID_ARG, "quartet shell index out of range");
+    if (bad[t] == 2) return fail(ctx, LGX_ERR_LMAX_EXCEEDED, "angular momentum beyond LGX_MAX_L");
   }
+  std::vector<long long> base(nthr, 0);  // packed output offset of each chunk
+  for (int t = 1; t < nthr; ++t) base[t] = base[t - 1] + span[t - 1];
+  // class order ascending; within a class, chunk order (= list order)
+  std::vector<G> gk(nkeys);
+  std::vector<std::vector<size_t>> pos(nthr, std::vector<size_t>(nkeys, 0));
   size_t total = 0;
   std::vector<int> order;  // keys with work, ascending
-  for (int k = 0; k < nkeys; ++k)
-    if (gk[k].count) {
-      gk[k].begin = gk[k].fill = total;
-      total += gk[k].count;
+  for (int k = 0; k < nkeys; ++k) {
+    G& g = gk[k];
+    g.begin = total;
+    for (int t = 0; t < nthr; ++t) {
+      pos[t][k] = total;
+      total += cnt[t][k];
+      g.nq += nqs[t][k];
+    }
+    g.count = total - g.begin;
+    if (g.count) {
+      const auto& sh = kTab.shape[k / 2];
+      g.la = sh[0]; g.lb = sh[1]; g.lc = sh[2]; g.ld = sh[3];
+      g.fp32 = (k & 1) != 0;
       order.push_back(k);
     }
+  }
   CK(ctx->items.ensure(std::max<size_t>(total, 1) * sizeof(QuartetItem)));
   std::vector<QuartetItem> all(total);
-  for (size_t q = 0; q < items.size(); ++q) all[gk[keys[q]].fill++] = items[q];
+  const bool packed = !offsets && mode != kModeSchwarz;
+  auto scatter = [&](int t) {
+    const size_t q0 = std::min(nn, size_t(t) * chunk), q1 = std::min(nn, q0 + chunk);
+    std::vector<size_t>& p = pos[t];
+    for (size_t q = q0; q < q1; ++q) {
+      QuartetItem it = items[q];
+      if (packed) it.out += base[t];
+      all[p[keys[q]]++] = it;
+    }
+  };
+  run_threads(scatter);
   CK(cudaMemcpyAsync(ctx->items.p, all.data(), total * sizeof(QuartetItem),
                      cudaMemcpyHostToDevice, ctx->stream));
   // the class launches run on parallel branches (streams forked from and

@@ -93,6 +93,18 @@ def test_config1_h2o4_every_unique_quartet_fp64(lgx, oracle_mod):
     ctx = lgx.Context(0)
     ctx.set_basis(bs)
     compare_batch(lgx, oracle_mod, ctx, ob, bs, q)
+    # offsets = NULL packs the sets in list order: identical to the explicit
+    # prefix-sum offsets the Python binding passes (a long list, so the host
+    # grouping runs on several threads and fixes the packed offsets per chunk)
+    import ctypes
+    out, offs, _ = ctx.compute_batch(q)
+    packed = np.full(out.size, np.nan)
+    lib = lgx._lgx.load()
+    qc = np.ascontiguousarray(q, np.int32)
+    st = lib.lgx_compute_batch(ctx._h, lgx._lgx.ptr(qc, ctypes.c_int32), len(qc), 0, 0, 1e-4,
+                               None, lgx._lgx.ptr(packed), packed.size, None)
+    assert st == 0
+    assert np.array_equal(packed, out)
     ctx.close()
 
 
