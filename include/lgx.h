@@ -2,9 +2,10 @@
  *
  * The library computes two-electron Coulomb repulsion integrals (ERIs) over
  * contracted Gaussian shells on one NVIDIA GB300 (sm_103a), with the buffer
- * layout and conventions of libint2::Engine (Operator::coulomb,
- * BraKet::xx_xx, deriv_order 0 and 1), plus batched and fused J/K entry
- * points.  Plain C types only; every call returns an lgx_status and never
+ * layout and conventions of libint2::Engine (Operator::coulomb and the
+ * attenuated erf / erfc operators, BraKet::xx_xx, deriv_order 0, 1 and 2),
+ * libint's generated per-quartet entry (libint2_build_eri*, through
+ * lgx_compute_primitive_set), plus batched and fused J/K entry points.  Plain C types only; every call returns an lgx_status and never
  * aborts.  A context is bound to one CUDA device and one CUDA stream; calls
  * on one context are serialized, distinct contexts may be used from distinct
  * threads (the reference's one-Engine-per-thread model).

@@ -1,5 +1,6 @@
-// libint2::Engine (Operator::coulomb, BraKet::xx_xx, deriv_order 0/1) as a
-// drop-in over liblgx (include/lgx.h).
+// libint2::Engine (Operator::coulomb / erf_coulomb / erfc_coulomb, BraKet
+// xx_xx / xs_xx / xs_xs, deriv_order 0, 1 and 2) as a drop-in over liblgx
+// (include/lgx.h).
 //
 // Names and signatures follow the reference's engine.h:444-1064 for this
 // path: Engine(Operator, max_nprim, max_l, deriv_order, precision, params,

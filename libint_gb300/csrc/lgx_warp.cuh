@@ -2,7 +2,9 @@
 // included by lgx_kernels.cu (generic instances) and the generated units
 // that pair it with unrolled per-class HRR / solid-harmonic stages.
 //
-// One warp owns one contracted shell quartet at a time:
+// One warp owns one contracted shell quartet at a time (the helpers of steps
+// 2-4 are also instantiated for a whole block, for the single-quartet
+// kernels of lgx_kernels.cu):
 //  1. primitive-quartet prologue, one primitive quartet per lane: libint's
 //     screening (engine.impl.h:1313-1386), pfac, T, the Boys function and
 //     the VRR geometric factors (engine.impl.h:1389-1757); survivors are
