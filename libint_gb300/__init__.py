@@ -34,19 +34,30 @@ class Operator(enum.Enum):
     erf_coulomb = 16
     erfc_coulomb = 17
 
+    @staticmethod
+    def rank(op) -> int:
+        """libint2::rank(Operator) (the binding's Operator.rank): the number
+        of electrons the operator couples, 2 for every operator here."""
+        return 2
+
 
 _OP_CODE = {Operator.coulomb: _lgx.LGX_OP_COULOMB, Operator.erf_coulomb: _lgx.LGX_OP_ERF_COULOMB,
             Operator.erfc_coulomb: _lgx.LGX_OP_ERFC_COULOMB}
 
 
 class BraKet(enum.Enum):
-    """libint2::BraKet (engine.h:188-206; binding names XXXX, XSXX, XSXS):
-    four-centre xx_xx, and the three- and two-centre xs_xx / xs_xs that the
-    reference computes with Shell.unit() in the empty positions."""
+    """libint2::BraKet (engine.h:188-206; binding names XXXX, XSXX, XSXS,
+    XXXS): four-centre xx_xx, and the three- and two-centre xs_xx / xs_xs
+    that the reference computes with Shell.unit() in the empty positions.
+    The binding's XXXS is an alias of the three-centre braket here: libint's
+    Engine evaluates every three-shell call as (a unit|c d)
+    (engine.impl.h:159-166), and the binding's own test expects that value
+    (python/tests/test_libint2.py:40-43)."""
     XXXX = 1
     xx_xx = 1
     XSXX = 3
     xs_xx = 3
+    XXXS = 3
     XSXS = 4
     xs_xs = 4
 
@@ -123,6 +134,20 @@ class Shell:
     @property
     def coeffs(self):
         return list(self.coeff)
+
+    @property
+    def coeffs_normalized(self):
+        """Coefficients of unit-normalized primitives (Shell::coeff_normalized,
+        shell.h:915-928): the embedded coefficients times the inverse
+        primitive normalization sqrt(pi^{3/2} (2l-1)!! / (2^l (2a)^{l+3/2}));
+        a zero exponent (the unit shell) keeps its coefficient."""
+        l = self.l
+        dfact = float(np.prod(np.arange(2 * l - 1, 0, -2))) if l > 0 else 1.0
+        a2 = 2.0 * self.alpha
+        out = self.coeff.copy()
+        nz = a2 > 0
+        out[nz] = self.coeff[nz] * np.sqrt(np.pi ** 1.5 * dfact / (2.0 ** l * a2[nz] ** (l + 1.5)))
+        return list(out)
 
     def move(self, center):
         self.O = np.asarray(center, dtype=float).reshape(3).copy()
@@ -573,6 +598,23 @@ class Engine:
         if r is None:
             return None
         return r[0] if self.deriv_order == 0 else r
+
+    def compute_2body_fock(self, D, basis):
+        """The binding's Engine.compute_2body_fock(D, basis)
+        (python/src/libint2/engine.cc:230-279): the closed-shell two-body
+        Fock matrix G = 2J - K of density D over `basis` (J_ab = sum_cd
+        (ab|cd) D_cd, K_ab = sum_cd (ac|bd) D_cd, which is what the binding's
+        quartet loop accumulates), for this engine's operator and omega,
+        from one J/K pass on the GPU with every quartet (no Schwarz
+        screening, as the binding's loop)."""
+        if self.braket != BraKet.xx_xx or self.deriv_order != 0:
+            raise NotImplementedError("compute_2body_fock: BraKet.xx_xx and deriv_order 0")
+        bs = basis if isinstance(basis, BasisSet) else BasisSet(list(basis))
+        ctx = self._ctx or _default_context()
+        ctx.set_operator(self.oper, self._omega)
+        ctx.set_basis(bs)
+        J, K, _ = ctx.jk(np.asarray(D, dtype=float), 0.0)
+        return 2.0 * J - K
 
     def _compute_basis(self, A, B, C, D):
         nb = [sum(s.size() for s in X) for X in (A, B, C, D)]

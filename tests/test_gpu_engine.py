@@ -66,6 +66,10 @@ def test_python_binding_golden_norms(lgx):
     basis = [s, p, s, p]
     full = eng.compute(basis, basis, basis, basis)
     assert abs(np.linalg.norm(full) - 14.7036075402) < 1e-9
+    # :40-43, braket XXXS on three identical s shells: the Engine evaluates a
+    # three-shell call as (a unit|c d) (engine.impl.h:159-166), = (ss|s) here
+    eng3 = lgx.Engine(lgx.Operator.coulomb, braket=lgx.BraKet.XXXS)
+    assert abs(np.linalg.norm(eng3.compute(s, s, s)) - 3.6563211198) < 1e-9
 
 
 def test_fully_screened_returns_none(lgx):
@@ -88,3 +92,15 @@ def test_water_cc_pvdz_quartets(lgx, oracle_mod):
         got = eng.compute(*[bs[i] for i in q])
         ref = oracle_mod.compute_quartet(ob, *q)
         assert np.max(np.abs(got - ref[0])) < TOL, q
+
+
+def test_compute_2body_fock_vs_oracle(lgx, oracle_mod):
+    # the binding's Engine.compute_2body_fock(D, basis) (python/src/libint2/
+    # engine.cc:230-279) through one GPU J/K pass: G = 2J - K
+    atoms = lgx.water_cluster(1, 1, 1, seed=3)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    D = lgx.random_density(bs.nbf, 5, seed=4)
+    G = lgx.Engine(lgx.Operator.coulomb).compute_2body_fock(D, bs)
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    J, K, _ = oracle_mod.jk(ob, D, oracle_mod.schwarz(ob), 0.0)
+    assert np.max(np.abs(G - (2 * J - K))) < 1e-11

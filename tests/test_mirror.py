@@ -1,0 +1,81 @@
+"""Host logic of the Python mirror of the reference's pybind11 module
+(python/src/libint2/libint2.cc, engine.cc), without a GPU: Shell
+coefficients of normalized primitives, Operator.rank, the XXXS braket name,
+and Engine.compute_2body_fock against the binding's own quartet loop, with
+the J/K supplied by the oracle through a stand-in context."""
+import numpy as np
+import pytest
+
+
+def test_shell_coeffs_normalized(lgx):
+    # Shell::coeff_normalized (shell.h:915-928): one primitive of a unit-
+    # normalized shell has coefficient 1; a contraction keeps its ratios
+    assert np.allclose(lgx.Shell(1, [(1.0, 10.0)]).coeffs_normalized, [1.0], rtol=1e-14)
+    s = lgx.Shell(2, [(2.0, 0.3), (0.5, 0.7)])
+    r = np.array(s.coeffs_normalized) / np.array([0.3, 0.7])
+    assert abs(r[0] - r[1]) < 1e-14 * r[0]
+    assert lgx.Shell.unit().coeffs_normalized == [1.0]
+
+
+def test_operator_rank_and_braket_names(lgx):
+    assert lgx.Operator.rank(lgx.Operator.coulomb) == 2
+    assert lgx.BraKet.XXXS is lgx.BraKet.xs_xx
+    e = lgx.Engine(lgx.Operator.coulomb, braket=lgx.BraKet.XXXS)
+    assert e.braket_rank() == 3 and e.nshellsets() == 1
+
+
+class _OracleContext:
+    """Stand-in for Context: J and K from the oracle."""
+
+    def __init__(self, oracle_mod):
+        self.o = oracle_mod
+        self.calls = []
+
+    def set_operator(self, oper, omega=0.0):
+        self.calls.append(("op", oper, omega))
+
+    def set_basis(self, bs):
+        self.bs = bs
+        self.calls.append(("basis", len(bs)))
+
+    def jk(self, D, schwarz_thresh=1e-12, mode=0, mixed_thresh=1e-4):
+        ob = self.o.OracleBasis.from_basis(self.bs)
+        J, K, _ = self.o.jk(ob, D, self.o.schwarz(ob), schwarz_thresh)
+        return J, K, None
+
+
+def _binding_fock(oracle_mod, bs, D):
+    # the binding's compute_2body_fock loop (engine.cc:241-279), restated
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    bf, n, ns = bs.shell2bf(), bs.nbf, len(bs)
+    sz = [s.size() for s in bs]
+    f = np.zeros((n, n))
+    for P in range(ns):
+        for Q in range(P + 1):
+            for R in range(ns):
+                for S in range(R + 1):
+                    r = oracle_mod.compute_quartet(ob, P, Q, R, S)
+                    if r is None:
+                        continue
+                    v = r[0].reshape(sz[P], sz[Q], sz[R], sz[S])
+                    v = v * ((0.5 if P == Q else 1.0) * (0.5 if R == S else 1.0))
+                    p_, q_, r_, s_ = (slice(bf[X], bf[X] + sz[X]) for X in (P, Q, R, S))
+                    f[p_, q_] += 4 * np.einsum("pqrs,rs->pq", v, D[r_, s_])
+                    f[p_, s_] -= 0.5 * np.einsum("pqrs,qr->ps", v, D[q_, r_])
+                    f[p_, r_] -= 0.5 * np.einsum("pqrs,qs->pr", v, D[q_, s_])
+                    f[q_, r_] -= 0.5 * np.einsum("pqrs,ps->qr", v, D[p_, s_])
+                    f[q_, s_] -= 0.5 * np.einsum("pqrs,pr->qs", v, D[p_, r_])
+    return f + f.T
+
+
+def test_compute_2body_fock_matches_binding_loop(lgx, oracle_mod):
+    atoms = [(1, (0.0, 0.0, 0.0)), (1, (0.0, 0.0, 1.4))]
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    D = lgx.random_density(bs.nbf, 1, seed=5)
+    ctx = _OracleContext(oracle_mod)
+    G = lgx.Engine(lgx.Operator.coulomb, context=ctx).compute_2body_fock(D, bs)
+    assert ("basis", len(bs)) in ctx.calls
+    ref = _binding_fock(oracle_mod, bs, D)
+    assert np.max(np.abs(G - ref)) < 1e-12 * max(1.0, np.abs(ref).max())
+    with pytest.raises(NotImplementedError):
+        lgx.Engine(lgx.Operator.coulomb, deriv_order=1, context=ctx).compute_2body_fock(D, bs)

@@ -136,3 +136,28 @@ def test_attenuated_operators_identities(oracle_mod):
         assert abs(v - ref) < 1e-13 * abs(ref)
     finally:
         oracle_mod.set_operator(0)
+
+
+def test_python_binding_golden_norms(oracle_mod):
+    # the reference's python/tests/test_libint2.py:9-10,37-48: norms of
+    # (pp|ss), of every quartet of [s, p, s, p], and of the three-shell
+    # braket XXXS on s = Shell(0, [(1, 10)]) at the origin, which libint's
+    # Engine evaluates as (a unit|c d) (engine.impl.h:159-166)
+    import libint_gb300 as lg
+    s = lg.Shell(0, [(1, 10)])
+    p = lg.Shell(1, [(1, 10)])
+    u = lg.Shell.unit()
+    ob = oracle_mod.OracleBasis.from_basis(lg.BasisSet([s, p, u]))
+    pp_ss = oracle_mod.compute_quartet(ob, 1, 1, 0, 0, precision=1e-15)[0]
+    assert abs(np.linalg.norm(pp_ss) - 1.62867503968) < 1e-10
+    idx = [0, 1, 0, 1]
+    sq = 0.0
+    for a in idx:
+        for b in idx:
+            for c in idx:
+                for d in idx:
+                    r = oracle_mod.compute_quartet(ob, a, b, c, d, precision=1e-15)
+                    sq += float(np.sum(r[0] ** 2)) if r is not None else 0.0
+    assert abs(np.sqrt(sq) - 14.7036075402) < 1e-9
+    s_u_ss = oracle_mod.compute_quartet(ob, 0, 2, 0, 0, precision=1e-15)[0]
+    assert abs(np.linalg.norm(s_u_ss) - 3.6563211198) < 1e-9
