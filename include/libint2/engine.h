@@ -62,6 +62,31 @@ enum class BraKet { x_x = 0, xx_xx, xs_xx, xx_xs, xs_xs, invalid = -1 };
 
 enum class CartesianShellNormalization { standard, uniform };
 
+/// libint2::operator_traits<Op> (engine.h:200-371), the part callers use:
+/// the parameter type of an operator and its default value (empty for the
+/// Coulomb operator, the attenuation omega for erf / erfc_coulomb).
+namespace detail {
+struct default_operator_traits {
+  typedef struct {
+  } oper_params_type;
+  static oper_params_type default_params() { return oper_params_type{}; }
+  static constexpr auto nopers = 1u;
+  static constexpr auto intrinsic_deriv_order = 0u;
+};
+}  // namespace detail
+template <Operator Op>
+struct operator_traits : public detail::default_operator_traits {};
+template <>
+struct operator_traits<Operator::erf_coulomb> : public detail::default_operator_traits {
+  typedef double oper_params_type;
+  static oper_params_type default_params() { return 0.0; }
+};
+template <>
+struct operator_traits<Operator::erfc_coulomb> : public detail::default_operator_traits {
+  typedef double oper_params_type;
+  static oper_params_type default_params() { return 0.0; }
+};
+
 constexpr size_t num_geometrical_derivatives(size_t ncenter, size_t deriv_order) {
   return deriv_order > 0 ? (num_geometrical_derivatives(ncenter, deriv_order - 1) *
                             (3 * ncenter + deriv_order - 1)) /
@@ -135,6 +160,12 @@ class Engine {
       : Engine(oper, max_nprim, max_l, deriv_order, precision, nullptr, braket, screening) {
     set_params(omega);
   }
+  /// Coulomb with its (empty) parameters as libint callers pass them:
+  /// operator_traits<Operator::coulomb>::default_params()
+  Engine(Operator oper, size_t max_nprim, int max_l, int deriv_order, scalar_type precision,
+         detail::default_operator_traits::oper_params_type /*params*/,
+         BraKet braket = BraKet::invalid, ScreeningMethod screening = default_screening_method())
+      : Engine(oper, max_nprim, max_l, deriv_order, precision, nullptr, braket, screening) {}
   Engine(Operator oper, size_t max_nprim, int max_l, int deriv_order = 0,
          scalar_type precision = std::numeric_limits<scalar_type>::epsilon(),
          std::nullptr_t /*params*/ = nullptr, BraKet braket = BraKet::invalid,
@@ -167,6 +198,27 @@ class Engine {
   Engine& set_params(double omega) {
     if (!(omega >= 0)) throw std::invalid_argument("Engine::set_params: omega must be >= 0");
     omega_ = omega;
+    return *this;
+  }
+  /// the Coulomb operator's (empty) parameters
+  Engine& set_params(detail::default_operator_traits::oper_params_type) { return *this; }
+  /// Engine::set(Operator) / set(BraKet) (engine.h:658-684): change the
+  /// operator or the braket of a constructed engine (one of those served)
+  Engine& set(Operator new_oper) {
+    if (new_oper != Operator::coulomb && new_oper != Operator::erf_coulomb &&
+        new_oper != Operator::erfc_coulomb)
+      throw std::invalid_argument(
+          "libint2::Engine (GB300): only Operator::coulomb, erf_coulomb, erfc_coulomb");
+    oper_ = new_oper;
+    return *this;
+  }
+  Engine& set(BraKet new_braket) {
+    if (new_braket != BraKet::xx_xx && new_braket != BraKet::xs_xx && new_braket != BraKet::xs_xs)
+      throw std::invalid_argument("libint2::Engine (GB300): only BraKet::xx_xx, xs_xx, xs_xs");
+    if (deriv_order_ == 2 && new_braket != BraKet::xx_xx)
+      throw std::invalid_argument("libint2::Engine (GB300): deriv_order 2 needs BraKet::xx_xx");
+    braket_ = new_braket;
+    targets_.assign(nshellsets(), nullptr);
     return *this;
   }
   double params() const { return omega_; }
@@ -206,6 +258,14 @@ class Engine {
     max_nprim_ = n;
     return *this;
   }
+  /// Engine::prescale_by / prescaled_by (engine.h:851-861): every target
+  /// integral is multiplied by `sc` (default 1); libint folds it into the
+  /// primitive prefactor, here it scales the returned sets.
+  Engine& prescale_by(scalar_type sc) {
+    scale_ = sc;
+    return *this;
+  }
+  scalar_type prescaled_by() const { return scale_; }
   Engine& set_max_l(int L) {
     if (L > LGX_MAX_L) throw lmax_exceeded("eri", LGX_MAX_L, L);
     lmax_ = L;
@@ -253,6 +313,7 @@ class Engine {
   scalar_type precision_ = 0, ln_precision_ = 0;
   ScreeningMethod screening_ = ScreeningMethod::Original;
   double omega_ = 0;
+  scalar_type scale_ = 1;
   bool initialized_ = false;
   std::vector<value_type> buf_;
   target_ptr_vec targets_;
@@ -297,6 +358,8 @@ class Engine {
       throw std::runtime_error(std::string("libint2::Engine::compute: ") + lgx_last_error(rt.ctx));
     targets_.assign(ns, nullptr);
     if (is_null) return targets_;
+    if (scale_ != scalar_type(1))
+      for (size_t i = 0; i < size_t(nsets) * size_t(nvalues); ++i) buf_[i] *= scale_;
     // derivative sets of the real centres only: the unit shells' sets (zero)
     // are left out, which leaves the reference's order (centres A, C, D for
     // xs_xx; A, C for xs_xs; each x, y, z)
