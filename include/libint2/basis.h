@@ -136,6 +136,40 @@ class BasisSet : public std::vector<Shell> {
     return r;
   }
   const std::vector<long>& shell2atom_index() const { return shell2atom_; }
+  /// BasisSet::shell2atom / atom2shell (basis.h.in:279-335): shell k maps to
+  /// the first atom whose coordinates equal its origin exactly (-1 when none,
+  /// or std::logic_error with throw_if_no_match); atom a maps to the shells
+  /// whose origin equals its coordinates, in shell order.
+  std::vector<long> shell2atom(const std::vector<Atom>& atoms) const {
+    return shell2atom(*this, atoms, false);
+  }
+  std::vector<std::vector<long>> atom2shell(const std::vector<Atom>& atoms) const {
+    return atom2shell(atoms, *this);
+  }
+  static std::vector<long> shell2atom(const std::vector<Shell>& shells,
+                                      const std::vector<Atom>& atoms,
+                                      bool throw_if_no_match = false) {
+    std::vector<long> r;
+    r.reserve(shells.size());
+    for (const auto& s : shells) {
+      long hit = -1;
+      for (size_t a = 0; a < atoms.size() && hit < 0; ++a)
+        if (s.O[0] == atoms[a].x && s.O[1] == atoms[a].y && s.O[2] == atoms[a].z) hit = long(a);
+      if (hit < 0 && throw_if_no_match) throw std::logic_error("shell2atom: no matching atom found");
+      r.push_back(hit);
+    }
+    return r;
+  }
+  static std::vector<std::vector<long>> atom2shell(const std::vector<Atom>& atoms,
+                                                   const std::vector<Shell>& shells) {
+    std::vector<std::vector<long>> r(atoms.size());
+    for (size_t a = 0; a < atoms.size(); ++a)
+      for (size_t k = 0; k < shells.size(); ++k)
+        if (shells[k].O[0] == atoms[a].x && shells[k].O[1] == atoms[a].y &&
+            shells[k].O[2] == atoms[a].z)
+          r[a].push_back(long(k));
+    return r;
+  }
   void set_pure(bool pure) {
     for (auto& s : *this)
       for (auto& c : s.contr) c.pure = pure;

@@ -178,3 +178,43 @@ def test_cpp_facade_api_compiles(tmp_path):
     src.write_text(CPP_FACADE_PROBE)
     subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I",
                            os.path.join(ROOT, "include"), str(src)])
+
+
+BASIS_MAP_PROBE = r"""
+#include <libint2.hpp>
+#include <iostream>
+#include <sstream>
+int main() {
+  std::istringstream xyz("3\n\nO 0 0 0\nH 0 0.757 0.587\nH 0 -0.757 0.587\n");
+  const auto atoms = libint2::read_dotxyz(xyz);
+  libint2::BasisSet obs("cc-pVDZ", atoms);
+  const auto s2a = obs.shell2atom(atoms);
+  const auto a2s = obs.atom2shell(atoms);
+  int bad = 0;
+  for (size_t k = 0; k < obs.size(); ++k) bad += s2a[k] != obs.shell2atom_index()[k];
+  size_t n = 0;
+  for (size_t a = 0; a < a2s.size(); ++a)
+    for (long k : a2s[a]) { bad += s2a[size_t(k)] != long(a); ++n; }
+  bad += n != obs.size();
+  std::vector<libint2::Atom> far = {{1, 9.0, 9.0, 9.0}};
+  bad += libint2::BasisSet::shell2atom(obs, far)[0] != -1;
+  try { libint2::BasisSet::shell2atom(obs, far, true); ++bad; } catch (const std::logic_error&) {}
+  std::cout << obs.size() << " " << bad << std::endl;
+  return bad;
+}
+"""
+
+
+def test_cpp_basis_shell_atom_maps(lgx, tmp_path):
+    # BasisSet::shell2atom / atom2shell of the C++ drop-in (host code only)
+    import subprocess
+    lgx._lgx.load()
+    src = tmp_path / "maps.cpp"
+    src.write_text(BASIS_MAP_PROBE)
+    exe = str(tmp_path / "maps")
+    libdir = os.path.join(ROOT, "libint_gb300")
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           str(src), "-L", libdir, "-llgx", "-Wl,-rpath," + libdir, "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    assert r.stdout.split() == ["12", "0"]
