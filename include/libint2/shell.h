@@ -18,6 +18,7 @@
 #include <limits>
 #include <ostream>
 #include <stdexcept>
+#include <utility>
 #include <vector>
 
 #include "../lgx.h"
@@ -58,6 +59,15 @@ struct Shell {
   Shell& move(std::array<real_t, 3> new_origin) {
     O = new_origin;
     return *this;
+  }
+  /// Shell::extract_primitive (shell.h:930-945): primitive p alone, with
+  /// coefficient 1 in every contraction; normalized when unit_normalized,
+  /// else normalization-free
+  Shell extract_primitive(size_t p, bool unit_normalized = true) const {
+    svector<Contraction> c;
+    c.reserve(contr.size());
+    for (const auto& x : contr) c.push_back(Contraction{x.l, x.pure, {real_t(1)}});
+    return Shell({alpha.at(p)}, c, O, unit_normalized);
   }
   size_t cartesian_size() const {
     size_t s = 0;
@@ -166,6 +176,47 @@ struct ShellPair {
   ShellPair(const Shell& s1, const Shell& s2, Real ln_prec_,
             ScreeningMethod method = default_screening_method()) {
     init(s1, s2, ln_prec_, method);
+  }
+  /// Schwarz / SchwarzInf screening of the primitive pairs (shell.h:1258-1328):
+  /// pair (p1, p2) is kept when log(nprim1 nprim2 K(p1, p2)) + ln|c1| + ln|c2|
+  /// >= ln_prec, K from the caller's evaluator (s1, p1, s2, p2) -> Schwarz
+  /// factor of the primitive pair
+  template <typename Real, typename SchwarzFactorEvaluator>
+  ShellPair(const Shell& s1, const Shell& s2, Real ln_prec_, ScreeningMethod method,
+            SchwarzFactorEvaluator&& schwarz_factor) {
+    init(s1, s2, ln_prec_, method, std::forward<SchwarzFactorEvaluator>(schwarz_factor));
+  }
+  template <typename Real, typename SchwarzFactorEvaluator>
+  void init(const Shell& s1, const Shell& s2, Real ln_prec_, ScreeningMethod method,
+            SchwarzFactorEvaluator&& schwarz_factor) {
+    if (method != ScreeningMethod::Schwarz && method != ScreeningMethod::SchwarzInf)
+      throw std::invalid_argument("ShellPair: the evaluator form takes Schwarz / SchwarzInf");
+    primpairs.clear();
+    double AB2 = 0;
+    for (int i = 0; i < 3; ++i) {
+      AB[i] = s1.O[i] - s2.O[i];
+      AB2 += AB[i] * AB[i];
+    }
+    const double n12 = double(s1.nprim() * s2.nprim());
+    for (size_t p1 = 0; p1 < s1.nprim(); ++p1)
+      for (size_t p2 = 0; p2 < s2.nprim(); ++p2) {
+        const double ln_scr = std::log(n12 * double(schwarz_factor(s1, p1, s2, p2))) +
+                              s1.max_ln_coeff[p1] + s2.max_ln_coeff[p2];
+        if (ln_scr < ln_prec_) continue;
+        const double a1 = s1.alpha[p1], a2 = s2.alpha[p2], oog = 1 / (a1 + a2);
+        PrimPairData d;
+        for (int i = 0; i < 3; ++i)
+          d.P[i] = AB2 == 0 ? s1.O[i] : (a1 * s1.O[i] + a2 * s2.O[i]) * oog;
+        d.K = 5.9149671727956128778 * std::exp(-a1 * a2 * oog * AB2) * oog;
+        d.one_over_gamma = oog;
+        d.nonsph_screen_fac = 0;
+        d.ln_scr = ln_scr;
+        d.p1 = int(p1);
+        d.p2 = int(p2);
+        primpairs.push_back(d);
+      }
+    ln_prec = ln_prec_;
+    screening_method_ = method;
   }
   template <typename Real>
   void init(const Shell& s1, const Shell& s2, Real ln_prec_,

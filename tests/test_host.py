@@ -218,3 +218,42 @@ def test_cpp_basis_shell_atom_maps(lgx, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, (r.stdout, r.stderr)
     assert r.stdout.split() == ["12", "0"]
+
+
+SHELL_PAIR_PROBE = r"""
+#include <libint2.hpp>
+#include <cmath>
+#include <iostream>
+int main() {
+  using libint2::Shell;
+  Shell s({3.0, 0.5}, {{1, false, {0.4, 0.7}}}, {{0.0, 0.0, 0.0}});
+  Shell t({1.2}, {{0, false, {1.0}}}, {{0.0, 0.0, 1.0}});
+  int bad = 0;
+  const Shell p = s.extract_primitive(1, false);
+  bad += p.nprim() != 1 || p.alpha[0] != 0.5 || p.contr[0].coeff[0] != 1.0 || p.contr[0].l != 1;
+  const Shell q = s.extract_primitive(0, true);
+  bad += !(q.contr[0].coeff[0] > 0.0) || q.contr[0].coeff[0] == 1.0;
+  // Schwarz primitive screening: an evaluator that drops primitive 1 of s
+  auto K = [](const Shell&, size_t p1, const Shell&, size_t) { return p1 == 1 ? 1e-30 : 1.0; };
+  libint2::ShellPair sp(s, t, std::log(1e-12), libint2::ScreeningMethod::SchwarzInf, K);
+  bad += sp.primpairs.size() != 1 || sp.primpairs[0].p1 != 0;
+  libint2::ShellPair so(s, t, std::log(1e-12));
+  bad += so.primpairs.size() != 2;
+  std::cout << bad << std::endl;
+  return bad;
+}
+"""
+
+
+def test_cpp_shell_primitive_and_schwarz_pairs(lgx, tmp_path):
+    # Shell::extract_primitive and the Schwarz form of ShellPair (host code)
+    import subprocess
+    src = tmp_path / "sp.cpp"
+    src.write_text(SHELL_PAIR_PROBE)
+    exe = str(tmp_path / "sp")
+    libdir = os.path.join(ROOT, "libint_gb300")
+    lgx._lgx.load()
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           str(src), "-L", libdir, "-llgx", "-Wl,-rpath," + libdir, "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.stdout, r.stderr)
