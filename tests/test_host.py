@@ -257,3 +257,65 @@ def test_cpp_shell_primitive_and_schwarz_pairs(lgx, tmp_path):
                            str(src), "-L", libdir, "-llgx", "-Wl,-rpath," + libdir, "-o", exe])
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, (r.stdout, r.stderr)
+
+
+DERIV_ITER_PROBE = r"""
+#include <libint2.hpp>
+#include <iostream>
+#include <vector>
+int main() {
+  int bad = 0;
+  for (unsigned d = 1; d <= 2; ++d) {
+    libint2::CartesianDerivIterator<4> it(d);
+    intmax_t idx = 0;
+    bool more = true;
+    while (more) {
+      const auto& p = *it;
+      bad += libint2::CartesianDerivIterator<4>::rank(p) != idx;
+      std::cout << d;
+      for (auto v : p) std::cout << ' ' << v;
+      std::cout << '\n';
+      ++idx;
+      more = !it.last();
+      if (more) it.next();
+    }
+    bad += idx != it.range_size();
+  }
+  // resizable form: partitions of 3 into 4 parts
+  libint2::FixedOrderedIntegerPartitionIterator<std::vector<int>> v(3, 4);
+  intmax_t n = 1;
+  while (!v.last()) {
+    v.next();
+    bad += libint2::FixedOrderedIntegerPartitionIterator<std::vector<int>>::rank(*v) != n;
+    ++n;
+  }
+  bad += n != 20 || v.range_size() != 20;
+  std::cerr << "bad " << bad << '\n';
+  return bad;
+}
+"""
+
+
+def test_cpp_deriv_iterator_matches_reference_order(tmp_path):
+    # CartesianDerivIterator<4>: deriv 1 = A_x..D_z, deriv 2 = the reference's
+    # own set order (tests/golden/eri_d2.npz c1 / c2, from its deriv_iter.h)
+    import subprocess
+    from golden_util import load
+    src = tmp_path / "di.cpp"
+    src.write_text(DERIV_ITER_PROBE)
+    exe = str(tmp_path / "di")
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           str(src), "-o", exe, "-L", os.path.join(ROOT, "libint_gb300"), "-llgx",
+                           "-Wl,-rpath," + os.path.join(ROOT, "libint_gb300")])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    rows = [list(map(int, line.split())) for line in r.stdout.splitlines()]
+    d1 = [row[1:] for row in rows if row[0] == 1]
+    d2 = [row[1:] for row in rows if row[0] == 2]
+    assert d1 == [[1 if j == i else 0 for j in range(12)] for i in range(12)]
+    g = load("eri_d2.npz")
+    pairs = []
+    for p in d2:
+        nz = [i for i, v in enumerate(p) for _ in range(v)]
+        pairs.append(tuple(nz))
+    assert pairs == list(zip(g["c1"].tolist(), g["c2"].tolist()))
