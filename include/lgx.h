@@ -303,6 +303,13 @@ int lgx_enforce_unit_normalization(int flag);
 lgx_status lgx_shell_normalize(int l, int nprim, const double* alpha,
                                const double* coeff_in, double* coeff_out);
 
+/* SolidHarmonicsCoefficients::coeff (include/libint2/solidharmonics.h:
+ * 114-174): the coefficient of the Cartesian component x^lx y^ly z^lz in
+ * the real solid harmonic (l, m), m = -l..l, in libint's convention (all
+ * Cartesian components sharing the x^l normalization), as the kernels'
+ * transform uses it; 0 when lx + ly + lz != l or |m| > l. */
+double lgx_solid_coeff(int l, int m, int lx, int ly, int lz);
+
 /* BasisSet(name, atoms) with the G94 reader of basis.h.in:473-621: loads
  * `<data_dir>/<name>.g94` (name canonicalized: lower case, '*'->'_st_')
  * for natoms atoms with atomic numbers Z and positions xyz (bohr).

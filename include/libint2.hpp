@@ -10,6 +10,7 @@
 #include "libint2/basis.h"
 #include "libint2/engine.h"
 #include "libint2/deriv_iter.h"
+#include "libint2/solidharmonics.h"
 #include "libint2/jk.h"
 
 #endif

@@ -633,6 +633,17 @@ class Engine:
         return out
 
 
+class SolidHarmonicsCoefficients:
+    """libint2.SolidHarmonicsCoefficients of the binding (libint2.cc:255-261):
+    coefficient(l, m, lx, ly, lz) of the Cartesian component x^lx y^ly z^lz
+    in the real solid harmonic (l, m) (solidharmonics.h:114-174), the set
+    the kernels' transform uses (lgx_solid_coeff)."""
+
+    @staticmethod
+    def coefficient(l, m, lx, ly, lz) -> float:
+        return float(_lgx.load().lgx_solid_coeff(int(l), int(m), int(lx), int(ly), int(lz)))
+
+
 def coulomb() -> Engine:
     """The reference binding's coulomb() factory: precision 1e-15
     (python/src/libint2/libint2.cc:50-55)."""

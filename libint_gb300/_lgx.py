@@ -127,6 +127,8 @@ SIGNATURES = {
                                    ctypes.c_double, ctypes.POINTER(LgxJkStats)]),
     "lgx_enforce_unit_normalization": (ctypes.c_int, [ctypes.c_int]),
     "lgx_shell_normalize": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
+    "lgx_solid_coeff": (ctypes.c_double, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int]),
     "lgx_basis_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, _ip, _dp,
                                       ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int), _ip, _ip, _ip, _ip, _dp,

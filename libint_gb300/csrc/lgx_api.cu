@@ -2161,6 +2161,11 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int
   return LGX_OK;
 }
 
+double lgx_solid_coeff(int l, int m, int lx, int ly, int lz) {
+  if (l < 0 || lx < 0 || ly < 0 || lz < 0 || lx + ly + lz != l || m < -l || m > l) return 0.0;
+  return solid_coeff(l, m, lx, ly, lz);
+}
+
 lgx_status lgx_compute_primitive_set(lgx_context* ctx, int l1, int l2, int l3, int l4,
                                      int deriv, const lgx_prim_quartet* prims, int nprim,
                                      const double AB[3], const double CD[3], double* out,

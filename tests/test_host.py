@@ -319,3 +319,28 @@ def test_cpp_deriv_iterator_matches_reference_order(tmp_path):
         nz = [i for i, v in enumerate(p) for _ in range(v)]
         pairs.append(tuple(nz))
     assert pairs == list(zip(g["c1"].tolist(), g["c2"].tolist()))
+
+
+def test_cpp_solid_harmonics_header(lgx, tmp_path):
+    # libint2::solidharmonics::SolidHarmonicsCoefficients<double>::coeff from
+    # the C++ drop-in equals the Python mirror's value (host code)
+    import subprocess
+    src = tmp_path / "sh.cpp"
+    src.write_text(r'''
+#include <libint2.hpp>
+#include <cstdio>
+int main() {
+  using C = libint2::solidharmonics::SolidHarmonicsCoefficients<double>;
+  std::printf("%.17g %.17g\n", C::coeff(2, 0, 0, 0, 2), C::coeff(3, -2, 1, 1, 1));
+  return 0;
+}
+''')
+    exe = str(tmp_path / "sh")
+    libdir = os.path.join(ROOT, "libint_gb300")
+    lgx._lgx.load()
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           str(src), "-L", libdir, "-llgx", "-Wl,-rpath," + libdir, "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60).stdout.split()
+    want = [lgx.SolidHarmonicsCoefficients.coefficient(2, 0, 0, 0, 2),
+            lgx.SolidHarmonicsCoefficients.coefficient(3, -2, 1, 1, 1)]
+    assert [float(x) for x in out] == want and want[0] == 1.0

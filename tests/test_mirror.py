@@ -79,3 +79,15 @@ def test_compute_2body_fock_matches_binding_loop(lgx, oracle_mod):
     assert np.max(np.abs(G - ref)) < 1e-12 * max(1.0, np.abs(ref).max())
     with pytest.raises(NotImplementedError):
         lgx.Engine(lgx.Operator.coulomb, deriv_order=1, context=ctx).compute_2body_fock(D, bs)
+
+
+def test_solid_harmonics_coefficients_vs_reference(lgx):
+    # the binding's SolidHarmonicsCoefficients.coefficient against the
+    # reference's own coefficients (tests/golden/solid.npz)
+    from golden_util import load
+    g = load("solid.npz")
+    for (l, m, lx, ly, lz), c in zip(g["idx"], g["coeff"]):
+        got = lgx.SolidHarmonicsCoefficients.coefficient(int(l), int(m), int(lx), int(ly), int(lz))
+        assert abs(got - c) < 1e-13, (l, m, lx, ly, lz)
+    assert lgx.SolidHarmonicsCoefficients.coefficient(2, 3, 2, 0, 0) == 0.0   # |m| > l
+    assert lgx.SolidHarmonicsCoefficients.coefficient(2, 0, 1, 0, 0) == 0.0   # sum != l
