@@ -575,8 +575,7 @@ class Engine:
         rank = self.braket_rank()
         if len(shells) != rank:
             raise ValueError("compute: %s takes %d shells" % (self.braket.name, rank))
-        if len(shells) == 4 and all(isinstance(s, BasisSet) or isinstance(s, list)
-                                    for s in shells) and not isinstance(shells[0], Shell):
+        if all(isinstance(s, (BasisSet, list)) for s in shells):
             return self._compute_basis(*shells)
         for s in shells:
             if s.l > self.max_l:
@@ -616,20 +615,21 @@ class Engine:
         J, K, _ = ctx.jk(np.asarray(D, dtype=float), 0.0)
         return 2.0 * J - K
 
-    def _compute_basis(self, A, B, C, D):
-        nb = [sum(s.size() for s in X) for X in (A, B, C, D)]
+    def _compute_basis(self, *bases):
+        """The binding's compute over basis sets (parallel_compute,
+        engine.cc:146-157): the full array (nbf of each argument), block by
+        block from the shell sets (first set for derivatives); screened-out
+        blocks are zero."""
+        import itertools
+        nb = [sum(s.size() for s in X) for X in bases]
         out = np.zeros(nb)
-        offs = [np.cumsum([0] + [s.size() for s in X]) for X in (A, B, C, D)]
-        for i, a in enumerate(A):
-            for j, b in enumerate(B):
-                for k, c in enumerate(C):
-                    for l, d in enumerate(D):
-                        r = self.compute(a, b, c, d)
-                        if r is None:
-                            continue
-                        blk = r if self.deriv_order == 0 else r[0]
-                        out[offs[0][i]:offs[0][i + 1], offs[1][j]:offs[1][j + 1],
-                            offs[2][k]:offs[2][k + 1], offs[3][l]:offs[3][l + 1]] = blk
+        offs = [np.cumsum([0] + [s.size() for s in X]) for X in bases]
+        for idx in itertools.product(*[range(len(X)) for X in bases]):
+            r = self.compute(*[X[i] for X, i in zip(bases, idx)])
+            if r is None:
+                continue
+            blk = r if self.deriv_order == 0 else r[0]
+            out[tuple(slice(offs[k][i], offs[k][i + 1]) for k, i in enumerate(idx))] = blk
         return out
 
 

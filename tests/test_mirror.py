@@ -91,3 +91,36 @@ def test_solid_harmonics_coefficients_vs_reference(lgx):
         assert abs(got - c) < 1e-13, (l, m, lx, ly, lz)
     assert lgx.SolidHarmonicsCoefficients.coefficient(2, 3, 2, 0, 0) == 0.0   # |m| > l
     assert lgx.SolidHarmonicsCoefficients.coefficient(2, 0, 1, 0, 0) == 0.0   # sum != l
+
+
+class _OracleShellsetContext(_OracleContext):
+    """Stand-in for Context: shell sets from the oracle."""
+
+    def compute_shellset(self, shells, deriv=0, precision=0.0, screening=0):
+        import libint_gb300 as lg
+        ob = self.o.OracleBasis.from_basis(lg.BasisSet(list(shells)))
+        return self.o.compute_quartet(ob, 0, 1, 2, 3, deriv=deriv, precision=precision)
+
+
+def test_compute_over_basis_sets_all_ranks(lgx, oracle_mod):
+    # Engine.compute(basis, ...) for xx_xx, xs_xx, xs_xs: full arrays whose
+    # blocks are the shell sets (the binding's compute2/3/4 over BasisSet)
+    atoms = [(1, (0.0, 0.0, 0.0)), (1, (0.0, 0.0, 1.4))]
+    obs = lgx.BasisSet("cc-pVDZ", atoms)
+    aux = list(lgx.BasisSet("cc-pVDZ-jkfit", atoms))[:4]
+    ctx = _OracleShellsetContext(oracle_mod)
+    for bk, args in ((lgx.BraKet.xs_xs, (aux, aux)), (lgx.BraKet.xs_xx, (aux, obs, obs)),
+                     (lgx.BraKet.xx_xx, (list(obs)[:3],) * 4)):
+        eng = lgx.Engine(lgx.Operator.coulomb, braket=bk, context=ctx)
+        full = eng.compute(*args)
+        sizes = [[s.size() for s in X] for X in args]
+        assert full.shape == tuple(sum(x) for x in sizes)
+        # one block against a direct shell-set call
+        blk = eng.compute(*[X[1] for X in args])
+        sl = tuple(slice(x[0], x[0] + x[1]) for x in sizes)
+        assert np.array_equal(full[sl], blk)
+    # (P|Q) symmetric, (P|ab) symmetric in a, b
+    V = lgx.Engine(lgx.Operator.coulomb, braket=lgx.BraKet.xs_xs, context=ctx).compute(aux, aux)
+    assert np.allclose(V, V.T, atol=1e-13)
+    B = lgx.Engine(lgx.Operator.coulomb, braket=lgx.BraKet.xs_xx, context=ctx).compute(aux, obs, obs)
+    assert np.allclose(B, B.transpose(0, 2, 1), atol=1e-13)
