@@ -124,3 +124,20 @@ def test_compute_over_basis_sets_all_ranks(lgx, oracle_mod):
     assert np.allclose(V, V.T, atol=1e-13)
     B = lgx.Engine(lgx.Operator.coulomb, braket=lgx.BraKet.xs_xx, context=ctx).compute(aux, obs, obs)
     assert np.allclose(B, B.transpose(0, 2, 1), atol=1e-13)
+
+
+def test_reference_python_test_core(lgx):
+    # the reference's python/tests/test_libint2.py test_core against the
+    # mirror: 6-31G water has 9 shells; the basis-wide pure setter and a
+    # per-shell pure write through basis[i]
+    h2o = [(8, [0.0, -0.07579, 0.0]), (1, [0.86681, 0.60144, 0.0]),
+           (1, [-0.86681, 0.60144, 0.0])]
+    assert lgx.MAX_AM > 0
+    basis = lgx.BasisSet("6-31g", h2o)
+    assert len(basis) == 9
+    basis.pure = False
+    pure = [False] * len(basis)
+    assert [s.pure for s in basis] == pure
+    basis[0].pure = True
+    pure[0] = True
+    assert [s.pure for s in basis] == pure
