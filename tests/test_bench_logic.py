@@ -1,0 +1,46 @@
+"""Host logic of bench.py without a GPU: the roofline of the dominant class
+launch from per-launch records, and the caller-side Boys values used to
+prepare the generated-library inputs (against the oracle)."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_kernel_roofline_picks_dominant_launch():
+    import bench
+    launches = [
+        {"class": (0, 0, 1, 0), "fp32": 0, "kernel": "register", "ms_avg": 30.0,
+         "flops": 1.5e10, "prim_quartets": 10, "quartets": 5},
+        {"class": (1, 0, 1, 0), "fp32": 1, "kernel": "register", "ms_avg": 10.0,
+         "flops": 2.0e11, "prim_quartets": 20, "quartets": 7},
+    ]
+    peaks = {"fp64": 1.1, "fp32": 70.0}
+    r = bench.kernel_roofline(launches, peaks, "h2o32_cc-pvdz", "mixed")
+    assert r["kernel"] == "rk_kernel<double,0,0,1,0,J/K>"
+    assert abs(r["achieved"] - 1.5e10 / 0.030 / 1e12) < 1e-12
+    assert abs(r["frac"] - r["achieved"] / 1.1) < 1e-12
+    assert abs(r["share_of_pass"] - 0.75) < 1e-12 and r["bound"] == "fp64-pipe"
+    assert bench.kernel_roofline([], peaks, "x", "mixed") is None
+
+
+def test_primitive_inputs_boys_match_oracle():
+    # the scipy Boys values bench.py uses for --primitive-api inputs
+    import bench
+    import libint_gb300 as lg
+    from oracle import oracle
+    oracle.build()
+    rng = np.random.default_rng(3)
+    sh, prims, AB, CD = bench._prim_inputs(rng, (1, 0, 2, 1), 2, 1, lg._lgx.PRIM_DTYPE)
+    assert len(prims) == 16
+    for r in prims[:4]:
+        # ss[m] / ss[0] = F_m(T) / F_0(T); recover T from the records
+        P_Q = (r["PA"] + sh[0][3]) - (r["QC"] + sh[2][3])
+        rho = r["roz"] / (2.0 * r["oo2z"])
+        T = rho * float(np.dot(P_Q, P_Q))
+        F = np.asarray(oracle.boys(T, 5))
+        got = r["ss"][:6] / r["ss"][0]
+        assert np.allclose(got, F / F[0], rtol=1e-12, atol=0)
