@@ -242,6 +242,18 @@ def run_reference(args):
     return 0
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The slowest rank's value: an all-reduce MAX over the process group
+    when world > 1 (one process per GPU; the ranks' timed regions are
+    bracketed by barriers), the value itself otherwise."""
+    if world <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args):
     import torch
     import libint_gb300 as lg
@@ -303,12 +315,7 @@ def run_gpu(args):
     clocks = clk.summary()
 
     def agg(ms):
-        t = float(np.sum(ms))
-        if world > 1:
-            tt = torch.tensor([t], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t = float(tt.item())
-        return t
+        return max_over_ranks(float(np.sum(ms)), world)
 
     t64 = agg(ms64) / 1e3
     tmx = agg(msmx) / 1e3
@@ -335,6 +342,7 @@ def run_gpu(args):
         flush.zero_()
         torch.cuda.synchronize()
     te2e -= time.perf_counter() - f0
+    te2e = max_over_ranks(te2e, world)
     ve2e = world * st_e.integrals * args.steps / te2e
 
     # roofline of the whole mixed pass: time at peak for its FP64 and FP32 work

@@ -44,3 +44,43 @@ def test_primitive_inputs_boys_match_oracle():
         F = np.asarray(oracle.boys(T, 5))
         got = r["ss"][:6] / r["ss"][0]
         assert np.allclose(got, F / F[0], rtol=1e-12, atol=0)
+
+
+def _max_rank_worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    q.put((rank, bench.max_over_ranks(1.5 + rank, world, device="cpu")))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_two_processes():
+    # the N > 1 reduction of bench.py (slowest rank's time) on two gloo ranks
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_max_rank_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert got == [(0, 2.5), (1, 2.5)]
+    import bench
+    assert bench.max_over_ranks(3.25, 1) == 3.25
+
+
+def test_reference_arm_other_ranks_exit_without_work(monkeypatch):
+    # under torchrun only rank 0 times the CPU reference; the others exit 0
+    import bench
+    monkeypatch.setenv("RANK", "1")
+    args = bench.argparse.Namespace(workload="h2o32_cc-pvdz", steps=1, warmup=1, gpus=2,
+                                    ref_budget=1.0)
+    assert bench.run_reference(args) == 0
