@@ -1,7 +1,8 @@
 """Host logic: the per-class VRR/HRR programs executed on the CPU by a test
 interpreter (tests/cpp/program_interp.cpp) reproduce the oracle's canonical
-Cartesian shell sets for every class up to (ff|ff) (deriv 0) and (dd|dd)
-plus f classes (deriv 1)."""
+Cartesian shell sets for every class up to (ff|ff) (deriv 0), (dd|dd) plus
+f classes (deriv 1), and the internal g classes of the second-derivative
+composition (deriv 1)."""
 import ctypes
 import itertools
 import os
@@ -67,5 +68,14 @@ def test_programs_deriv0(interp, oracle_mod):
 def test_programs_deriv1(interp, oracle_mod):
     rng = np.random.default_rng(1)
     classes = [c for c in canonical_classes(3) if sum(c) <= 6]
+    worst = max(_run(interp, oracle_mod, ls, 1, rng) for ls in classes)
+    assert worst < 1e-12, worst
+
+
+def test_programs_deriv1_internal_g_classes(interp, oracle_mod):
+    # the Cartesian g classes the second-derivative composition raises f
+    # shells to (first derivatives of one shell raised by a quantum)
+    rng = np.random.default_rng(7)
+    classes = [(0, 0, 4, 0), (1, 0, 4, 1), (2, 1, 4, 0), (2, 0, 4, 2), (3, 0, 4, 1), (3, 3, 4, 3)]
     worst = max(_run(interp, oracle_mod, ls, 1, rng) for ls in classes)
     assert worst < 1e-12, worst
