@@ -2,16 +2,25 @@
 (one "step" = one Schwarz-screened J/K pass over all unique shell quartets
 of a synthetic water cluster), FP64 and mixed FP32/FP64, on 1 GPU.
 
+Default workload: (H2O)64 / cc-pVTZ on a 4x4x4 grid, Schwarz 1e-12 (3712
+basis functions, 1.95e10 screened quartets, 5.4e11 integrals per pass).
+
 Prints ONE JSON line (rank 0).  `value` = mixed-precision ERIs/s with D, J,
 K resident in HBM (device time of the whole pass from CUDA events on the
-launching stream, L2 flushed between steps); `e2e` = the same metric
-through the host-buffer API (lgx_jk: host D in, host J/K out, copies
-timed); `fp64` = the plain FP64 path; `cpu_baseline` = the CPU oracle
-(FP64 restatement of libint's algorithm) on a bounded sample of the same
-screened quartet space, all host threads.
+launching stream, L2 flushed between steps, over --steps passes); `e2e` =
+the same metric through the host-buffer API (lgx_jk: host D in, host J/K
+out, copies inside each step's timed interval, the L2 flush outside it);
+`fp64` = the plain FP64 path over its own, smaller step count
+(--fp64-steps); `cpu_baseline` = the CPU oracle (FP64 restatement of
+libint's Engine and of compute_2body_fock's digestion) on a fixed sample
+of the same screened pass, all host threads.
 
---impl reference times that CPU implementation alone (the reference libint
-library cannot be built here, so its algorithm restated in C++ stands in).
+--impl reference times that CPU implementation alone, built from the
+oracle's own inputs (its G94 reader, cluster construction and Schwarz
+factors), so it loads no part of the GPU library.  The reference libint
+library itself cannot be built here (its generated integral code needs
+Boost.MPL and GMP, its Engine Eigen), so its algorithm restated in C++
+stands in for it.
 """
 from __future__ import annotations
 
@@ -37,11 +46,18 @@ WORKLOADS = {
     "h2o4_cc-pvdz": ((2, 2, 1), "cc-pVDZ", 0.0, "(H2O)4 cc-pVDZ 2x2x1 grid, no screening"),
     "h2o8_cc-pvtz": ((2, 2, 2), "cc-pVTZ", 1e-12, "(H2O)8 cc-pVTZ 2x2x2 grid, Schwarz 1e-12"),
 }
+DEFAULT_WORKLOAD = "h2o64_cc-pvtz"
 MIXED_THRESH = 1e-4
 SEED = 2024
+# CPU sample: this many bra shell pairs (a fixed, seeded, class-stratified
+# draw from the significant pairs), whatever the time budget or core count
+CPU_SAMPLE_PAIRS = 1024
+# pair subset of the oracle comparison of the full J/K kernels
+CHECK_SUBSET_PAIRS = 3000
 
 
 def build_inputs(name):
+    """GPU arm: atoms, basis (the product's loader), density."""
     import libint_gb300 as lg
     grid, basis, thresh, desc = WORKLOADS[name]
     atoms = lg.water_cluster(*grid, spacing=3.0, jitter=0.2, seed=SEED)
@@ -49,6 +65,86 @@ def build_inputs(name):
     nwater = grid[0] * grid[1] * grid[2]
     D = lg.random_density(bs.nbf, 5 * nwater, seed=SEED + 1)
     return atoms, bs, D, thresh, desc
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+class CpuArm:
+    """The CPU implementation of the path (the oracle: libint's Engine
+    algorithm and compute_2body_fock's digestion restated in C++, OpenMP over
+    bra shell pairs) on the workload, with inputs from the oracle's own
+    loaders and its own Schwarz factors (compute_schwarz_ints,
+    hartree-fock++.cc:1231-1298), so nothing of the GPU library is loaded.
+
+    A step is the fixed sample of CPU_SAMPLE_PAIRS bra shell pairs with all
+    their kets of the screened pass; ERIs/s = the sample's integrals over its
+    time, which estimates the full pass's rate (every significant pair is
+    drawn with the same probability, stratified by pair class).  The full
+    pass's time is extrapolated from the sample plus the one reduction of
+    the per-thread accumulators that a full pass makes."""
+
+    def __init__(self, workload, nthreads=0, npairs=CPU_SAMPLE_PAIRS):
+        from oracle import inputs, oracle
+        oracle.build()
+        self.oracle = oracle
+        grid, basis, self.thresh, self.desc = WORKLOADS[workload]
+        atoms = inputs.water_cluster(*grid, spacing=3.0, jitter=0.2, seed=SEED)
+        self.ob = inputs.load_basis(basis, atoms)
+        self.basis_name = basis
+        nwater = grid[0] * grid[1] * grid[2]
+        self.D = inputs.random_density(self.ob.nbf, 5 * nwater, seed=SEED + 1)
+        self.nthreads = nthreads or cpu_threads()
+        t0 = time.perf_counter()
+        self.K = oracle.schwarz(self.ob, self.nthreads)
+        self.t_schwarz = time.perf_counter() - t0
+        self.total_quartets, self.total_integrals = oracle.count_screened(self.ob, self.K,
+                                                                          self.thresh)
+        self.pairs = sample_pairs(self.ob, self.K, self.thresh, npairs, SEED + 7)
+        self.acc = oracle.JKAccumulator(self.ob.nbf, self.nthreads)
+
+    def step(self):
+        t0 = time.perf_counter()
+        nq, nint = self.acc.add_pairs(self.ob, self.D, self.K, self.thresh, self.pairs)
+        return nint, time.perf_counter() - t0
+
+    def reduce_seconds(self):
+        t0 = time.perf_counter()
+        self.acc.reduce()
+        return time.perf_counter() - t0
+
+    def describe(self, nint, seconds):
+        return ("%d bra shell pairs (seeded draw of the significant pairs, stratified by pair "
+                "class), all their kets: %d integrals, %.1f s per step; the full pass has %d "
+                "integrals" % (len(self.pairs), nint, seconds, self.total_integrals))
+
+    def close(self):
+        self.acc.close()
+
+
+def sample_pairs(ob, K, thresh, npairs, seed):
+    """A fixed draw of bra shell pairs (canonical indices s1 (s1+1)/2 + s2)
+    among the significant ones (K12 max K >= thresh), stratified by pair
+    class (l1, l2) in proportion to the class sizes."""
+    ns = ob.nshell
+    s1, s2 = np.tril_indices(ns)
+    kp = K[s1, s2]
+    sig = kp * K.max() >= thresh
+    l = ob.l
+    cls = np.maximum(l[s1], l[s2]) * 8 + np.minimum(l[s1], l[s2])
+    idx = s1.astype(np.int64) * (s1 + 1) // 2 + s2
+    rng = np.random.default_rng(seed)
+    n_sig = int(sig.sum())
+    take = []
+    for c in np.unique(cls[sig]):
+        members = idx[sig & (cls == c)]
+        k = max(1, int(round(npairs * len(members) / n_sig)))
+        take.append(rng.choice(members, min(k, len(members)), replace=False))
+    return np.sort(np.concatenate(take))
 
 
 class ClockSampler:
@@ -132,18 +228,12 @@ def measure_peaks(torch):
     return out
 
 
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
-# a class kernel in the timed pass, from an ncu launch list of this same
-# bench command on the full workload (one-pass metrics; the summary and the
-# command line are in profiles/launches_dram_jk_h2o32_cc-pvdz.md).  Keyed by
-# (workload, pass precision mode, kernel).  The traffic does not grow with
-# the primitive quartets (it is the cold read of the pair records, the
-# density and the Boys table), so it is not scaled to other workloads.
-NCU_TRAFFIC_BYTES = {
-    ("h2o32_cc-pvdz", "mixed", "rk_kernel<double,0,0,1,0,J/K>"): 11.6e6,
-    ("h2o32_cc-pvdz", "fp64", "rk_kernel<double,0,0,1,0,J/K>"): 29.9e6,
-    ("h2o32_cc-pvdz", "mixed", "rk_kernel<double,0,0,0,0,J/K>"): 8.2e6,
-    ("h2o32_cc-pvdz", "fp64", "rk_kernel<double,0,0,0,0,J/K>"): 19.1e6,
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+# of the dominant class kernel, from a one-pass ncu capture of that launch
+# in this benchmark's workload (the command and figures are in the profiles/
+# summary named beside each entry).  Not measured in the run that prints it.
+NCU_TRAFFIC = {
+    # (workload, pass mode, kernel): (bytes per launch, profiles/ summary)
 }
 
 
@@ -159,8 +249,9 @@ def kernel_name(r):
 
 def kernel_roofline(launches, peaks, workload, mode):
     """Roofline of the dominant class launch of a pass (largest average
-    device time over the timed steps): its algorithmic FLOPs per launch over
-    its average duration, against the FP64 or FP32 pipe peak measured live
+    device time): its algorithmic FLOPs per launch (the class's operation
+    counts from the equations, see lgx_api.cu prologue_flops) over its
+    average duration, against the FP64 or FP32 pipe peak measured live
     (cuBLAS DGEMM / SGEMM without TF32)."""
     if not launches:
         return None
@@ -169,75 +260,57 @@ def kernel_roofline(launches, peaks, workload, mode):
     pipe = "fp32" if r["fp32"] else "fp64"
     ach = r["flops"] / (r["ms_avg"] * 1e-3) / 1e12
     name = kernel_name(r)
-    return {"bound": pipe + "-pipe", "kernel": name, "achieved": ach, "peak": peaks[pipe],
-            "unit": "TFLOP/s", "frac": ach / peaks[pipe],
-            "traffic": NCU_TRAFFIC_BYTES.get((workload, mode, name)),
-            "launch_ms": r["ms_avg"], "share_of_pass": r["ms_avg"] / total if total else None,
-            "flops_per_launch": r["flops"], "prim_quartets": r["prim_quartets"],
-            "quartets": r["quartets"],
-            "peak_source": "cuBLAS %s measured live in this run (MEASURED_PEAKS.json holds "
-                           "only HBM and bf16 figures)" % ("SGEMM, no TF32" if r["fp32"]
-                                                           else "DGEMM")}
-
-
-def cpu_baseline(bs, D, Kq, thresh, budget_s, nthreads=0):
-    """Oracle J/K over bounded samples of bra shell pairs spread across the
-    canonical quartet enumeration; returns ERIs/s and the sample size."""
-    from oracle import oracle
-    ob = oracle.OracleBasis.from_basis(bs)
-    ns = len(bs)
-    npairs = ns * (ns + 1) // 2
-    # chunks at 8 positions of the pair range, grown until the budget is used
-    chunk = 1
-    nint_tot, t_tot, npair_tot = 0, 0.0, 0
-    positions = [int(npairs * f) for f in (0.05, 0.2, 0.35, 0.5, 0.65, 0.8, 0.9, 0.97)]
-    while t_tot < budget_s and chunk < npairs:
-        for p0 in positions:
-            p1 = min(npairs, p0 + chunk)
-            t0 = time.perf_counter()
-            _, _, nq, nint = oracle.jk_sample(ob, D, Kq, thresh, p0, p1, nthreads)
-            t_tot += time.perf_counter() - t0
-            nint_tot += nint
-            npair_tot += p1 - p0
-        chunk *= 2
-    return nint_tot / t_tot, nint_tot, t_tot, npair_tot
+    tr = NCU_TRAFFIC.get((workload, mode, name))
+    out = {"bound": pipe + "-pipe", "kernel": name, "achieved": ach, "peak": peaks[pipe],
+           "unit": "TFLOP/s", "frac": ach / peaks[pipe],
+           "traffic": tr[0] if tr else None,
+           "launch_ms": r["ms_avg"], "share_of_pass": r["ms_avg"] / total if total else None,
+           "flops_per_launch": r["flops"], "prim_quartets": r["prim_quartets"],
+           "quartets": r["quartets"],
+           "peak_source": "cuBLAS %s measured live in this run (MEASURED_PEAKS.json holds "
+                          "no FP64/FP32 CUDA-core figure)" % ("SGEMM, no TF32" if r["fp32"]
+                                                              else "DGEMM")}
+    if tr:
+        out["traffic_source"] = "ncu capture of this workload's launch, not this run: " + tr[1]
+    return out
 
 
 def run_reference(args):
     """--impl reference: the CPU implementation of the path (oracle port of
-    libint's Engine + compute_2body_fock digestion), all host threads."""
+    libint's Engine + compute_2body_fock digestion) on all host threads,
+    rank 0 only; each step is the same fixed sample of the screened pass."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import libint_gb300 as lg
-    from oracle import oracle
-    oracle.build()
-    atoms, bs, D, thresh, desc = build_inputs(args.workload)
-    ctx = lg.Context(int(os.environ.get("LOCAL_RANK", "0")))
-    ctx.set_basis(bs)
-    Kq = ctx.schwarz()  # the screening list input, shared with the GPU arm
-    ctx.close()
-    cores = os.cpu_count()
-    per_step = max(2.0, args.ref_budget / max(1, args.steps + args.warmup))
-    vals = []
+    arm = CpuArm(args.workload)
+    per = []
     for i in range(args.warmup + args.steps):
-        v, nint, t, npair = cpu_baseline(bs, D, Kq, thresh, per_step)
+        nint, t = arm.step()
         if i >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
+            per.append((nint, t))
+    t_red = arm.reduce_seconds()
+    nint = per[0][0]
+    tsum = sum(t for _, t in per)
+    value = nint * len(per) / tsum
+    t_step = tsum / len(per)
+    full_s = t_step * arm.total_integrals / nint + t_red
     line = {
         "impl": "reference", "metric": "screened ERIs/s per J/K build", "value": value,
         "unit": "ERI/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "basis": bs.name, "nbf": bs.nbf, "nshell": len(bs),
-                   "schwarz_thresh": thresh},
-        "cpu_baseline": {"value": value, "unit": "ERI/s", "cores": cores, "kind": "port",
-                         "sample": "oracle J/K over bra-pair chunks at 8 positions of the "
-                                   "canonical quartet enumeration, %.1f s per step" % per_step},
+        "config": {"workload": arm.desc, "basis": arm.basis_name, "nbf": arm.ob.nbf,
+                   "nshell": arm.ob.nshell, "schwarz_thresh": arm.thresh,
+                   "integrals_per_pass": arm.total_integrals,
+                   "quartets_per_pass": arm.total_quartets},
+        "cpu_baseline": {"value": value, "unit": "ERI/s", "cores": arm.nthreads, "kind": "port",
+                         "sample": arm.describe(nint, t_step),
+                         "full_pass_s_extrapolated": full_s,
+                         "schwarz_s": arm.t_schwarz},
         "e2e": {"value": value, "unit": "ERI/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    arm.close()
     print(json.dumps(line))
     return 0
 
@@ -252,6 +325,47 @@ def max_over_ranks(value, world, device="cuda"):
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
     torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     return float(t.item())
+
+
+def oracle_subset_check(lg, bs, D, thresh, local, modes, npairs=CHECK_SUBSET_PAIRS):
+    """J/K of the GPU pass restricted to a pair subset (lgx_set_pair_subset:
+    every quartet whose bra and ket pairs are both in the subset) against the
+    oracle's J/K over the same quartets: energy and element errors per
+    precision mode, with the oracle as the FP64 reference."""
+    import torch
+    from oracle import oracle
+    ob = oracle.OracleBasis.from_basis(bs)
+    K = oracle.schwarz(ob, cpu_threads())
+    pairs = sample_pairs(ob, K, thresh, npairs, SEED + 11)
+    acc = oracle.JKAccumulator(ob.nbf, cpu_threads())
+    nq, nint = acc.add_pairs(ob, D, K, thresh, pairs, ket_subset=True)
+    Jo, Ko = acc.reduce()
+    acc.close()
+    EJo, EKo = lg.jk_energies(D, Jo, Ko)
+    s1 = (np.sqrt(8.0 * pairs + 1) - 1).astype(np.int64) // 2
+    s1 = np.where(s1 * (s1 + 1) // 2 > pairs, s1 - 1, s1)
+    s1 = np.where((s1 + 1) * (s1 + 2) // 2 <= pairs, s1 + 1, s1)
+    s2 = pairs - s1 * (s1 + 1) // 2
+    os.environ["LGX_TUNE"] = "0"
+    ctx = lg.Context(local)
+    del os.environ["LGX_TUNE"]
+    ctx.set_basis(bs)
+    ctx.set_pair_subset(np.stack([s1, s2], 1))
+    dD = torch.tensor(D, device="cuda")
+    dJ, dK = torch.empty_like(dD), torch.empty_like(dD)
+    out = {"pairs": int(len(pairs)), "quartets": int(nq), "integrals": int(nint),
+           "E_J_oracle": EJo, "E_K_oracle": EKo}
+    for name, mode in modes:
+        st = ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, mode,
+                           MIXED_THRESH)
+        J, Kx = dJ.cpu().numpy(), dK.cpu().numpy()
+        EJ, EK = lg.jk_energies(D, J, Kx)
+        out[name] = {"dE_J": abs(EJ - EJo), "dE_K": abs(EK - EKo),
+                     "max_abs_dJ": float(np.max(np.abs(J - Jo))),
+                     "max_abs_dK": float(np.max(np.abs(Kx - Ko))),
+                     "gpu_quartets": int(st.quartets_fp64 + st.quartets_fp32)}
+    ctx.close()
+    return out
 
 
 def run_gpu(args):
@@ -278,13 +392,12 @@ def run_gpu(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def timed(mode):
-        for _ in range(args.warmup):
+    def timed(mode, warmup, steps):
+        for _ in range(warmup):
             ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, mode, MIXED_THRESH)
         barrier()
         ms, last, launches = [], None, None
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
             last = ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, mode,
@@ -301,17 +414,31 @@ def run_gpu(args):
                 for r, x in zip(launches, rec):
                     r["ms_sum"] += x["ms"]
         barrier()
-        wall = time.perf_counter() - t0
         for r in launches or []:
-            r["ms_avg"] = r.pop("ms_sum") / args.steps
-        return ms, last, wall, launches
+            r["ms_avg"] = r.pop("ms_sum") / steps
+        return ms, last, launches
 
     peaks = measure_peaks(torch)
     with ClockSampler(local) as clk:
-        ms64, st64, wall64, lau64 = timed(lg._lgx.LGX_FP64)
+        ms64, st64, lau64 = timed(lg._lgx.LGX_FP64, args.fp64_warmup, args.fp64_steps)
         J64, K64 = dJ.cpu().numpy(), dK.cpu().numpy()
-        msmx, stmx, wallmx, laumx = timed(lg._lgx.LGX_MIXED)
+        msmx, stmx, laumx = timed(lg._lgx.LGX_MIXED, args.warmup, args.steps)
         Jmx, Kmx = dJ.cpu().numpy(), dK.cpu().numpy()
+
+        # e2e: host buffers through the public API (lgx_jk: D copied in, the
+        # pass, J and K copied out); each step's interval brackets that call
+        # alone, the L2 flush before it stays outside
+        for _ in range(1):
+            ctx.jk(D, thresh, lg._lgx.LGX_MIXED, MIXED_THRESH)
+        barrier()
+        te2e = 0.0
+        for _ in range(args.e2e_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            J_h, K_h, st_e = ctx.jk(D, thresh, lg._lgx.LGX_MIXED, MIXED_THRESH)
+            te2e += time.perf_counter() - t0
+        barrier()
     clocks = clk.summary()
 
     def agg(ms):
@@ -319,31 +446,12 @@ def run_gpu(args):
 
     t64 = agg(ms64) / 1e3
     tmx = agg(msmx) / 1e3
-    v64 = world * st64.integrals * args.steps / t64
+    te2e = max_over_ranks(te2e, world)
+    v64 = world * st64.integrals * args.fp64_steps / t64
     vmx = world * stmx.integrals * args.steps / tmx
+    ve2e = world * st_e.integrals * args.e2e_steps / te2e
     e64 = lg.jk_energies(D, J64, K64)
     emx = lg.jk_energies(D, Jmx, Kmx)
-
-    # e2e: host buffers through the public API, copies inside the timed region
-    J_h = np.zeros((nbf, nbf)); K_h = np.zeros((nbf, nbf))
-    for _ in range(max(1, args.warmup // 2)):
-        ctx.jk(D, thresh, lg._lgx.LGX_MIXED, MIXED_THRESH)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        J_h, K_h, st_e = ctx.jk(D, thresh, lg._lgx.LGX_MIXED, MIXED_THRESH)
-    barrier()
-    te2e = time.perf_counter() - t0
-    # remove the flush time, measured separately
-    f0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-    te2e -= time.perf_counter() - f0
-    te2e = max_over_ranks(te2e, world)
-    ve2e = world * st_e.integrals * args.steps / te2e
 
     # roofline of the whole mixed pass: time at peak for its FP64 and FP32 work
     fl64, fl32 = stmx.flops_fp64, stmx.flops_fp32
@@ -351,7 +459,7 @@ def run_gpu(args):
     t_step = tmx / args.steps
     achieved = (fl64 + fl32) / t_step / 1e12
     peak_blend = (fl64 + fl32) / t_min / 1e12
-    roof64 = st64.flops_fp64 / (t64 / args.steps) / 1e12
+    roof64 = st64.flops_fp64 / (t64 / args.fp64_steps) / 1e12
     dom = kernel_roofline(laumx, peaks, args.workload, "mixed")
     dom64 = kernel_roofline(lau64, peaks, args.workload, "fp64")
     # the timed passes run class launches on parallel branches, so a launch
@@ -361,9 +469,8 @@ def run_gpu(args):
     ser = lg.Context(local)
     del os.environ["LGX_OVERLAP"]
     ser.set_basis(bs)
-    for _ in range(2):
-        ser.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, lg._lgx.LGX_MIXED,
-                      MIXED_THRESH)
+    ser.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, lg._lgx.LGX_MIXED,
+                  MIXED_THRESH)
     flush.zero_()
     torch.cuda.synchronize()
     ser.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, lg._lgx.LGX_MIXED,
@@ -373,7 +480,7 @@ def run_gpu(args):
         r["ms_avg"] = r["ms"]
     dom_ser = kernel_roofline(lau_ser, peaks, args.workload, "mixed")
     dom64_ser = None
-    if t64 / args.steps < 5.0:  # the FP64 pass too, when it is short
+    if t64 / args.fp64_steps < 5.0:  # the FP64 pass too, when it is short
         ser.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, lg._lgx.LGX_FP64,
                       MIXED_THRESH)
         flush.zero_()
@@ -396,13 +503,20 @@ def run_gpu(args):
 
     if rank != 0:
         return 0
+    subset = None
+    if not args.no_check:
+        subset = oracle_subset_check(lg, bs, D, thresh, local,
+                                     (("fp64", lg._lgx.LGX_FP64), ("mixed", lg._lgx.LGX_MIXED)))
     cpu = None
     if not args.no_cpu:
-        Kq = ctx.schwarz()
-        v, nint, t, npair = cpu_baseline(bs, D, Kq, thresh, args.cpu_budget)
-        cpu = {"value": v, "unit": "ERI/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "%d integrals from %d bra shell pairs at 8 positions of the "
-                         "screened quartet enumeration, %.1f s" % (nint, npair, t)}
+        arm = CpuArm(args.workload)
+        arm.step()  # first touch of the sample's code and data
+        nint, tc = arm.step()
+        t_red = arm.reduce_seconds()
+        cpu = {"value": nint / tc, "unit": "ERI/s", "cores": arm.nthreads, "kind": "port",
+               "sample": arm.describe(nint, tc),
+               "full_pass_s_extrapolated": tc * arm.total_integrals / nint + t_red}
+        arm.close()
     line = {
         "metric": "screened ERIs/s per J/K build",
         "value": vmx, "unit": "ERI/s", "n_gpus": world, "steps": args.steps,
@@ -415,16 +529,19 @@ def run_gpu(args):
                    "quartets_fp64": stmx.quartets_fp64, "quartets_fp32": stmx.quartets_fp32,
                    "integrals_per_step": stmx.integrals,
                    "prim_quartets_per_step": stmx.prim_quartets},
-        "fp64": {"value": v64, "unit": "ERI/s", "ms_per_step": t64 / args.steps * 1e3,
+        "fp64": {"value": v64, "unit": "ERI/s", "dtype": "f64", "steps": args.fp64_steps,
+                 "warmup": args.fp64_warmup, "ms_per_step": t64 / args.fp64_steps * 1e3,
                  "quartets": st64.quartets_fp64, "E_J": e64[0], "E_K": e64[1],
                  "roofline": dom64_ser or dom64,
                  "roofline_concurrent": dom64,
                  "roofline_pass": {"bound": "fp64-pipe", "achieved": roof64,
                                    "peak": peaks["fp64"], "unit": "TFLOP/s",
                                    "frac": roof64 / peaks["fp64"]}},
-        "mixed_error": {"dE_J": abs(emx[0] - e64[0]), "dE_K": abs(emx[1] - e64[1]),
+        "mixed_error": {"vs": "GPU FP64 pass of the same step (full pass)",
+                        "dE_J": abs(emx[0] - e64[0]), "dE_K": abs(emx[1] - e64[1]),
                         "max_abs_dJ": float(np.max(np.abs(Jmx - J64))),
                         "max_abs_dK": float(np.max(np.abs(Kmx - K64)))},
+        "oracle_subset": subset,
         "speedup_mixed_vs_fp64": vmx / v64,
         "roofline": dom_ser,
         "roofline_concurrent": dom,
@@ -434,9 +551,10 @@ def run_gpu(args):
                                          "measured live; blended by the pass's FP64/FP32 work"
                                          % (peaks["fp64"], peaks["fp32"]),
                           "flops_fp64": fl64, "flops_fp32": fl32},
-        "e2e": {"value": ve2e, "unit": "ERI/s", "h2d_bytes_per_step": nbf * nbf * 8,
-                "d2h_bytes_per_step": 2 * nbf * nbf * 8},
-        "gpu_launches": int(stmx.launches) * args.steps + int(st64.launches) * args.steps,
+        "e2e": {"value": ve2e, "unit": "ERI/s", "steps": args.e2e_steps,
+                "h2d_bytes_per_step": nbf * nbf * 8, "d2h_bytes_per_step": 2 * nbf * nbf * 8},
+        "gpu_launches": int(stmx.launches) * args.steps + int(st64.launches) * args.fp64_steps
+        + int(st_e.launches) * args.e2e_steps,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
@@ -635,9 +753,15 @@ def run_rows(args):
             roof["note"] = ("dominant class launch of the last pass (concurrent branches: its "
                             "time includes sharing the GPU); FLOPs counted as for the Coulomb "
                             "operator (the attenuation's second Boys evaluation not included)")
-        Kq = ctx.schwarz()
         oracle.set_operator(oracle.OP_ERFC_COULOMB if name == "erfc" else oracle.OP_COULOMB, 0.4)
-        v, nsamp, tsamp, npair = cpu_baseline(bs, D, Kq, thresh, 8.0)
+        ob = oracle.OracleBasis.from_basis(bs)
+        Kq = oracle.schwarz(ob, cpu_threads())
+        acc = oracle.JKAccumulator(ob.nbf, cpu_threads())
+        pairs = sample_pairs(ob, Kq, thresh, CPU_SAMPLE_PAIRS, SEED + 7)
+        t0 = time.perf_counter()
+        _, nsamp = acc.add_pairs(ob, D, Kq, thresh, pairs)
+        v = nsamp / (time.perf_counter() - t0)
+        acc.close()
         res[name] = {"pass_ms": statistics.median(ms), "integrals": int(st.integrals),
                      "eri_per_s": st.integrals / (statistics.median(ms) * 1e-3),
                      "roofline_pass": {"bound": "fp64-pipe", "unit": "TFLOP/s",
@@ -662,11 +786,16 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="timed passes of the FP64 comparison (default 2)")
+    ap.add_argument("--fp64-warmup", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3,
+                    help="timed host-buffer passes of the e2e figure (default 3)")
     ap.add_argument("--impl", default="lgx", choices=["lgx", "reference"])
-    ap.add_argument("--workload", default="h2o32_cc-pvdz", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--ref-budget", type=float, default=60.0)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-check", action="store_true",
+                    help="skip the pair-subset comparison with the oracle")
     ap.add_argument("--primitive-api", action="store_true",
                     help="time the generated-library entry (libint2_build_eri*) instead")
     ap.add_argument("--rows", action="store_true",

@@ -91,6 +91,31 @@ lgx_status lgx_destroy(lgx_context* ctx);
  * quartet bins. */
 lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega);
 
+/* The Boys function F_m(T) = int_0^1 u^{2m} exp(-T u^2) du, m = 0..mmax, of
+ * n arguments T[i] >= 0 (HOST arrays; F is n x (mmax+1), row-major),
+ * evaluated on the GPU by exactly the device function a class kernel uses:
+ * variant 0 the program kernels' FP64 evaluator (mmax <= 16), 1 the
+ * register kernels' FP64 evaluator (mmax <= 6), 2 and 3 their FP32
+ * counterparts (results widened to double).  The batch counterpart of
+ * libint's FmEval_Taylor / FmEval_Chebyshev7 eval(F, T, mmax)
+ * (include/libint2/boys.h:345-454,679-821), so the evaluators can be
+ * checked against libint's reference values on their own. */
+lgx_status lgx_boys(lgx_context* ctx, int variant, const double* T, int64_t n, int mmax,
+                    double* F);
+
+/* Device-side watchdog of the program kernels' work loops.  Each warp of a
+ * program-kernel launch takes chunks of quartets from a device counter and
+ * raises the context's error flag (the call then returns LGX_ERR_WATCHDOG)
+ * once it would take more than a bound of chunks; by default (max_chunks
+ * < 0) the bound is the launch's whole work plus slack, which a valid launch
+ * never reaches.  max_chunks >= 0 replaces that bound on every later launch
+ * of the context (0: a warp may take no chunk, so any program-kernel launch
+ * with work trips it), so that a test can make the watchdog fire without a
+ * fault or a hang: the loop ends, the flag is read and cleared, and the
+ * context stays usable.  The counterpart of libint's assert-on-misuse
+ * (engine.impl.h:173-174), which aborts instead. */
+lgx_status lgx_set_watchdog(lgx_context* ctx, int64_t max_chunks);
+
 /* Message of the last failed call on this context (never NULL). */
 const char* lgx_last_error(const lgx_context* ctx);
 /* Library version string. */
@@ -172,6 +197,18 @@ lgx_status lgx_set_basis(lgx_context* ctx, int nshell, const int32_t* l,
                          const int32_t* pure, const int32_t* nprim,
                          const int32_t* atom, const double* origins,
                          const double* alpha, const double* coeff);
+/* Restricts every later J/K and gradient pass (lgx_jk*, lgx_jk_grad) to the
+ * unique quartets (s1 s2|s3 s4) whose bra and ket shell pairs are both in
+ * `pairs` (2*n shell indices, either order within a pair), still screened
+ * by K12*K34 >= schwarz_thresh; n = 0 lifts the restriction, as does
+ * lgx_set_basis.  The quartet set is the same whichever way a caller
+ * enumerates bra and ket, so a CPU J/K over the same pairs (the reference's
+ * compute_2body_fock loop, hartree-fock++.cc:1617-1700, with both pairs
+ * drawn from the list) gives the same J and K: this is how the J/K kernels
+ * are checked against a CPU implementation on bases far too large for a
+ * CPU pass.  No counterpart in the reference's Engine API. */
+lgx_status lgx_set_pair_subset(lgx_context* ctx, const int32_t* pairs, int64_t n);
+
 /* Number of basis functions of the current basis. */
 lgx_status lgx_basis_nbf(lgx_context* ctx, int* nbf);
 

@@ -312,6 +312,22 @@ class Context:
         self._check(self._lib.lgx_set_operator(self._h, _OP_CODE[Operator(oper)], float(omega)),
                     "lgx_set_operator")
 
+    def boys(self, T, mmax: int, variant: int = 0):
+        """F_0..F_mmax(T) for an array of T from the device evaluator
+        `variant` (lgx_boys: 0/1 FP64 program/register kernel, 2/3 FP32)."""
+        T = np.ascontiguousarray(T, np.float64).reshape(-1)
+        F = np.zeros((len(T), int(mmax) + 1))
+        self._check(self._lib.lgx_boys(self._h, int(variant), _lgx.ptr(T), len(T), int(mmax),
+                                       _lgx.ptr(F)), "lgx_boys")
+        return F
+
+    def set_watchdog(self, max_chunks: int = -1):
+        """Bound on the work chunks a program-kernel warp may take per launch
+        before the call fails with LGX_ERR_WATCHDOG (lgx_set_watchdog);
+        a negative value restores the default bound derived from each
+        launch's work, 0 trips on any program-kernel launch with work."""
+        self._check(self._lib.lgx_set_watchdog(self._h, int(max_chunks)), "lgx_set_watchdog")
+
     # ------------------------------------------------------------ engine
     def compute_shellset(self, shells, deriv=0, precision=np.finfo(float).eps,
                          screening=ScreeningMethod.Original):
@@ -364,6 +380,15 @@ class Context:
                                      _lgx.ptr(alpha), _lgx.ptr(coeff))
         self._check(st, "lgx_set_basis")
         self.basis = basis
+
+    def set_pair_subset(self, pairs=None):
+        """Restrict later J/K and gradient passes to quartets whose bra and ket
+        shell pairs both come from `pairs` (n x 2 shell indices);
+        None or an empty list lifts the restriction (lgx_set_pair_subset)."""
+        p = np.ascontiguousarray(np.zeros((0, 2)) if pairs is None else pairs,
+                                 np.int32).reshape(-1, 2)
+        self._check(self._lib.lgx_set_pair_subset(self._h, _lgx.ptr(p, ctypes.c_int32),
+                                                  len(p)), "lgx_set_pair_subset")
 
     def schwarz(self):
         n = len(self.basis)

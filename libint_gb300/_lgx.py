@@ -88,6 +88,9 @@ SIGNATURES = {
     "lgx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "lgx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "lgx_set_operator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
+    "lgx_set_watchdog": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    "lgx_boys": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int64, ctypes.c_int,
+                                _dp]),
     "lgx_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "lgx_version": (ctypes.c_char_p, []),
     "lgx_compute_shellset": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(LgxShell),
@@ -105,6 +108,7 @@ SIGNATURES = {
     "lgx_set_basis": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip, _ip,
                                      _dp, _dp, _dp]),
     "lgx_basis_nbf": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "lgx_set_pair_subset": (ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.c_int64]),
     "lgx_schwarz": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "lgx_compute_batch": (ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.c_int64, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_double, _i64p, _dp,

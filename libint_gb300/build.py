@@ -18,7 +18,7 @@ BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liblgx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu"]
+CUDA_SOURCES = ["lgx_kernels.cu", "lgx_api.cu", "lgx_boys.cu"]
 CXX_SOURCES = ["lgx_program.cpp", "lgx_host.cpp", "lgx_libint_c.cpp"]
 
 

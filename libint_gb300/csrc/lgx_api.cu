@@ -30,6 +30,9 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
 size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
+cudaError_t launch_boys_eval(const double* tab, const double* tay, const float* tab32,
+                             const double* inv_odd, int variant, const double* T, long long n,
+                             int mmax, double* F, cudaStream_t st);
 cudaError_t launch_prim_set(const PrimSetArgs& a, size_t smem, cudaStream_t st);
 cudaError_t launch_eri_block_store(const EriArgs& a, int grid, size_t smem, cudaStream_t st);
 cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int ld, const EriArgs& a,
@@ -122,6 +125,7 @@ struct BinCache {
   bool valid = false;
   double thresh = -1, mixed = -1;
   int mode = -1;
+  unsigned long long subset_version = ~0ull;  // pair subset the bins were built for
   DBuf class_lists;                 // pair ids of every pair class, sorted
   std::vector<long long> class_off; // offsets of each class in class_lists
   // FP32 records per list position (PrimPairJK32 layout) and their source
@@ -227,6 +231,13 @@ struct lgx_context {
   std::vector<cudaEvent_t> lev;
   std::vector<lgx_launch_stats> last_launches;
   bool noalloc = false;  // set during lgx_jk_device_noalloc: no device allocation
+  // work chunks a program-kernel warp may take per launch before it raises
+  // the watchdog flag (< 0: derived from the launch's work; lgx_set_watchdog)
+  long long watchdog_chunks = -1;
+  // shell pairs a J/K pass is restricted to (lgx_set_pair_subset; one flag
+  // per pair index, empty: every pair) and a version bumped on each change
+  std::vector<unsigned char> pair_subset;
+  unsigned long long subset_version = 0;
   // two-body operator of every pass (lgx_set_operator): LGX_OP_* and omega
   int op = LGX_OP_COULOMB;
   double omega = 0.0;
@@ -235,6 +246,7 @@ struct lgx_context {
   DBuf items, out, isnull;
   DBuf Jacc, Kacc, Dd, Jd, Kd, gJ, gK;
   DBuf prim_rows, prim_slots;  // lgx_compute_primitive_set
+  DBuf boysT, boysF;           // lgx_boys
   DBuf xcounters;              // explicit lists: one work counter per class launch
   BinCache bins;
   std::mutex mu;
@@ -763,7 +775,9 @@ lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bo
   cudaStream_t lst = ctx->launch_stream ? ctx->launch_stream : ctx->stream;
   const long long nwarps = (long long)L.grid * L.wpb;
   a.chunk = int(std::max<long long>(1, std::min<long long>(32, nwork / (nwarps * 8))));
-  a.max_chunks = nwork / a.chunk + 2;
+  // every warp takes at most all chunks of the launch (plus slack); a test
+  // hook (lgx_set_watchdog) can lower the bound to make the watchdog fire
+  a.max_chunks = ctx->watchdog_chunks >= 0 ? ctx->watchdog_chunks : nwork / a.chunk + 2;
   if (own_counter) CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), lst));
   if (gen)
     CK(post_launch(fp32, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, L.grid, L.block, L.smem,
@@ -1052,7 +1066,9 @@ int pair_class(int lhi, int llo) { return lhi * (lhi + 1) / 2 + llo; }  // 10 cl
 
 lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, double mixed) {
   BinCache& C = ctx->bins;
-  if (C.valid && C.thresh == thresh && C.mode == mode && C.mixed == mixed) return LGX_OK;
+  if (C.valid && C.thresh == thresh && C.mode == mode && C.mixed == mixed &&
+      C.subset_version == ctx->subset_version)
+    return LGX_OK;
   C.valid = false;
   C.bins.clear();
   const long long npairs = (long long)B.hpairs.size();
@@ -1062,6 +1078,7 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
   std::vector<std::vector<int>> lists(10);
   for (long long p = 0; p < npairs; ++p) {
     if (B.Kpair[p] * Kmax < thresh) continue;
+    if (!ctx->pair_subset.empty() && !ctx->pair_subset[p]) continue;
     const int s1 = B.hpairs[p].s1, s2 = B.hpairs[p].s2;
     const int lhi = std::max(B.l[s1], B.l[s2]), llo = std::min(B.l[s1], B.l[s2]);
     lists[pair_class(lhi, llo)].push_back(int(p));
@@ -1217,6 +1234,7 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
   C.thresh = thresh;
   C.mode = mode;
   C.mixed = mixed;
+  C.subset_version = ctx->subset_version;
   return LGX_OK;
 }
 
@@ -2188,8 +2206,32 @@ lgx_status lgx_set_basis(lgx_context* ctx, int nshell, const int32_t* l, const i
   CK(cudaSetDevice(ctx->device));
   ctx->bins.valid = false;
   ctx->tuned.clear();
+  ctx->pair_subset.clear();  // pair indices refer to the previous basis
+  ++ctx->subset_version;
   ++ctx->version;
   return upload_basis(ctx, ctx->basis, nshell, l, pure, nprim, atom, origins, alpha, coeff);
+}
+
+lgx_status lgx_set_pair_subset(lgx_context* ctx, const int32_t* pairs, int64_t n) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const int ns = ctx->basis.nshell;
+  if (ns == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
+  if (n < 0 || (n > 0 && !pairs)) return fail(ctx, LGX_ERR_INVALID_ARG, "bad pair list");
+  std::vector<unsigned char> mask;
+  if (n > 0) {
+    mask.assign(size_t(ns) * (ns + 1) / 2, 0);
+    for (int64_t i = 0; i < n; ++i) {
+      const int a = pairs[2 * i], b = pairs[2 * i + 1];
+      if (a < 0 || b < 0 || a >= ns || b >= ns)
+        return fail(ctx, LGX_ERR_INVALID_ARG, "shell index out of range in the pair list");
+      mask[pidx(std::max(a, b), std::min(a, b))] = 1;
+    }
+  }
+  ctx->pair_subset.swap(mask);
+  ++ctx->subset_version;
+  ++ctx->version;
+  return LGX_OK;
 }
 
 lgx_status lgx_basis_nbf(lgx_context* ctx, int* nbf) {
@@ -2291,10 +2333,12 @@ lgx_status lgx_compute_batch_device(lgx_context* ctx, const int32_t* quartets, i
                        d_is_null, true);
 }
 
-lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double* dK,
-                         double thresh, int mode, double mixed, lgx_jk_stats* stats) {
-  if (!ctx) return LGX_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(ctx->mu);
+}  // extern "C"
+
+namespace {
+// Body of lgx_jk_device; the caller holds ctx->mu.
+lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, double* dK,
+                            double thresh, int mode, double mixed, lgx_jk_stats* stats) {
   if (!dD || !dJ || !dK) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
   if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
   if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
@@ -2395,6 +2439,16 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double*
   }
   return LGX_OK;
 }
+}  // namespace
+
+extern "C" {
+
+lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ, double* dK,
+                         double thresh, int mode, double mixed, lgx_jk_stats* stats) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return jk_device_locked(ctx, dD, dJ, dK, thresh, mode, mixed, stats);
+}
 
 }  // extern "C"
 
@@ -2427,7 +2481,10 @@ lgx_status noalloc_scratch(lgx_context* ctx, unsigned char** out) {
 struct NoAllocGuard {
   lgx_context* c;
   explicit NoAllocGuard(lgx_context* ctx) : c(ctx) { c->noalloc = true; }
-  ~NoAllocGuard() { c->noalloc = false; }
+  ~NoAllocGuard() {
+    c->noalloc = false;
+    c->scratch = nullptr;
+  }
 };
 }  // namespace
 
@@ -2449,7 +2506,8 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   const BinCache& C = ctx->bins;
   const double mixed_key = mode == LGX_MIXED ? mixed : 0.0;
   if (!B.schwarz_ok || !B.pairs_ok || B.pairs_lnprec != std::log(eps) || B.pairs_method != 0 ||
-      !C.valid || C.thresh != thresh || C.mode != mode || C.mixed != mixed_key)
+      !C.valid || C.thresh != thresh || C.mode != mode || C.mixed != mixed_key ||
+      C.subset_version != ctx->subset_version)
     return fail(ctx, LGX_ERR_INVALID_ARG,
                 "lgx_jk_device_noalloc: basis state not prepared for these settings; call "
                 "lgx_jk_device (or lgx_jk) once with the same threshold and mode first");
@@ -2464,6 +2522,14 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   double* Jacc = reinterpret_cast<double*>(scratch);
   double* Kacc = Jacc + kNoAllocN;
   float* Df = reinterpret_cast<float*>(Kacc + kNoAllocN);
+  // The prepared pass ran its program-kernel launches on parallel branches,
+  // each growing its own slot scratch; this pass runs every launch on
+  // ctx->stream one after another, so the largest of those buffers serves
+  // all of them (plan_launch clamps each grid to it).
+  DBuf* slot_scratch = &ctx->gscratch;
+  for (DBuf& b : ctx->gscratch_br)
+    if (b.n > slot_scratch->n) slot_scratch = &b;
+  ctx->scratch = slot_scratch;
   CK(cudaEventRecord(ctx->ev2, ctx->stream));
   CK(cudaMemsetAsync(Jacc, 0, nn * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(Kacc, 0, nn * sizeof(double), ctx->stream));
@@ -2494,21 +2560,20 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
 lgx_status lgx_jk(lgx_context* ctx, const double* D, double* J, double* K, double thresh,
                   int mode, double mixed, lgx_jk_stats* stats) {
   if (!ctx) return LGX_ERR_INVALID_ARG;
+  // one lock over the copy in, the pass and the copy out, so that two
+  // threads sharing a context cannot interleave their D, J and K
+  std::lock_guard<std::mutex> lk(ctx->mu);
   if (!D || !J || !K) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
   if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
   const size_t nn = size_t(ctx->basis.nbf) * ctx->basis.nbf;
-  {
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    CK(cudaSetDevice(ctx->device));
-    CK(ctx->Dd.ensure(nn * sizeof(double)));
-    CK(ctx->Jd.ensure(nn * sizeof(double)));
-    CK(ctx->Kd.ensure(nn * sizeof(double)));
-    CK(cudaMemcpyAsync(ctx->Dd.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  }
-  lgx_status s = lgx_jk_device(ctx, ctx->Dd.as<double>(), ctx->Jd.as<double>(),
-                               ctx->Kd.as<double>(), thresh, mode, mixed, stats);
+  CK(cudaSetDevice(ctx->device));
+  CK(ctx->Dd.ensure(nn * sizeof(double)));
+  CK(ctx->Jd.ensure(nn * sizeof(double)));
+  CK(ctx->Kd.ensure(nn * sizeof(double)));
+  CK(cudaMemcpyAsync(ctx->Dd.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  lgx_status s = jk_device_locked(ctx, ctx->Dd.as<double>(), ctx->Jd.as<double>(),
+                                  ctx->Kd.as<double>(), thresh, mode, mixed, stats);
   if (s != LGX_OK) return s;
-  std::lock_guard<std::mutex> lk(ctx->mu);
   CK(cudaMemcpyAsync(J, ctx->Jd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(K, ctx->Kd.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -2530,6 +2595,43 @@ lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega) {
   ctx->basis.schwarz_ok = false;
   ctx->bins.valid = false;
   ++ctx->version;
+  return LGX_OK;
+}
+
+lgx_status lgx_boys(lgx_context* ctx, int variant, const double* T, int64_t n, int mmax,
+                    double* F) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (variant < 0 || variant > 3) return fail(ctx, LGX_ERR_INVALID_ARG, "bad Boys variant");
+  const int mmax_cap = (variant == 1 || variant == 3) ? 6 : kBoysMaxM;
+  if (mmax < 0 || mmax > mmax_cap)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "mmax out of range for this evaluator");
+  if (n < 0 || (n > 0 && (!T || !F))) return fail(ctx, LGX_ERR_INVALID_ARG, "bad arrays");
+  if (n == 0) return LGX_OK;
+  for (int64_t i = 0; i < n; ++i)  // the table lookup needs 0 <= T (NaN rejected too)
+    if (!(T[i] >= 0.0) || !std::isfinite(T[i]))
+      return fail(ctx, LGX_ERR_INVALID_ARG, "Boys argument T must be finite and >= 0");
+  CK(cudaSetDevice(ctx->device));
+  const size_t nf = size_t(n) * (mmax + 1);
+  CK(ctx->boysT.ensure(size_t(n) * sizeof(double)));
+  CK(ctx->boysF.ensure(nf * sizeof(double)));
+  CK(cudaMemcpyAsync(ctx->boysT.p, T, size_t(n) * sizeof(double), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(launch_boys_eval(ctx->boys.as<double>(), ctx->boys_tay.as<double>(), ctx->boys32.as<float>(),
+                      ctx->inv_odd.as<double>(), variant, ctx->boysT.as<double>(), n, mmax,
+                      ctx->boysF.as<double>(), ctx->stream));
+  CK(cudaMemcpyAsync(F, ctx->boysF.p, nf * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_set_watchdog(lgx_context* ctx, int64_t max_chunks) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (max_chunks < 0) max_chunks = -1;
+  if (max_chunks == ctx->watchdog_chunks) return LGX_OK;
+  ctx->watchdog_chunks = max_chunks;
+  ++ctx->version;  // the bound is a launch argument of the captured pass
   return LGX_OK;
 }
 

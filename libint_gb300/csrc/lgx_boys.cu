@@ -1,0 +1,65 @@
+// The device Boys evaluators as a batch call (lgx_boys): each thread
+// evaluates F_0..F_mmax(T) of one argument with exactly the function a class
+// kernel uses, so that the evaluators can be checked on their own.
+#include "lgx_boys.cuh"
+#include "lgx_warp.cuh"
+
+namespace lgx {
+namespace {
+
+template <int MMAX>
+__device__ void rk_boys_to(int variant, const double* tay, const float* tab32, double T,
+                           double* out) {
+  if (variant == 1) {
+    rk_boys<MMAX>(tay, T, 1.0, out);
+  } else {
+    float f[MMAX + 1];
+    rk_boys<MMAX>(tab32, float(T), 1.0f, f);
+#pragma unroll
+    for (int m = 0; m <= MMAX; ++m) out[m] = double(f[m]);
+  }
+}
+
+__global__ void boys_eval_kernel(const double* tab, const double* tay, const float* tab32,
+                                 const double* inv_odd, int variant, const double* Targ,
+                                 long long n, int mmax, double* F) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double T = Targ[i];
+  double out[kBoysMaxM + 1];
+  if (variant == 0) {
+    boys_to_stage(tab, inv_odd, T, mmax, 1.0, out);
+  } else if (variant == 2) {
+    float f[kBoysMaxM + 1];
+    boys_to_stage(tab32, float(T), mmax, 1.0f, f);
+    for (int m = 0; m <= mmax; ++m) out[m] = double(f[m]);
+  } else {
+    switch (mmax) {
+      case 0: rk_boys_to<0>(variant, tay, tab32, T, out); break;
+      case 1: rk_boys_to<1>(variant, tay, tab32, T, out); break;
+      case 2: rk_boys_to<2>(variant, tay, tab32, T, out); break;
+      case 3: rk_boys_to<3>(variant, tay, tab32, T, out); break;
+      case 4: rk_boys_to<4>(variant, tay, tab32, T, out); break;
+      case 5: rk_boys_to<5>(variant, tay, tab32, T, out); break;
+      default: rk_boys_to<6>(variant, tay, tab32, T, out); break;
+    }
+  }
+  for (int m = 0; m <= mmax; ++m) F[i * (mmax + 1) + m] = out[m];
+}
+
+}  // namespace
+
+// variant: 0 program kernel FP64, 1 register kernel FP64 (mmax <= 6),
+// 2 program kernel FP32, 3 register kernel FP32 (mmax <= 6); the caller
+// checks the ranges.
+cudaError_t launch_boys_eval(const double* tab, const double* tay, const float* tab32,
+                             const double* inv_odd, int variant, const double* T, long long n,
+                             int mmax, double* F, cudaStream_t st) {
+  const int block = 128;
+  const long long grid = (n + block - 1) / block;
+  boys_eval_kernel<<<(unsigned)grid, block, 0, st>>>(tab, tay, tab32, inv_odd, variant, T, n,
+                                                     mmax, F);
+  return cudaGetLastError();
+}
+
+}  // namespace lgx

@@ -13,113 +13,13 @@
 // so that it keeps FP32 relative precision.
 #pragma once
 #include "gen/rk_classes.cuh"
+#include "lgx_boys.cuh"
 
 namespace lgx {
 
 // T -> double for the FP64 accumulators (integer-only for float)
 __device__ __forceinline__ double rk_f64(double x) { return x; }
 __device__ __forceinline__ double rk_f64(float x) { return f2d_int(x); }
-
-// Boys F_0..F_MMAX(T) times the primitive prefactor pfac.
-//  T <= kBoysTmax: 7-term Taylor expansion about the nearest grid point
-//   T_k = k/32 of the pre-divided table; every m directly when MMAX <= 2,
-//   else the top m plus the downward recursion, with e^{-T} formed as the
-//   tabulated e^{-T_k} (slot 7 of the m = 0 row) times the 7-term Maclaurin
-//   series of e^{T_k - T} (|T_k - T| <= 1/64: relative error < 5e-17).
-//  T > kBoysTmax (= 50): F_0 = sqrt(pi/T)/2 and the upward recursion
-//   F_{m+1} = (2m+1)/(2T) F_m with the e^{-T} terms dropped; the relative
-//   error of that, the regularised upper incomplete gamma Q(m+1/2, T), is
-//   below 2e-16 for m <= 5 and 1.7e-15 for m = 6 at T = 50.
-template <int MMAX>
-__device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T, double pfac,
-                                        double* F) {
-  static_assert(MMAX <= 6, "asymptotic branch without e^{-T} is exact to 2e-15 only for m <= 6");
-  if (T > kBoysTmax) {
-    const double rs = rsqrt(T);
-    const double oo2T = 0.5 * (rs * rs);
-    double f = (0.88622692545275801365 * pfac) * rs;
-    F[0] = f;
-#pragma unroll
-    for (int m = 0; m < MMAX; ++m) {
-      f *= (2 * m + 1) * oo2T;
-      F[m + 1] = f;
-    }
-    return;
-  }
-  // nearest grid point: adding 1.5*2^52 rounds T*32 to an integer held in
-  // the low mantissa bits (read back with an integer move)
-  const double t32 = fma(T, kBoysInvDT, 6755399441055744.0);
-  const int k = __double2loint(t32);
-  const double md = fma(t32 - 6755399441055744.0, kBoysDT, -T);  // = -(T - T_k)
-  const double* row = tay + (k * (kBoysMaxM + 1)) * kBoysTaylorStride;
-  if (MMAX <= 2) {
-#pragma unroll
-    for (int m = 0; m <= MMAX; ++m) {
-      const double* c = row + m * kBoysTaylorStride;
-      double s = __ldg(c + 6);
-#pragma unroll
-      for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
-      F[m] = s * pfac;
-    }
-  } else {
-    const double* c = row + MMAX * kBoysTaylorStride;
-    double s = __ldg(c + 6);
-#pragma unroll
-    for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
-    s *= pfac;
-    F[MMAX] = s;
-    double e = 1.0 / 720.0;
-    e = fma(e, md, 1.0 / 120.0);
-    e = fma(e, md, 1.0 / 24.0);
-    e = fma(e, md, 1.0 / 6.0);
-    e = fma(e, md, 0.5);
-    e = fma(e, md, 1.0);
-    e = fma(e, md, 1.0);
-    const double eTp = (__ldg(row + 7) * pfac) * e;  // pfac e^{-T}
-    const double twoT = 2.0 * T;
-#pragma unroll
-    for (int m = MMAX - 1; m >= 0; --m) {
-      s = fma(twoT, s, eTp) * (1.0 / (2 * m + 1));
-      F[m] = s;
-    }
-  }
-}
-
-template <int MMAX>
-__device__ __forceinline__ void rk_boys(const float* __restrict__ tab, float T, float pfac,
-                                        float* F) {
-  if (T > float(kBoysTmax)) {
-    const float rs = rsqrtf(T);
-    const float oo2T = 0.5f * (rs * rs);
-    float f = (0.886226925f * pfac) * rs;
-    F[0] = f;
-#pragma unroll
-    for (int m = 0; m < MMAX; ++m) {
-      f *= (2 * m + 1) * oo2T;  // e^{-T} < 2e-22 is below FP32 resolution
-      F[m + 1] = f;
-    }
-    return;
-  }
-  const int k = __float2int_rn(T * float(kBoysInvDT));
-  const float d = T - k * float(kBoysDT);
-  const float* row = tab + k * kBoysCols;
-  const float c3 = -d * (1.0f / 3.0f), c2 = -d * 0.5f, c1 = -d;
-  float s = __ldg(row + MMAX + 3);
-  s = fmaf(s, c3, __ldg(row + MMAX + 2));
-  s = fmaf(s, c2, __ldg(row + MMAX + 1));
-  s = fmaf(s, c1, __ldg(row + MMAX));
-  s *= pfac;
-  F[MMAX] = s;
-  if (MMAX > 0) {
-    const float eTp = __expf(-T) * pfac;
-    const float twoT = 2.0f * T;
-#pragma unroll
-    for (int m = MMAX - 1; m >= 0; --m) {
-      s = fmaf(twoT, s, eTp) * (1.0f / (2 * m + 1));
-      F[m] = s;
-    }
-  }
-}
 
 // Attenuated operators (register kernels of the J/K passes): F holds
 // pfac F_m(T) on entry; with s = omega^2 / (omega^2 + rho) the core

@@ -44,7 +44,9 @@ def extract(src, dst):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LGX_REFERENCE_ROOT")
+    if not ref:
+        sys.exit("usage: extract_basis.py LIBINT_TREE  (or set LGX_REFERENCE_ROOT)")
     here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "basis")
     os.makedirs(here, exist_ok=True)
     for n in NAMES:

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <limits>
 #include <mutex>
+#include <random>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -941,40 +942,86 @@ void orc_schwarz(const orc_basis* bs, double* Kmat, int nthreads) {
   }
 }
 
-int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,
-                      const double* Ks, double thresh, const double* D,
-                      double* J, double* K, int nthreads, int64_t pb_begin,
-                      int64_t pb_end, int64_t* n_integrals) {
+}  // extern "C"
+
+// Per-thread J/K accumulators, as compute_2body_fock keeps one G per thread
+// and sums them at the end (tests/hartree-fock/hartree-fock++.cc:1601-1607,
+// 1766).  They persist across calls, so that a timed sample of bra pairs
+// pays the integral evaluation and digestion only; zeroing and reducing the
+// per-thread matrices happens once per pass, as in the reference.
+struct orc_jk_acc {
+  int nbf = 0, nt = 1;
+  std::vector<std::vector<double>> J, K;
+};
+
+namespace {
+// Bra shell pair index pb = s1 (s1 + 1) / 2 + s2 (s2 <= s1) -> (s1, s2).
+void bra_pair_shells(int64_t pb, int* s1o, int* s2o) {
+  int s1 = int((std::sqrt(8.0 * double(pb) + 1) - 1) / 2);
+  while (int64_t(s1) * (s1 + 1) / 2 > pb) --s1;
+  while (int64_t(s1 + 1) * (s1 + 2) / 2 <= pb) ++s1;
+  *s1o = s1;
+  *s2o = int(pb - int64_t(s1) * (s1 + 1) / 2);
+}
+}  // namespace
+
+extern "C" {
+
+orc_jk_acc* orc_jk_acc_create(int nbf, int nthreads) {
+  if (nbf <= 0) return nullptr;
+  auto* a = new orc_jk_acc;
+  a->nbf = nbf;
+  a->nt = nthreads_or_default(nthreads);
+  a->J.resize(a->nt);
+  a->K.resize(a->nt);
+#pragma omp parallel for num_threads(a->nt) schedule(static, 1)
+  for (int t = 0; t < a->nt; ++t) {  // first touch by the thread that uses it
+    a->J[t].assign(size_t(nbf) * nbf, 0.0);
+    a->K[t].assign(size_t(nbf) * nbf, 0.0);
+  }
+  return a;
+}
+
+void orc_jk_acc_destroy(orc_jk_acc* a) { delete a; }
+
+// J/K contributions of the listed bra shell pairs (indices of the canonical
+// enumeration, s1 >= s2): every unique ket pair (s3, s4) <= (s1, s2) with
+// K12 K34 >= thresh, digested with the 8-fold degeneracy factors of
+// hartree-fock++.cc:1709-1743, OpenMP over the list (dynamic schedule, as
+// the reference's task loop hands shell pairs to threads).  ket_mask (one
+// flag per canonical pair index, or NULL for every pair) restricts the
+// kets: with the bra list and the mask holding the same pairs, each
+// unordered quartet of that pair subset is digested exactly once.
+int64_t orc_jk_acc_pairs(orc_jk_acc* acc, const orc_basis* bs, const int* bf_off,
+                         const double* Ks, double thresh, const double* D,
+                         const int64_t* pairs, int64_t npairs, const unsigned char* ket_mask,
+                         int64_t* n_integrals) {
+  if (!acc || !bs || npairs < 0) return -1;
   const int ns = bs->nshell;
-  const int nt = nthreads_or_default(nthreads);
-  std::vector<std::vector<double>> Jt(nt), Kt(nt);
+  const int nbf = acc->nbf;
   int64_t nq = 0, nint = 0;
   const double eps = std::numeric_limits<double>::epsilon();
-#pragma omp parallel num_threads(nt) reduction(+ : nq, nint)
+#pragma omp parallel num_threads(acc->nt) reduction(+ : nq, nint)
   {
 #ifdef _OPENMP
     const int tid = omp_get_thread_num();
 #else
     const int tid = 0;
 #endif
-    Jt[tid].assign(size_t(nbf) * nbf, 0.0);
-    Kt[tid].assign(size_t(nbf) * nbf, 0.0);
-    double* Jl = Jt[tid].data();
-    double* Kl = Kt[tid].data();
+    double* Jl = acc->J[tid].data();
+    double* Kl = acc->K[tid].data();
     Work w;
     std::vector<double> buf;
 #pragma omp for schedule(dynamic, 1)
-    for (int64_t pb = pb_begin; pb < pb_end; ++pb) {
-      // bra pair index pb = s1*(s1+1)/2 + s2, s2 <= s1
-      int s1 = int((std::sqrt(8.0 * pb + 1) - 1) / 2);
-      while (int64_t(s1) * (s1 + 1) / 2 > pb) --s1;
-      while (int64_t(s1 + 1) * (s1 + 2) / 2 <= pb) ++s1;
-      const int s2 = int(pb - int64_t(s1) * (s1 + 1) / 2);
+    for (int64_t ip = 0; ip < npairs; ++ip) {
+      int s1, s2;
+      bra_pair_shells(pairs[ip], &s1, &s2);
       const double K12 = Ks[size_t(s1) * ns + s2];
       for (int s3 = 0; s3 <= s1; ++s3) {
         const int s4max = (s1 == s3) ? s2 : s3;
         for (int s4 = 0; s4 <= s4max; ++s4) {
           if (K12 * Ks[size_t(s3) * ns + s4] < thresh) continue;
+          if (ket_mask && !ket_mask[int64_t(s3) * (s3 + 1) / 2 + s4]) continue;
           const int n1 = nfunc(bs, s1), n2 = nfunc(bs, s2), n3 = nfunc(bs, s3),
                     n4 = nfunc(bs, s4);
           buf.resize(size_t(n1) * n2 * n3 * n4);
@@ -1003,16 +1050,136 @@ int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,
       }
     }
   }
-  // J = 1/2 sym(Jacc), K = 1/4 sym(Kacc) (libint's G = 2J - K form,
-  // hartree-fock++.cc:1721-1743,1766)
-  for (int t = 0; t < nt; ++t)
-    for (int a = 0; a < nbf; ++a)
-      for (int b = 0; b < nbf; ++b) {
-        J[size_t(a) * nbf + b] += 0.25 * (Jt[t][size_t(a) * nbf + b] + Jt[t][size_t(b) * nbf + a]);
-        K[size_t(a) * nbf + b] += 0.125 * (Kt[t][size_t(a) * nbf + b] + Kt[t][size_t(b) * nbf + a]);
-      }
   if (n_integrals) *n_integrals = nint;
   return nq;
+}
+
+// Adds the symmetrised sums of the per-thread accumulators to J and K:
+// J = 1/2 sym(Jacc), K = 1/4 sym(Kacc) (libint's G = 2J - K form,
+// hartree-fock++.cc:1721-1743,1766).
+void orc_jk_acc_reduce(const orc_jk_acc* acc, double* J, double* K) {
+  const int nbf = acc->nbf;
+#pragma omp parallel for num_threads(acc->nt) schedule(static)
+  for (int a = 0; a < nbf; ++a)
+    for (int t = 0; t < acc->nt; ++t)
+      for (int b = 0; b < nbf; ++b) {
+        J[size_t(a) * nbf + b] +=
+            0.25 * (acc->J[t][size_t(a) * nbf + b] + acc->J[t][size_t(b) * nbf + a]);
+        K[size_t(a) * nbf + b] +=
+            0.125 * (acc->K[t][size_t(a) * nbf + b] + acc->K[t][size_t(b) * nbf + a]);
+      }
+}
+
+int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,
+                      const double* Ks, double thresh, const double* D,
+                      double* J, double* K, int nthreads, int64_t pb_begin,
+                      int64_t pb_end, int64_t* n_integrals) {
+  std::vector<int64_t> pairs;
+  for (int64_t pb = pb_begin; pb < pb_end; ++pb) pairs.push_back(pb);
+  orc_jk_acc* acc = orc_jk_acc_create(nbf, nthreads);
+  if (!acc) return -1;
+  const int64_t nq = orc_jk_acc_pairs(acc, bs, bf_off, Ks, thresh, D, pairs.data(),
+                                      int64_t(pairs.size()), nullptr, n_integrals);
+  orc_jk_acc_reduce(acc, J, K);
+  orc_jk_acc_destroy(acc);
+  return nq;
+}
+
+// Unique shell quartets (s1 s2|s3 s4) of the canonical enumeration (bra pair
+// index >= ket pair index) with K12 K34 >= thresh, and their integrals
+// (n1 n2 n3 n4 summed): a sweep over the bra pairs in index order with a
+// Fenwick tree of the ket pairs inserted so far, keyed by their rank in
+// descending K, so each bra pair's kets are one prefix query.
+void orc_count_screened(const orc_basis* bs, const double* Ks, double thresh,
+                        int64_t* n_quartets, int64_t* n_integrals) {
+  const int ns = bs->nshell;
+  const int64_t np = int64_t(ns) * (ns + 1) / 2;
+  std::vector<double> kp(np);
+  std::vector<int64_t> nf(np);
+  for (int s1 = 0, p = 0; s1 < ns; ++s1)
+    for (int s2 = 0; s2 <= s1; ++s2, ++p) {
+      kp[p] = Ks[size_t(s1) * ns + s2];
+      nf[p] = int64_t(nfunc(bs, s1)) * nfunc(bs, s2);
+    }
+  std::vector<int64_t> order(np);
+  for (int64_t p = 0; p < np; ++p) order[p] = p;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return kp[a] > kp[b]; });
+  std::vector<int64_t> rank(np);
+  std::vector<double> ksorted(np);
+  for (int64_t r = 0; r < np; ++r) {
+    rank[order[r]] = r;
+    ksorted[r] = kp[order[r]];
+  }
+  std::vector<int64_t> cnt(np + 1, 0), wsum(np + 1, 0);  // Fenwick trees (1-based)
+  int64_t nq = 0, nint = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    for (int64_t i = rank[p] + 1; i <= np; i += i & -i) {
+      cnt[i] += 1;
+      wsum[i] += nf[p];
+    }
+    if (!(kp[p] > 0)) continue;
+    // ket pairs with K34 >= thresh / K12: the first L ranks
+    const double need = thresh / kp[p];
+    const int64_t L = int64_t(std::upper_bound(ksorted.begin(), ksorted.end(), need,
+                                               [](double v, double k) { return v > k; }) -
+                              ksorted.begin());
+    int64_t c = 0, w = 0;
+    for (int64_t i = L; i > 0; i -= i & -i) {
+      c += cnt[i];
+      w += wsum[i];
+    }
+    nq += c;
+    nint += w * nf[p];
+  }
+  *n_quartets = nq;
+  *n_integrals = nint;
+}
+
+// The synthetic water cluster of the benchmark configurations: nx ny nz
+// molecules, O on a grid of `spacing` angstrom jittered by
+// uniform(-jitter, jitter) per axis, H at 0.96 A and 104.5 deg, each
+// molecule in a uniformly random orientation (Shoemake's random unit
+// quaternion), all from one mt19937_64(seed) stream; atoms O, H, H per
+// molecule in bohr (CODATA 2018 0.529177210903 A/bohr,
+// include/libint2/atom.h:52-55).
+int orc_water_cluster(int nx, int ny, int nz, double spacing, double jitter, uint64_t seed,
+                      int* Z, double* xyz) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || !Z || !xyz) return -1;
+  std::mt19937_64 rng(seed);
+  auto uni = [&]() { return double(rng() >> 11) * (1.0 / 9007199254740992.0); };
+  const double bohr_per_ang = 1.0 / 0.529177210903;
+  const double pi = 3.14159265358979323846;
+  const double r = 0.96, half = 0.5 * 104.5 * pi / 180.0;
+  const double hpos[2][3] = {{r * std::sin(half), 0.0, r * std::cos(half)},
+                             {-r * std::sin(half), 0.0, r * std::cos(half)}};
+  int m = 0;
+  for (int ix = 0; ix < nx; ++ix)
+    for (int iy = 0; iy < ny; ++iy)
+      for (int iz = 0; iz < nz; ++iz, ++m) {
+        double O[3] = {ix * spacing, iy * spacing, iz * spacing};
+        for (double& o : O) o += (2 * uni() - 1) * jitter;
+        const double u1 = uni(), u2 = uni(), u3 = uni();
+        const double q[4] = {std::sqrt(1 - u1) * std::sin(2 * pi * u2),
+                             std::sqrt(1 - u1) * std::cos(2 * pi * u2),
+                             std::sqrt(u1) * std::sin(2 * pi * u3),
+                             std::sqrt(u1) * std::cos(2 * pi * u3)};  // x y z w
+        const double x = q[0], y = q[1], zq = q[2], w = q[3];
+        const double R[3][3] = {{1 - 2 * (y * y + zq * zq), 2 * (x * y - zq * w), 2 * (x * zq + y * w)},
+                                {2 * (x * y + zq * w), 1 - 2 * (x * x + zq * zq), 2 * (y * zq - x * w)},
+                                {2 * (x * zq - y * w), 2 * (y * zq + x * w), 1 - 2 * (x * x + y * y)}};
+        Z[3 * m] = 8;
+        Z[3 * m + 1] = 1;
+        Z[3 * m + 2] = 1;
+        for (int c = 0; c < 3; ++c) xyz[9 * m + c] = O[c] * bohr_per_ang;
+        for (int h = 0; h < 2; ++h)
+          for (int c = 0; c < 3; ++c) {
+            double v = O[c];
+            for (int k = 0; k < 3; ++k) v += R[c][k] * hpos[h][k];
+            xyz[9 * m + 3 * (h + 1) + c] = v * bohr_per_ang;
+          }
+      }
+  return 0;
 }
 
 int64_t orc_jk(const orc_basis* bs, const int* bf_off, int nbf, const double* Ks,

@@ -83,6 +83,32 @@ int64_t orc_jk(const orc_basis* bs, const int* bf_off, int nbf,
                const double* Kschwarz, double schwarz_thresh, const double* D,
                double* J, double* K, int nthreads);
 
+// Per-thread J/K accumulators that persist across calls (one nbf x nbf pair
+// per thread, as compute_2body_fock keeps one G per thread,
+// hartree-fock++.cc:1601-1607): create, add the contributions of listed bra
+// shell pairs (canonical pair indices s1 (s1+1)/2 + s2, s2 <= s1; returns
+// the computed quartets and their integral count), reduce into J/K (adds
+// the symmetrised sums), destroy.  ket_mask: NULL, or one flag per pair
+// index restricting the ket pairs.
+typedef struct orc_jk_acc orc_jk_acc;
+orc_jk_acc* orc_jk_acc_create(int nbf, int nthreads);
+void orc_jk_acc_destroy(orc_jk_acc* acc);
+int64_t orc_jk_acc_pairs(orc_jk_acc* acc, const orc_basis* bs, const int* bf_off,
+                         const double* Kschwarz, double schwarz_thresh, const double* D,
+                         const int64_t* bra_pairs, int64_t n_bra_pairs,
+                         const unsigned char* ket_mask, int64_t* n_integrals);
+void orc_jk_acc_reduce(const orc_jk_acc* acc, double* J, double* K);
+
+// Counts of the screened pass: unique quartets with K12 K34 >= thresh and
+// their integrals (no integral is computed).
+void orc_count_screened(const orc_basis* bs, const double* Kschwarz, double schwarz_thresh,
+                        int64_t* n_quartets, int64_t* n_integrals);
+
+// The benchmark configurations' synthetic water cluster (Z [3n], xyz [9n]
+// bohr, atoms O, H, H per molecule) from mt19937_64(seed); 0 or -1.
+int orc_water_cluster(int nx, int ny, int nz, double spacing, double jitter, uint64_t seed,
+                      int* Z, double* xyz);
+
 // As orc_jk, but only over the quartets [q_begin, q_end) of the canonical
 // quartet enumeration (used to time a bounded sample); J/K accumulate.
 int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,

@@ -36,13 +36,15 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
+def build_ref(reference_root: str | None = None) -> str | None:
     """Compile the reference's own headers into oracle/_ref/libref.so when the
-    reference tree is present (development container only)."""
-    if not os.path.isdir(os.path.join(reference_root, "include", "libint2")):
-        return None
-    subprocess.check_call(["bash", os.path.join(_HERE, "ref", "build_ref.sh"),
-                           reference_root])
+    reference tree is present (development container only).  The tree is
+    `reference_root`, else $LGX_REFERENCE_ROOT, else the default location
+    that oracle/ref/build_ref.sh knows; the recipe skips quietly when the
+    tree is absent (as on a GPU machine)."""
+    root = reference_root or os.environ.get("LGX_REFERENCE_ROOT")
+    cmd = ["bash", os.path.join(_HERE, "ref", "build_ref.sh")] + ([root] if root else [])
+    subprocess.check_call(cmd)
     return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
 
 
@@ -233,6 +235,79 @@ def jk_sample(basis: OracleBasis, D, Kschwarz, thresh, pair_begin, pair_end,
                               ctypes.c_int64(pair_begin), ctypes.c_int64(pair_end),
                               ctypes.byref(nint))
     return J, K, int(nq), int(nint.value)
+
+
+class JKAccumulator:
+    """Per-thread J/K accumulators kept across calls (orc_jk_acc_*): add the
+    contributions of listed bra shell pairs, then reduce once, as the
+    reference's compute_2body_fock keeps one G per thread."""
+
+    def __init__(self, nbf: int, nthreads: int = 0):
+        lib = _lib()
+        lib.orc_jk_acc_create.restype = ctypes.c_void_p
+        lib.orc_jk_acc_create.argtypes = [ctypes.c_int, ctypes.c_int]
+        lib.orc_jk_acc_destroy.argtypes = [ctypes.c_void_p]
+        lib.orc_jk_acc_pairs.restype = ctypes.c_int64
+        lib.orc_jk_acc_pairs.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Basis), _ip, _dp,
+                                         ctypes.c_double, _dp,
+                                         ctypes.POINTER(ctypes.c_int64), ctypes.c_int64,
+                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+        lib.orc_jk_acc_reduce.argtypes = [ctypes.c_void_p, _dp, _dp]
+        self._lib = lib
+        self.nbf = int(nbf)
+        self._h = lib.orc_jk_acc_create(self.nbf, int(nthreads))
+        if not self._h:
+            raise ValueError("orc_jk_acc_create failed")
+
+    def add_pairs(self, basis: OracleBasis, D, Kschwarz, thresh, pairs, ket_subset=False):
+        """Adds the quartets of bra pairs `pairs` (canonical pair indices
+        s1 (s1 + 1) / 2 + s2, s2 <= s1) with every ket pair up to the bra, or
+        with `ket_subset` only the kets among `pairs` (each unordered quartet
+        of the subset once); returns (n_quartets, n_integrals)."""
+        D = np.ascontiguousarray(D, np.float64)
+        Ks = np.ascontiguousarray(Kschwarz, np.float64)
+        p = np.ascontiguousarray(pairs, np.int64)
+        mask = None
+        if ket_subset:
+            ns = basis.nshell
+            mask = np.zeros(ns * (ns + 1) // 2, np.uint8)
+            mask[p] = 1
+        nint = ctypes.c_int64(0)
+        nq = self._lib.orc_jk_acc_pairs(self._h, ctypes.byref(basis._c),
+                                        _ptr(basis.bf_off, ctypes.c_int),
+                                        _ptr(Ks, ctypes.c_double), ctypes.c_double(thresh),
+                                        _ptr(D, ctypes.c_double), _ptr(p, ctypes.c_int64),
+                                        len(p), None if mask is None else mask.ctypes.data,
+                                        ctypes.byref(nint))
+        if nq < 0:
+            raise ValueError("orc_jk_acc_pairs: bad arguments")
+        return int(nq), int(nint.value)
+
+    def reduce(self):
+        J = np.zeros((self.nbf, self.nbf)); K = np.zeros((self.nbf, self.nbf))
+        self._lib.orc_jk_acc_reduce(self._h, _ptr(J, ctypes.c_double), _ptr(K, ctypes.c_double))
+        return J, K
+
+    def close(self):
+        if self._h:
+            self._lib.orc_jk_acc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def count_screened(basis: OracleBasis, Kschwarz, thresh):
+    """(unique quartets, integrals) of the Schwarz-screened pass."""
+    lib = _lib()
+    lib.orc_count_screened.argtypes = [ctypes.POINTER(_Basis), _dp, ctypes.c_double,
+                                       ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64)]
+    nq, ni = ctypes.c_int64(0), ctypes.c_int64(0)
+    Ks = np.ascontiguousarray(Kschwarz, np.float64)
+    lib.orc_count_screened(ctypes.byref(basis._c), _ptr(Ks, ctypes.c_double),
+                           ctypes.c_double(thresh), ctypes.byref(nq), ctypes.byref(ni))
+    return int(nq.value), int(ni.value)
 
 
 def jk_grad(basis: OracleBasis, D, Kschwarz, natoms, thresh=1e-12, nthreads=0):

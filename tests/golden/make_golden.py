@@ -2,10 +2,10 @@
 code, compiled in place by oracle/ref/build_ref.sh into oracle/_ref/libref.so
 (libint2::Shell::renorm, SolidHarmonicsCoefficients::coeff,
 FmEval_Reference2, BasisSet, DerivMapGenerator and the brute-force ERI of
-src/bin/test_eri/eri.h).  Run in the development container, where the
-reference tree exists:
+src/bin/test_eri/eri.h).  Run where the reference tree exists, naming it
+in LGX_REFERENCE_ROOT:
 
-    python tests/golden/make_golden.py
+    LGX_REFERENCE_ROOT=<libint tree> python tests/golden/make_golden.py
 
 Outputs (numpy .npz, committed):
   boys.npz        F_m(T) from FmEval_Reference2 and FmEval_Reference<long double>
@@ -264,7 +264,8 @@ def eri_d2_fixtures():
                         values=np.concatenate(vals), c1=c1, c2=c2)
 
 
-REFERENCE = "/root/reference"
+# the libint source tree whose test files hold the HF golden values
+REFERENCE = os.environ.get("LGX_REFERENCE_ROOT", "")
 SYMBOL_Z = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10}
 
 
@@ -282,6 +283,8 @@ def _scalar_after(text, name):
 
 
 def hf_fixtures(root=REFERENCE):
+    if not root or not os.path.isdir(root):
+        sys.exit("hf fixtures: set LGX_REFERENCE_ROOT to the libint source tree")
     import re
     hf = os.path.join(root, "tests", "hartree-fock")
     with open(os.path.join(hf, "h2o_rotated.xyz")) as f:

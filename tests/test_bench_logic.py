@@ -81,6 +81,5 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch):
     # under torchrun only rank 0 times the CPU reference; the others exit 0
     import bench
     monkeypatch.setenv("RANK", "1")
-    args = bench.argparse.Namespace(workload="h2o32_cc-pvdz", steps=1, warmup=1, gpus=2,
-                                    ref_budget=1.0)
+    args = bench.argparse.Namespace(workload="h2o32_cc-pvdz", steps=1, warmup=1, gpus=2)
     assert bench.run_reference(args) == 0

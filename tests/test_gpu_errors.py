@@ -104,3 +104,28 @@ int main() {
                            "-Wl,-rpath," + os.path.join(root, "libint_gb300"), "-o", exe])
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, (r.stdout, r.stderr)
+
+
+def test_watchdog_fires_and_context_recovers(lgx):
+    # A bound of zero work chunks per warp makes the program kernels' bounded
+    # work loops give up at their first chunk (no fault, no hang: the loop
+    # ends and raises the context's error flag); the call returns
+    # LGX_ERR_WATCHDOG, the flag is cleared, and with the default bound
+    # restored the same context computes the same J/K as before.  cc-pVDZ
+    # (dd|dd) and (dd|dp) run on the program kernel.
+    atoms = lgx.water_cluster(2, 2, 1, spacing=3.0, jitter=0.2, seed=4)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    D = lgx.random_density(bs.nbf, 20, seed=5)
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    J0, K0, _ = ctx.jk(D, 1e-12, lgx._lgx.LGX_FP64)
+    kinds = {r["kernel"] for r in ctx.last_pass_launches()}
+    assert any(k != "register" for k in kinds), kinds
+    ctx.set_watchdog(0)
+    with pytest.raises(lgx.LgxError) as e:
+        ctx.jk(D, 1e-12, lgx._lgx.LGX_FP64)
+    assert e.value.status == lgx._lgx.LGX_ERR_WATCHDOG
+    ctx.set_watchdog(-1)
+    J1, K1, _ = ctx.jk(D, 1e-12, lgx._lgx.LGX_FP64)
+    assert np.max(np.abs(J1 - J0)) < 1e-12 and np.max(np.abs(K1 - K0)) < 1e-12
+    ctx.close()
