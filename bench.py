@@ -260,16 +260,28 @@ def kernel_roofline(launches, peaks, workload, mode):
     pipe = "fp32" if r["fp32"] else "fp64"
     ach = r["flops"] / (r["ms_avg"] * 1e-3) / 1e12
     name = kernel_name(r)
+    f64 = r.get("flops_fp64", 0.0 if r["fp32"] else r["flops"])
+    peak = peaks[pipe]
+    bound = pipe + "-pipe"
+    if r["fp32"] and f64 > 0:
+        # FP32 launch of the mixed scheme with its Boys function in FP64: the
+        # time at peak is the FP64 share at the FP64 peak plus the rest at
+        # the FP32 peak
+        peak = r["flops"] / (f64 / peaks["fp64"] + (r["flops"] - f64) / peaks["fp32"])
+        bound = "fp64+fp32 pipes"
     tr = NCU_TRAFFIC.get((workload, mode, name))
-    out = {"bound": pipe + "-pipe", "kernel": name, "achieved": ach, "peak": peaks[pipe],
-           "unit": "TFLOP/s", "frac": ach / peaks[pipe],
+    out = {"bound": bound, "kernel": name, "achieved": ach, "peak": peak,
+           "unit": "TFLOP/s", "frac": ach / peak, "flops_fp64_per_launch": f64,
            "traffic": tr[0] if tr else None,
            "launch_ms": r["ms_avg"], "share_of_pass": r["ms_avg"] / total if total else None,
            "flops_per_launch": r["flops"], "prim_quartets": r["prim_quartets"],
            "quartets": r["quartets"],
            "peak_source": "cuBLAS %s measured live in this run (MEASURED_PEAKS.json holds "
-                          "no FP64/FP32 CUDA-core figure)" % ("SGEMM, no TF32" if r["fp32"]
-                                                              else "DGEMM")}
+                          "no FP64/FP32 CUDA-core figure)" % (
+                              "DGEMM %.2f / SGEMM (no TF32) %.1f TFLOP/s, blended by the "
+                              "launch's FP64 / FP32 operations" % (peaks["fp64"], peaks["fp32"])
+                              if bound.startswith("fp64+") else
+                              ("SGEMM, no TF32" if r["fp32"] else "DGEMM"))}
     if tr:
         out["traffic_source"] = "ncu capture of this workload's launch, not this run: " + tr[1]
     return out
@@ -368,6 +380,46 @@ def oracle_subset_check(lg, bs, D, thresh, local, modes, npairs=CHECK_SUBSET_PAI
     return out
 
 
+def mixed_integral_error(lg, bs, thresh, local, modes, n=20000):
+    """Maximum integral error of each mixed mode against the FP64 oracle on
+    quartets sampled from the FP32 space of the screened pass (thresh <=
+    K12 K34 < MIXED_THRESH), through the batched entry, which runs the same
+    FP32 kernel family as the J/K pass in store mode."""
+    from oracle import oracle
+    ob = oracle.OracleBasis.from_basis(bs)
+    K = oracle.schwarz(ob, cpu_threads())
+    ns = ob.nshell
+    a, b = np.tril_indices(ns)
+    kp = K[a, b]
+    sig = kp * K.max() >= thresh
+    a, b, kp = a[sig], b[sig], kp[sig]
+    rng = np.random.default_rng(SEED + 13)
+    got = []
+    for _ in range(50):
+        i = rng.integers(0, len(a), 20 * n)
+        j = rng.integers(0, len(a), 20 * n)
+        w = kp[i] * kp[j]
+        ok = (w >= thresh) & (w < MIXED_THRESH)
+        got.append(np.stack([i[ok], j[ok]], 1))
+        if sum(len(g) for g in got) >= n:
+            break
+    p = np.concatenate(got)[:n]
+    q = np.stack([a[p[:, 0]], b[p[:, 0]], a[p[:, 1]], b[p[:, 1]]], 1).astype(np.int32)
+    ctx = lg.Context(local)
+    ctx.set_basis(bs)
+    out = {"quartets": int(len(q)), "integrals": None}
+    ref = None
+    for name, mode in modes:
+        v, offs, _ = ctx.compute_batch(q, mode=mode, mixed_thresh=MIXED_THRESH)
+        if ref is None:
+            ref, _ = oracle.compute_batch(ob, q, offs, len(v), nthreads=cpu_threads())
+            out["integrals"] = int(len(v))
+            out["max_abs_integral"] = float(np.max(np.abs(ref)))
+        out[name] = float(np.max(np.abs(v - ref)))
+    ctx.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     import libint_gb300 as lg
@@ -424,6 +476,10 @@ def run_gpu(args):
         J64, K64 = dJ.cpu().numpy(), dK.cpu().numpy()
         msmx, stmx, laumx = timed(lg._lgx.LGX_MIXED, args.warmup, args.steps)
         Jmx, Kmx = dJ.cpu().numpy(), dK.cpu().numpy()
+        # the faster, less exact variant (Boys function of the FP32 quartets
+        # in FP32 too), over its own step count
+        msfb, stfb, laufb = timed(lg._lgx.LGX_MIXED_FP32_BOYS, 1, args.alt_steps)
+        Jfb, Kfb = dJ.cpu().numpy(), dK.cpu().numpy()
 
         # e2e: host buffers through the public API (lgx_jk: D copied in, the
         # pass, J and K copied out); each step's interval brackets that call
@@ -449,6 +505,9 @@ def run_gpu(args):
     te2e = max_over_ranks(te2e, world)
     v64 = world * st64.integrals * args.fp64_steps / t64
     vmx = world * stmx.integrals * args.steps / tmx
+    tfb = agg(msfb) / 1e3
+    vfb = world * stfb.integrals * args.alt_steps / tfb
+    efb = lg.jk_energies(D, Jfb, Kfb)
     ve2e = world * st_e.integrals * args.e2e_steps / te2e
     e64 = lg.jk_energies(D, J64, K64)
     emx = lg.jk_energies(D, Jmx, Kmx)
@@ -506,7 +565,13 @@ def run_gpu(args):
     subset = None
     if not args.no_check:
         subset = oracle_subset_check(lg, bs, D, thresh, local,
-                                     (("fp64", lg._lgx.LGX_FP64), ("mixed", lg._lgx.LGX_MIXED)))
+                                     (("fp64", lg._lgx.LGX_FP64), ("mixed", lg._lgx.LGX_MIXED),
+                                      ("mixed_fp32_boys", lg._lgx.LGX_MIXED_FP32_BOYS)))
+        ierr = mixed_integral_error(lg, bs, thresh, local,
+                                    (("mixed", lg._lgx.LGX_MIXED),
+                                     ("mixed_fp32_boys", lg._lgx.LGX_MIXED_FP32_BOYS)))
+    else:
+        ierr = None
     cpu = None
     if not args.no_cpu:
         arm = CpuArm(args.workload)
@@ -537,10 +602,25 @@ def run_gpu(args):
                  "roofline_pass": {"bound": "fp64-pipe", "achieved": roof64,
                                    "peak": peaks["fp64"], "unit": "TFLOP/s",
                                    "frac": roof64 / peaks["fp64"]}},
+        "mixed_scheme": "FP32 VRR/HRR/contraction/transform for quartets with K12 K34 < "
+                        "%g; the Boys function of those quartets (its argument T, Taylor or "
+                        "asymptotic branch, e^-T, downward recursion) in FP64; all other "
+                        "quartets in FP64; J/K accumulated in FP64" % MIXED_THRESH,
         "mixed_error": {"vs": "GPU FP64 pass of the same step (full pass)",
                         "dE_J": abs(emx[0] - e64[0]), "dE_K": abs(emx[1] - e64[1]),
                         "max_abs_dJ": float(np.max(np.abs(Jmx - J64))),
                         "max_abs_dK": float(np.max(np.abs(Kmx - K64)))},
+        "max_integral_error_vs_oracle": ierr,
+        "mixed_fp32_boys": {
+            "scheme": "as mixed, with the Boys function of the FP32 quartets in FP32",
+            "value": vfb, "unit": "ERI/s", "steps": args.alt_steps, "warmup": 1,
+            "ms_per_step": tfb / args.alt_steps * 1e3, "speedup_vs_fp64": vfb / v64,
+            "mixed_error": {"vs": "GPU FP64 pass (full pass)",
+                            "dE_J": abs(efb[0] - e64[0]), "dE_K": abs(efb[1] - e64[1]),
+                            "max_abs_dJ": float(np.max(np.abs(Jfb - J64))),
+                            "max_abs_dK": float(np.max(np.abs(Kfb - K64)))},
+            "roofline_concurrent": kernel_roofline(laufb, peaks, args.workload,
+                                                   "mixed_fp32_boys")},
         "oracle_subset": subset,
         "speedup_mixed_vs_fp64": vmx / v64,
         "roofline": dom_ser,
@@ -554,7 +634,7 @@ def run_gpu(args):
         "e2e": {"value": ve2e, "unit": "ERI/s", "steps": args.e2e_steps,
                 "h2d_bytes_per_step": nbf * nbf * 8, "d2h_bytes_per_step": 2 * nbf * nbf * 8},
         "gpu_launches": int(stmx.launches) * args.steps + int(st64.launches) * args.fp64_steps
-        + int(st_e.launches) * args.e2e_steps,
+        + int(stfb.launches) * args.alt_steps + int(st_e.launches) * args.e2e_steps,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
@@ -789,6 +869,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="timed passes of the FP64 comparison (default 2)")
     ap.add_argument("--fp64-warmup", type=int, default=1)
+    ap.add_argument("--alt-steps", type=int, default=2,
+                    help="timed passes of the FP32-Boys mixed variant (default 2)")
     ap.add_argument("--e2e-steps", type=int, default=3,
                     help="timed host-buffer passes of the e2e figure (default 3)")
     ap.add_argument("--impl", default="lgx", choices=["lgx", "reference"])

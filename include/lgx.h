@@ -52,9 +52,16 @@ typedef int lgx_status;
 #define LGX_SCREEN_ORIGINAL 0
 #define LGX_SCREEN_CONSERVATIVE 1
 
-/* Precision modes of the batched paths. */
-#define LGX_FP64 0  /* every quartet in FP64                                 */
-#define LGX_MIXED 1 /* FP32 VRR/HRR/contraction when K12*K34 < mixed_thresh  */
+/* Precision modes of the batched paths.  In both mixed modes a quartet whose
+ * Schwarz bound K12*K34 is below mixed_thresh runs its VRR, HRR, contraction
+ * and solid-harmonic transform in FP32, every other quartet entirely in FP64,
+ * and J/K are accumulated in FP64.  LGX_MIXED keeps the Boys function of
+ * the FP32 quartets in FP64 (its argument T, the Taylor or asymptotic
+ * branch, e^{-T} and the downward recursion; Coulomb operator);
+ * LGX_MIXED_FP32_BOYS evaluates it in FP32 as well (faster, less exact). */
+#define LGX_FP64 0
+#define LGX_MIXED 1
+#define LGX_MIXED_FP32_BOYS 2
 
 /* Two-body operators (libint2::Operator, include/libint2/engine.h:98-184). */
 #define LGX_OP_COULOMB 0       /* 1/r                                        */
@@ -96,7 +103,9 @@ lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega);
  * evaluated on the GPU by exactly the device function a class kernel uses:
  * variant 0 the program kernels' FP64 evaluator (mmax <= 16), 1 the
  * register kernels' FP64 evaluator (mmax <= 6), 2 and 3 their FP32
- * counterparts (results widened to double).  The batch counterpart of
+ * counterparts, 4 and 5 the FP64 evaluators of 0 and 1 with each value
+ * rounded to FP32, as the LGX_MIXED scheme's FP32 kernels use them (all
+ * results widened to double).  The batch counterpart of
  * libint's FmEval_Taylor / FmEval_Chebyshev7 eval(F, T, mmax)
  * (include/libint2/boys.h:345-454,679-821), so the evaluators can be
  * checked against libint's reference values on their own. */
@@ -308,6 +317,9 @@ typedef struct {
   double flops;            /* algorithmic FP operations (FMA = 2)             */
   double ms;               /* device time of the launch (CUDA events on the
                               context's stream; -1 when not recorded)         */
+  double flops_fp64;       /* of `flops`, those done in FP64 (all of them for
+                              an FP64 launch; the Boys function and its
+                              argument for the mixed scheme's FP32 launches) */
 } lgx_launch_stats;
 
 /* Copies up to `max` per-launch records of the last lgx_jk / lgx_jk_device

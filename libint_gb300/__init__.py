@@ -502,7 +502,7 @@ class Context:
                         "kernel": self._KERNELS.get(r.kernel, str(r.kernel)), "shape": r.shape,
                         "deriv": r.deriv, "quartets": r.quartets,
                         "prim_quartets": r.prim_quartets, "integrals": r.integrals,
-                        "flops": r.flops, "ms": r.ms})
+                        "flops": r.flops, "flops_fp64": r.flops_fp64, "ms": r.ms})
         return out
 
 

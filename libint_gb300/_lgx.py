@@ -25,6 +25,7 @@ LGX_OP_ERFC_COULOMB = 2
 
 LGX_FP64 = 0
 LGX_MIXED = 1
+LGX_MIXED_FP32_BOYS = 2
 LGX_NOALLOC_MAX_NBF = 768
 LGX_SCREEN_ORIGINAL = 0
 LGX_SCREEN_CONSERVATIVE = 1
@@ -54,7 +55,7 @@ class LgxLaunchStats(ctypes.Structure):
                 ("shape", ctypes.c_int32), ("deriv", ctypes.c_int32),
                 ("quartets", ctypes.c_int64), ("prim_quartets", ctypes.c_int64),
                 ("integrals", ctypes.c_int64), ("flops", ctypes.c_double),
-                ("ms", ctypes.c_double)]
+                ("ms", ctypes.c_double), ("flops_fp64", ctypes.c_double)]
 
 
 LGX_PRIM_MAX_M = 15

@@ -211,7 +211,10 @@ def main():
     parts.append("}  // namespace lgx")
     _write_if_changed(os.path.join(GEN_DIR, "post_classes.cuh"), "\n".join(parts) + "\n")
 
-    items = [(p, c) for c in classes for p in ("double", "float")]
+    # (precision, mode): FP64, FP32, and FP32 with the FP64 Boys function of
+    # the mixed scheme
+    variants = (("double", "kModeJK"), ("float", "kModeJK"), ("float", "kModeJKB64"))
+    items = [(v, c) for c in classes for v in variants]
     items.sort(key=lambda it: -_cost(it[1]))
     units = [[] for _ in range(N_UNITS)]
     load = [0] * N_UNITS
@@ -226,17 +229,17 @@ def main():
         names.append(name)
         lines = ["// GENERATED by libint_gb300/codegen/gen_post.py -- do not edit.",
                  '#include "post_classes.cuh"', "", "namespace lgx {"]
-        for prec, c in u:
-            tag = "%s_%d%d%d%d" % (prec[0], *c)
-            decls.append((prec, c, tag))
+        for (prec, mode), c in u:
+            tag = "%s%s_%d%d%d%d" % (prec[0], "b" if mode == "kModeJKB64" else "", *c)
+            decls.append((prec, mode, c, tag))
             post = "PostGen<%d, %d, %d, %d>" % c
             lines.append("cudaError_t post_launch_%s(const EriArgs& a, int grid, int block, "
                          "size_t smem, cudaStream_t st) {" % tag)
-            lines.append("  return launch_eri_t<%s, kModeJK, %s>(a, grid, block, smem, st);" %
-                         (prec, post))
+            lines.append("  return launch_eri_t<%s, %s, %s>(a, grid, block, smem, st);" %
+                         (prec, mode, post))
             lines.append("}")
             lines.append("int post_occ_%s(int block, size_t smem) {" % tag)
-            lines.append("  return occ_t<%s, kModeJK, %s>(block, smem);" % (prec, post))
+            lines.append("  return occ_t<%s, %s, %s>(block, smem);" % (prec, mode, post))
             lines.append("}")
         lines.append("}  // namespace lgx")
         _write_if_changed(os.path.join(GEN_DIR, name), "\n".join(lines) + "\n")
@@ -244,7 +247,7 @@ def main():
     d = ["// GENERATED by libint_gb300/codegen/gen_post.py -- do not edit.",
          "// Run-time dispatch of the program kernels with generated post stages.",
          '#include "../lgx_kernels.cuh"', "", "namespace lgx {"]
-    for prec, c, tag in decls:
+    for prec, mode, c, tag in decls:
         d.append("cudaError_t post_launch_%s(const EriArgs& a, int grid, int block, size_t smem, "
                  "cudaStream_t st);" % tag)
         d.append("int post_occ_%s(int block, size_t smem);" % tag)
@@ -253,24 +256,29 @@ def main():
     def ckey(c):
         return ((c[0] * 8 + c[1]) * 8 + c[2]) * 8 + c[3]
 
-    d.append("// Launches the J/K program kernel of (precision, class) with its")
+    def vkey(prec, mode):
+        return (4096 if prec == "float" else 0) + (8192 if mode == "kModeJKB64" else 0)
+
+    d.append("// Launches the J/K program kernel of (precision, mode, class) with its")
     d.append("// generated post stage; cudaErrorNotSupported when there is none.")
-    d.append("cudaError_t post_launch(bool fp32, int la, int lb, int lc, int ld, const EriArgs& a, "
-             "int grid, int block, size_t smem, cudaStream_t st) {")
-    d.append("  switch ((fp32 ? 4096 : 0) + ((la * 8 + lb) * 8 + lc) * 8 + ld) {")
-    for prec, c, tag in decls:
+    d.append("cudaError_t post_launch(bool fp32, int mode, int la, int lb, int lc, int ld, "
+             "const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {")
+    d.append("  switch ((fp32 ? 4096 : 0) + (mode == kModeJKB64 ? 8192 : 0) + "
+             "((la * 8 + lb) * 8 + lc) * 8 + ld) {")
+    for prec, mode, c, tag in decls:
         d.append("    case %d: return post_launch_%s(a, grid, block, smem, st);" %
-                 ((4096 if prec == "float" else 0) + ckey(c), tag))
+                 (vkey(prec, mode) + ckey(c), tag))
     d.append("  }")
     d.append("  return cudaErrorNotSupported;")
     d.append("}")
     d.append("")
-    d.append("int post_blocks_per_sm(bool fp32, int la, int lb, int lc, int ld, int block, "
-             "size_t smem) {")
-    d.append("  switch ((fp32 ? 4096 : 0) + ((la * 8 + lb) * 8 + lc) * 8 + ld) {")
-    for prec, c, tag in decls:
+    d.append("int post_blocks_per_sm(bool fp32, int mode, int la, int lb, int lc, int ld, "
+             "int block, size_t smem) {")
+    d.append("  switch ((fp32 ? 4096 : 0) + (mode == kModeJKB64 ? 8192 : 0) + "
+             "((la * 8 + lb) * 8 + lc) * 8 + ld) {")
+    for prec, mode, c, tag in decls:
         d.append("    case %d: return post_occ_%s(block, smem);" %
-                 ((4096 if prec == "float" else 0) + ckey(c), tag))
+                 (vkey(prec, mode) + ckey(c), tag))
     d.append("  }")
     d.append("  return 0;")
     d.append("}")

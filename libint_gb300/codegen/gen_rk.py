@@ -33,10 +33,14 @@ RK_MAX_L_STORE = 4
 LMAX = 3
 # (precision, mode, class limit, attenuated operator) variants; the
 # attenuated (erf / erfc) register kernels serve the J/K passes only
+# (the kModeJKB64 / kModeStoreB64 FP32 kernels evaluate the Boys function in
+# FP64: the mixed scheme's FP32 quartets)
 VARIANTS = [("double", "kModeJK", RK_MAX_L, False), ("float", "kModeJK", RK_MAX_L, False),
+            ("float", "kModeJKB64", RK_MAX_L, False),
             ("double", "kModeStore", RK_MAX_L_STORE, False),
             ("double", "kModeSchwarz", RK_MAX_L_STORE, False),
             ("float", "kModeStore", RK_MAX_L_STORE, False),
+            ("float", "kModeStoreB64", RK_MAX_L_STORE, False),
             ("double", "kModeJK", RK_MAX_L, True), ("float", "kModeJK", RK_MAX_L, True)]
 N_UNITS = 24  # instantiation translation units (compiled in parallel)
 
@@ -355,7 +359,8 @@ def write_units(gen_dir):
              "((la * 8 + lb) * 8 + lc) * 8 + ld;")
     d.append("  switch (key) {")
     for prec, mode, att, c, fn in sorted(decls, key=lambda x: x[4]):
-        mode_id = {"kModeStore": 0, "kModeSchwarz": 1, "kModeJK": 2}[mode]
+        mode_id = {"kModeStore": 0, "kModeSchwarz": 1, "kModeJK": 2, "kModeJKB64": 4,
+                   "kModeStoreB64": 5}[mode]
         key = ((((1 if att else 0) * 2 + (1 if prec == "float" else 0)) * 8 + mode_id) * 4096) + \
             ((c[0] * 8 + c[1]) * 8 + c[2]) * 8 + c[3]
         d.append("    case %d: return %s(a, work, nsm, st);" % (key, fn))
@@ -367,6 +372,8 @@ def write_units(gen_dir):
     d.append("  const int L = la + lb + lc + ld;")
     d.append("  if (att) return mode == kModeJK && L <= %d;" % RK_MAX_L)
     d.append("  if (mode == kModeJK) return L <= %d;" % RK_MAX_L)
+    d.append("  if (mode == kModeJKB64) return fp32 && L <= %d;" % RK_MAX_L)
+    d.append("  if (mode == kModeStoreB64) return fp32 && L <= %d;" % RK_MAX_L_STORE)
     d.append("  if (mode == kModeStore) return L <= %d;" % RK_MAX_L_STORE)
     d.append("  if (mode == kModeSchwarz) return !fp32 && L <= %d;" % RK_MAX_L_STORE)
     d.append("  return false;")

@@ -8,28 +8,52 @@ cudaError_t post_launch_d_3333(const EriArgs& a, int grid, int block, size_t sme
 int post_occ_d_3333(int block, size_t smem) {
   return occ_t<double, kModeJK, PostGen<3, 3, 3, 3>>(block, smem);
 }
-cudaError_t post_launch_d_3033(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<double, kModeJK, PostGen<3, 0, 3, 3>>(a, grid, block, smem, st);
+cudaError_t post_launch_f_3232(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJK, PostGen<3, 2, 3, 2>>(a, grid, block, smem, st);
 }
-int post_occ_d_3033(int block, size_t smem) {
-  return occ_t<double, kModeJK, PostGen<3, 0, 3, 3>>(block, smem);
+int post_occ_f_3232(int block, size_t smem) {
+  return occ_t<float, kModeJK, PostGen<3, 2, 3, 2>>(block, smem);
 }
-cudaError_t post_launch_d_2132(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<double, kModeJK, PostGen<2, 1, 3, 2>>(a, grid, block, smem, st);
+cudaError_t post_launch_f_3033(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJK, PostGen<3, 0, 3, 3>>(a, grid, block, smem, st);
 }
-int post_occ_d_2132(int block, size_t smem) {
-  return occ_t<double, kModeJK, PostGen<2, 1, 3, 2>>(block, smem);
+int post_occ_f_3033(int block, size_t smem) {
+  return occ_t<float, kModeJK, PostGen<3, 0, 3, 3>>(block, smem);
 }
-cudaError_t post_launch_d_3122(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<double, kModeJK, PostGen<3, 1, 2, 2>>(a, grid, block, smem, st);
+cudaError_t post_launch_d_2033(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 0, 3, 3>>(a, grid, block, smem, st);
 }
-int post_occ_d_3122(int block, size_t smem) {
-  return occ_t<double, kModeJK, PostGen<3, 1, 2, 2>>(block, smem);
+int post_occ_d_2033(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 0, 3, 3>>(block, smem);
 }
-cudaError_t post_launch_d_2122(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<double, kModeJK, PostGen<2, 1, 2, 2>>(a, grid, block, smem, st);
+cudaError_t post_launch_fb_2222(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJKB64, PostGen<2, 2, 2, 2>>(a, grid, block, smem, st);
 }
-int post_occ_d_2122(int block, size_t smem) {
-  return occ_t<double, kModeJK, PostGen<2, 1, 2, 2>>(block, smem);
+int post_occ_fb_2222(int block, size_t smem) {
+  return occ_t<float, kModeJKB64, PostGen<2, 2, 2, 2>>(block, smem);
+}
+cudaError_t post_launch_f_3122(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJK, PostGen<3, 1, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_f_3122(int block, size_t smem) {
+  return occ_t<float, kModeJK, PostGen<3, 1, 2, 2>>(block, smem);
+}
+cudaError_t post_launch_d_1132(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<1, 1, 3, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_1132(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<1, 1, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_fb_2122(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJKB64, PostGen<2, 1, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_fb_2122(int block, size_t smem) {
+  return occ_t<float, kModeJKB64, PostGen<2, 1, 2, 2>>(block, smem);
+}
+cudaError_t post_launch_f_3031(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJK, PostGen<3, 0, 3, 1>>(a, grid, block, smem, st);
+}
+int post_occ_f_3031(int block, size_t smem) {
+  return occ_t<float, kModeJK, PostGen<3, 0, 3, 1>>(block, smem);
 }
 }  // namespace lgx

@@ -2,17 +2,23 @@
 #include "post_classes.cuh"
 
 namespace lgx {
-cudaError_t post_launch_f_3133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<float, kModeJK, PostGen<3, 1, 3, 3>>(a, grid, block, smem, st);
+cudaError_t post_launch_f_2233(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJK, PostGen<2, 2, 3, 3>>(a, grid, block, smem, st);
 }
-int post_occ_f_3133(int block, size_t smem) {
-  return occ_t<float, kModeJK, PostGen<3, 1, 3, 3>>(block, smem);
+int post_occ_f_2233(int block, size_t smem) {
+  return occ_t<float, kModeJK, PostGen<2, 2, 3, 3>>(block, smem);
 }
-cudaError_t post_launch_f_2133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<float, kModeJK, PostGen<2, 1, 3, 3>>(a, grid, block, smem, st);
+cudaError_t post_launch_d_3133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 1, 3, 3>>(a, grid, block, smem, st);
 }
-int post_occ_f_2133(int block, size_t smem) {
-  return occ_t<float, kModeJK, PostGen<2, 1, 3, 3>>(block, smem);
+int post_occ_d_3133(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 1, 3, 3>>(block, smem);
+}
+cudaError_t post_launch_fb_2133(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJKB64, PostGen<2, 1, 3, 3>>(a, grid, block, smem, st);
+}
+int post_occ_fb_2133(int block, size_t smem) {
+  return occ_t<float, kModeJKB64, PostGen<2, 1, 3, 3>>(block, smem);
 }
 cudaError_t post_launch_f_3132(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
   return launch_eri_t<float, kModeJK, PostGen<3, 1, 3, 2>>(a, grid, block, smem, st);
@@ -20,11 +26,17 @@ cudaError_t post_launch_f_3132(const EriArgs& a, int grid, int block, size_t sme
 int post_occ_f_3132(int block, size_t smem) {
   return occ_t<float, kModeJK, PostGen<3, 1, 3, 2>>(block, smem);
 }
-cudaError_t post_launch_f_2222(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<float, kModeJK, PostGen<2, 2, 2, 2>>(a, grid, block, smem, st);
+cudaError_t post_launch_d_2132(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<2, 1, 3, 2>>(a, grid, block, smem, st);
 }
-int post_occ_f_2222(int block, size_t smem) {
-  return occ_t<float, kModeJK, PostGen<2, 2, 2, 2>>(block, smem);
+int post_occ_d_2132(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<2, 1, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_fb_2231(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJKB64, PostGen<2, 2, 3, 1>>(a, grid, block, smem, st);
+}
+int post_occ_fb_2231(int block, size_t smem) {
+  return occ_t<float, kModeJKB64, PostGen<2, 2, 3, 1>>(block, smem);
 }
 cudaError_t post_launch_f_3131(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
   return launch_eri_t<float, kModeJK, PostGen<3, 1, 3, 1>>(a, grid, block, smem, st);
@@ -32,10 +44,16 @@ cudaError_t post_launch_f_3131(const EriArgs& a, int grid, int block, size_t sme
 int post_occ_f_3131(int block, size_t smem) {
   return occ_t<float, kModeJK, PostGen<3, 1, 3, 1>>(block, smem);
 }
-cudaError_t post_launch_f_3022(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
-  return launch_eri_t<float, kModeJK, PostGen<3, 0, 2, 2>>(a, grid, block, smem, st);
+cudaError_t post_launch_f_2032(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<float, kModeJK, PostGen<2, 0, 3, 2>>(a, grid, block, smem, st);
 }
-int post_occ_f_3022(int block, size_t smem) {
-  return occ_t<float, kModeJK, PostGen<3, 0, 2, 2>>(block, smem);
+int post_occ_f_2032(int block, size_t smem) {
+  return occ_t<float, kModeJK, PostGen<2, 0, 3, 2>>(block, smem);
+}
+cudaError_t post_launch_d_3022(const EriArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  return launch_eri_t<double, kModeJK, PostGen<3, 0, 2, 2>>(a, grid, block, smem, st);
+}
+int post_occ_d_3022(int block, size_t smem) {
+  return occ_t<double, kModeJK, PostGen<3, 0, 2, 2>>(block, smem);
 }
 }  // namespace lgx

@@ -5,16 +5,25 @@ namespace lgx {
 cudaError_t rk_launch_d_jk_1032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 1, 0, 3, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_2031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_2031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 2, 0, 3, 1, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 1, 2, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_att_3030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 3, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 1, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 3, 0, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 1, 2, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_store_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 3, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 0, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 1, 1, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

@@ -5,16 +5,31 @@ namespace lgx {
 cudaError_t rk_launch_d_jk_1122(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 1, 1, 2, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_2121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 1, 2, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_2121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 2, 1, 2, 1, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_1130(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 1, 3, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_0032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 0, 1, 1, kModeSchwarz, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 2, 2, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 1, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_storeb64_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 2, 0, kModeStoreB64, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_store_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 2, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jkb64_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 0, kModeJKB64, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_schwarz_0010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 1, 0, kModeSchwarz, false>(a, work, nsm, st);
 }
 }  // namespace lgx

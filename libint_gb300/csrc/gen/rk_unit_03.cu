@@ -5,16 +5,31 @@ namespace lgx {
 cudaError_t rk_launch_d_jk_1131(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 1, 1, 3, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_2130(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 1, 3, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_2130(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 2, 1, 3, 0, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_2021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 2, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 2, 0, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 2, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_storeb64_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 2, 0, 1, 1, kModeStoreB64, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 1, 1, kModeJK, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_storeb64_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 1, kModeStoreB64, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jkb64_1010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 1, 0, kModeJKB64, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_store_0010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 1, 0, kModeStore, false>(a, work, nsm, st);
 }
 }  // namespace lgx

@@ -5,25 +5,31 @@ namespace lgx {
 cudaError_t rk_launch_d_jk_2121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 2, 1, 2, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_0033(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 3, 3, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_0033(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 3, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 2, 2, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_1130(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_1021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 2, 1, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_2021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 1, 1, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_schwarz_0031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 1, kModeSchwarz, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_0031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 3, 0, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_0010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 1, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_storeb64_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 2, 0, kModeStoreB64, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_store_1010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 1, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_0010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 1, 0, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

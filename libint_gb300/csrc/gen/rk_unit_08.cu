@@ -5,28 +5,31 @@ namespace lgx {
 cudaError_t rk_launch_d_jk_3021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 3, 0, 2, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_1122(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 1, 2, 2, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1122(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 2, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 1, 2, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_2030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 1, 1, 1, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_att_0032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 3, 2, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 2, 1, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_schwarz_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 3, 0, kModeSchwarz, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 2, 0, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 0, 0, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 0, 0, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_schwarz_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 0, 0, kModeJK, false>(a, work, nsm, st);
 }
 }  // namespace lgx

@@ -5,28 +5,31 @@ namespace lgx {
 cudaError_t rk_launch_f_jk_0033(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<float, 0, 0, 3, 3, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_2022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 2, 2, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_2022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 2, 2, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_2021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_1022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 2, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_att_1031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 1, 1, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_schwarz_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 0, kModeSchwarz, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 1, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_1120(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 1, 2, 0, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_1010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 1, 0, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_0030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 3, 0, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_att_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 2, 0, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_store_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
 }
 cudaError_t rk_launch_d_store_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 0, 0, 0, 0, kModeStore, false>(a, work, nsm, st);
-}
-cudaError_t rk_launch_f_jk_att_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 0, 0, 0, 0, kModeJK, true>(a, work, nsm, st);
 }
 }  // namespace lgx

@@ -5,23 +5,29 @@ namespace lgx {
 cudaError_t rk_launch_f_jk_1032(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<float, 1, 0, 3, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_2031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_2031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 3, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_2030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_1031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 0, 3, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_store_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 2, 0, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_att_1121(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 2, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 2, 0, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_schwarz_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 1, 1, kModeSchwarz, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_1020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 2, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_2011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 2, 0, 1, 1, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_att_0011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 1, 1, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_store_1011(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 1, 0, 1, 1, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_0021(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 1, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_store_0020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 2, 0, kModeStore, false>(a, work, nsm, st);
 }
 cudaError_t rk_launch_d_schwarz_0000(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<double, 0, 0, 0, 0, kModeSchwarz, false>(a, work, nsm, st);

@@ -5,22 +5,28 @@ namespace lgx {
 cudaError_t rk_launch_f_jk_2031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
   return rk_launch_one<float, 2, 0, 3, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_3030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 3, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_att_3030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 3, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_jk_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_2030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 2, 0, 3, 0, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_2020(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 2, 0, 2, 0, kModeJK, false>(a, work, nsm, st);
+cudaError_t rk_launch_d_jk_0022(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 2, 2, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_schwarz_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 1, 0, 3, 0, kModeSchwarz, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_jk_0031(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 0, 0, 3, 1, kModeJK, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_f_jk_att_1030(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<float, 1, 0, 3, 0, kModeJK, true>(a, work, nsm, st);
+cudaError_t rk_launch_f_jkb64_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 1, 1, kModeJKB64, false>(a, work, nsm, st);
 }
-cudaError_t rk_launch_d_store_0010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
-  return rk_launch_one<double, 0, 0, 1, 0, kModeStore, false>(a, work, nsm, st);
+cudaError_t rk_launch_f_store_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 1, 1, kModeStore, false>(a, work, nsm, st);
+}
+cudaError_t rk_launch_f_jk_att_1111(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<float, 1, 1, 1, 1, kModeJK, true>(a, work, nsm, st);
+}
+cudaError_t rk_launch_d_jk_0010(const EriArgs& a, long long work, int nsm, cudaStream_t st) {
+  return rk_launch_one<double, 0, 0, 1, 0, kModeJK, false>(a, work, nsm, st);
 }
 }  // namespace lgx

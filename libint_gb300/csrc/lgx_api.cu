@@ -39,10 +39,11 @@ cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int
                       long long work, int nsm, cudaStream_t st);
 bool rk_available(bool fp32, int mode, bool att, int la, int lb, int lc, int ld);
 cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
-                              PrimPairJK32* out, cudaStream_t st);
-cudaError_t post_launch(bool fp32, int la, int lb, int lc, int ld, const EriArgs& a, int grid,
-                        int block, size_t smem, cudaStream_t st);
-int post_blocks_per_sm(bool fp32, int la, int lb, int lc, int ld, int block, size_t smem);
+                              PrimPairJK32* out, PrimPairJK64* out64, cudaStream_t st);
+cudaError_t post_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
+                        int grid, int block, size_t smem, cudaStream_t st);
+int post_blocks_per_sm(bool fp32, int mode, int la, int lb, int lc, int ld, int block,
+                       size_t smem);
 bool post_info(int la, int lb, int lc, int ld, int* nacc, int* slots);
 }  // namespace lgx
 
@@ -129,7 +130,7 @@ struct BinCache {
   DBuf class_lists;                 // pair ids of every pair class, sorted
   std::vector<long long> class_off; // offsets of each class in class_lists
   // FP32 records per list position (PrimPairJK32 layout) and their source
-  DBuf rec_idx, rec_src, recs;
+  DBuf rec_idx, rec_src, recs, recs64;
   long long nrec = 0;
   unsigned long long rec_version = ~0ull;  // pairs_version the records hold
   std::vector<std::unique_ptr<BinHost>> bins;
@@ -152,6 +153,7 @@ struct PassRec {
   int bin, sp;
   bool fp32;
   Variant v;
+  int mode;  // kernel mode of the launch
 };
 struct PassRecs {
   std::vector<PassRec> recs;
@@ -212,6 +214,7 @@ struct lgx_context {
   // (H2O)8 and (H2O)64 cc-pVTZ); 2: as 0 but issued in bin order
   int branch_policy = 1;
   int fp64_bps = 0;
+  int fp32_bps = 0;  // as fp64_bps, for the FP32 launches of a mixed pass
   cudaStream_t s64[kMaxBranches] = {}, s32[kMaxBranches] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[2 * kMaxBranches] = {};
   cudaStream_t launch_stream = nullptr;
@@ -264,6 +267,19 @@ lgx_status fail(lgx_context* c, lgx_status s, const std::string& msg) {
     if (e_ != cudaSuccess)                                                    \
       return fail(ctx, LGX_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
   } while (0)
+
+// Precision modes (LGX_FP64, LGX_MIXED, LGX_MIXED_FP32_BOYS): whether a pass
+// splits off an FP32 space, and the kernel mode of its FP32 launches.  The
+// mixed scheme's FP32 kernels evaluate the Boys function in FP64 for the
+// Coulomb operator; the attenuated operators' FP32 kernels keep it in FP32.
+bool mixed_mode(int mode) { return mode == LGX_MIXED || mode == LGX_MIXED_FP32_BOYS; }
+bool valid_mode(int mode) { return mode == LGX_FP64 || mixed_mode(mode); }
+int fp32_kernel_mode(const lgx_context* ctx, int mode, int base_mode) {
+  if (!mixed_mode(mode)) return -1;
+  const bool b64 = mode == LGX_MIXED && ctx->op == LGX_OP_COULOMB;
+  if (base_mode == kModeJK) return b64 ? kModeJKB64 : kModeJK;
+  return b64 ? kModeStoreB64 : kModeStore;
+}
 
 // ------------------------------------------------------- host constants
 // Boys table: F_m(k/32), m < kBoysCols, from the Maclaurin series (top m)
@@ -557,7 +573,7 @@ lgx_status ensure_jk_records(lgx_context* ctx, BasisDev& B) {
   BinCache& C = ctx->bins;
   if (C.rec_version == B.pairs_version) return LGX_OK;
   CK(launch_jk_records(B.pprims.as<PrimPairRec>(), C.rec_src.as<int>(), C.nrec,
-                       C.recs.as<PrimPairJK32>(), ctx->stream));
+                       C.recs.as<PrimPairJK32>(), C.recs64.as<PrimPairJK64>(), ctx->stream));
   C.rec_version = B.pairs_version;
   return LGX_OK;
 }
@@ -597,7 +613,8 @@ lgx_status plan_launch(lgx_context* ctx, const ProgDev& P, int mode, bool fp32,
     L.stride = (std::max(P.host.nacc + P.host.vrr_work, slots) + 1) & ~1;
   }
   auto occupancy = [&](int block, size_t smem) {
-    return gen ? post_blocks_per_sm(fp32, P.host.la, P.host.lb, P.host.lc, P.host.ld, block, smem)
+    return gen ? post_blocks_per_sm(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, block,
+                                    smem)
                : eri_blocks_per_sm(mode, fp32, block, smem);
   };
   const size_t slot_bytes = size_t(L.stride) * elt;
@@ -684,7 +701,7 @@ int choose_group(double nq_avg) {
 
 bool post_gen_ok(const lgx_context* ctx, const BasisDev& B, const ProgDev& P, int mode) {
   int nacc = 0, slots = 0;
-  return ctx->use_post && mode == kModeJK && B.std_pure && P.host.deriv == 0 &&
+  return ctx->use_post && mode_jk(mode) && B.std_pure && P.host.deriv == 0 &&
          ctx->op == LGX_OP_COULOMB &&
          post_info(P.host.la, P.host.lb, P.host.lc, P.host.ld, &nacc, &slots);
 }
@@ -780,7 +797,7 @@ lgx_status run_eri(lgx_context* ctx, BasisDev& B, const ProgDev& P, int mode, bo
   a.max_chunks = ctx->watchdog_chunks >= 0 ? ctx->watchdog_chunks : nwork / a.chunk + 2;
   if (own_counter) CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), lst));
   if (gen)
-    CK(post_launch(fp32, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, L.grid, L.block, L.smem,
+    CK(post_launch(fp32, mode, P.host.la, P.host.lb, P.host.lc, P.host.ld, a, L.grid, L.block, L.smem,
                    lst));
   else
     CK(launch_eri(a, mode, fp32, L.grid, L.block, L.smem, lst));
@@ -826,10 +843,12 @@ Canon canonicalize(const BasisDev& B, const int* s) {
 }
 
 // Explicit quartet list -> grouped launches (store mode).
+// mode32: kernel mode of the FP32 items (quartets with K12 K34 <
+// mixed_thresh; kModeStore or kModeStoreB64), used when mixed_thresh > 0.
 lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, long long n,
                         int deriv, int mode, double mixed_thresh, const int64_t* offsets,
                         double* d_out, int* d_isnull, double precision, int screening,
-                        double* d_kschwarz) {
+                        double* d_kschwarz, int mode32 = kModeStore) {
   // class key of each quartet from a (la, lb, lc, ld) table, counting
   // passes, and a stable scatter of the work items into one array grouped by
   // key (ascending key order, as the launches below go); long lists split
@@ -1018,7 +1037,7 @@ lgx_status run_explicit(lgx_context* ctx, BasisDev& B, const int32_t* quartets, 
     a.is_null = d_isnull;
     a.kschwarz = d_kschwarz;
     const double nq = grp.nq / double(std::max<size_t>(1, grp.count));
-    s = run_eri(ctx, B, *P, mode, fp32, a, a.nitems, nq);
+    s = run_eri(ctx, B, *P, fp32 ? mode32 : mode, fp32, a, a.nitems, nq);
     if (s != LGX_OK) break;
     ++gi;
   }
@@ -1136,6 +1155,7 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
     CK(C.rec_idx.ensure(idx.size() * sizeof(int2)));
     CK(C.rec_src.ensure(std::max<size_t>(1, src.size()) * sizeof(int)));
     CK(C.recs.ensure(std::max<size_t>(1, src.size()) * sizeof(PrimPairJK32)));
+    CK(C.recs64.ensure(std::max<size_t>(1, src.size()) * sizeof(PrimPairJK64)));
     CK(cudaMemcpyAsync(C.rec_idx.p, idx.data(), idx.size() * sizeof(int2),
                        cudaMemcpyHostToDevice, ctx->stream));
     if (!src.empty())
@@ -1238,10 +1258,27 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
   return LGX_OK;
 }
 
-// Algorithmic FP operations of the per-primitive-quartet prologue (pair
-// combination, T, the Boys interpolation and downward recursion, VRR
-// factors), counted from the kernel source; exp/sqrt/div count as one each.
-double prologue_flops(int mmax) { return 60.0 + 3.0 * (mmax + 1); }
+// Algorithmic FP operations of the per-primitive-quartet prologue, counted
+// from the equations of libint's primitive data (engine.impl.h:1389-1466),
+// each add, multiply, divide, square root or exponential one operation and
+// an FMA two:
+//   zeta + eta, 1/(zeta + eta), rho = zeta eta / (zeta + eta)        4
+//   P - Q, |P - Q|^2, T = rho |P - Q|^2                              9
+//   pfac = K_ab K_cd / sqrt(zeta + eta)                               3
+//   F_mmax(T) by the order-6 Taylor step, e^{-T}, 2T, and the downward
+//   recursion F_m = (2T F_{m+1} + e^{-T}) / (2m + 1)          14 + 3 mmax
+//   (00|00)^(m) = pfac F_m                                      mmax + 1
+//   W - P, W - Q (eta / (zeta + eta), zeta / (zeta + eta), 6 products) 8
+//   P - A, Q - C                                                      6
+//   1/2zeta, 1/2eta, 1/2(zeta + eta), rho/zeta, rho/eta               5
+// = 50 + 4 mmax.  The mixed scheme's FP32 kernels with the Boys function in
+// FP64 form rho, P - Q, T and F_m(T) again in FP64 (27 + 3 mmax on the FP64
+// pipe) besides the FP32 quantities the VRR uses; prologue_flops64 is that
+// FP64 share.
+double prologue_flops(int mmax, bool b64) {
+  return 50.0 + 4.0 * mmax + (b64 ? 13.0 : 0.0);
+}
+double prologue_flops64(int mmax, bool b64) { return b64 ? 27.0 + 3.0 * mmax : 0.0; }
 
 // FP operations of the Cartesian -> solid-harmonic transform of one set.
 double sph_flops(int la, int lb, int lc, int ld, const int* pure) {
@@ -1261,7 +1298,7 @@ double sph_flops(int la, int lb, int lc, int ld, const int* pure) {
 }
 
 int tune_key(const BinHost& bin, int deriv, int mode, bool fp32, int op) {
-  return (((class_index(bin.la, bin.lb, bin.lc, bin.ld) * 2 + deriv) * 4 + mode) * 2 +
+  return (((class_index(bin.la, bin.lb, bin.lc, bin.ld) * 2 + deriv) * 8 + mode) * 2 +
           (fp32 ? 1 : 0)) * 4 + op;
 }
 
@@ -1269,6 +1306,7 @@ int tune_key(const BinHost& bin, int deriv, int mode, bool fp32, int op) {
 void bin_args(const BinCache& C, const BinHost& bin, int sp, EriArgs& a) {
   a.implicit = 1;
   a.jk32 = C.recs.as<PrimPairJK32>();
+  a.jk64 = C.recs64.as<PrimPairJK64>();
   a.bin.bra_rec = C.rec_idx.as<int2>() + C.class_off[bin.bra_class];
   a.bin.ket_rec = C.rec_idx.as<int2>() + C.class_off[bin.ket_class];
   a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
@@ -1286,7 +1324,10 @@ void bin_args(const BinCache& C, const BinHost& bin, int sp, EriArgs& a) {
 // post stage and its staging rows) on a leading sample of the bin's
 // quartets, into scratch accumulators, and keeps the fastest.  Runs once per
 // basis; later passes reuse the choice.
-lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
+// mode32: kernel mode of the FP32 precision space (kModeJK, or kModeJKB64
+// for the mixed scheme with the Boys function in FP64), or -1 when the pass
+// runs every quartet in FP64.
+lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, int mode32,
                      EriArgs base) {
   if (!ctx->tune || ctx->noalloc) return LGX_OK;
   const BinCache& C = ctx->bins;
@@ -1299,11 +1340,12 @@ lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool al
     if (s != LGX_OK) return s;
     for (int sp = 0; sp < 2; ++sp) {
       if (bin.total[sp] == 0) continue;
-      const bool fp32 = (sp == 1) && allow_fp32;
-      const int key = tune_key(bin, deriv, mode, fp32, ctx->op);
+      const bool fp32 = (sp == 1) && mode32 >= 0;
+      const int kmode = fp32 ? mode32 : mode;
+      const int key = tune_key(bin, deriv, kmode, fp32, ctx->op);
       if (ctx->tuned.count(key)) continue;
       std::vector<Variant> cand;
-      const Variant d = default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
+      const Variant d = default_variant(ctx, B, *P, kmode, fp32, true, bin.nq_avg);
       cand.push_back(d);
       if (d.kind == 0) {
         for (int g = 2; g <= 8 && g <= 2 * bin.nq_avg; g *= 2) cand.push_back({0, g, 0});
@@ -1342,7 +1384,7 @@ lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool al
         float ms = 0;
         for (int rep = 0; rep < 2; ++rep) {  // the second run is timed
           CK(cudaEventRecord(ctx->ev0, ctx->stream));
-          s = run_eri(ctx, B, *P, mode, fp32, a, sample, bin.nq_avg, &cand[ci]);
+          s = run_eri(ctx, B, *P, kmode, fp32, a, sample, bin.nq_avg, &cand[ci]);
           if (s != LGX_OK) return s;
           CK(cudaEventRecord(ctx->ev1, ctx->stream));
         }
@@ -1365,7 +1407,7 @@ lgx_status tune_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool al
 // same sequence can be captured into a CUDA graph.  Work counters and
 // primitive counters live in ctx->primcount ([0, nslots) primitive quartets,
 // [nslots, 2 nslots) work counters) and are zeroed by the first node.
-lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
+lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, int mode32,
                         EriArgs base, PassRecs& pr) {
   BinCache& C = ctx->bins;
   pr = PassRecs{};
@@ -1382,7 +1424,7 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
     const BinHost& bin = *C.bins[bi];
     for (int sp = 0; sp < 2; ++sp) {
       if (bin.total[sp] == 0) continue;
-      const bool fp32 = (sp == 1) && allow_fp32;
+      const bool fp32 = (sp == 1) && mode32 >= 0;
       const double est = bin.last_ms[sp] > 0
                              ? bin.last_ms[sp]
                              : 1e-9 * double(bin.total[sp]) * bin.nq_avg * (fp32 ? 1.0 : 8.0);
@@ -1466,31 +1508,33 @@ lgx_status enqueue_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool
     if (s != LGX_OK) return s;
     const int sp = j.sp;
     const bool fp32 = j.fp32;
+    const int kmode = fp32 ? mode32 : mode;
     EriArgs a = base;
     bin_args(C, bin, sp, a);
     a.prim_count = pr.count ? ctx->primcount.as<unsigned long long>() + 2 * j.bi + sp : nullptr;
     a.counter = counters ? counters + 2 * j.bi + sp : nullptr;
-    const auto tv = ctx->tuned.find(tune_key(bin, deriv, mode, fp32, ctx->op));
+    const auto tv = ctx->tuned.find(tune_key(bin, deriv, kmode, fp32, ctx->op));
     const Variant v = tv != ctx->tuned.end()
                           ? tv->second
-                          : default_variant(ctx, B, *P, mode, fp32, true, bin.nq_avg);
+                          : default_variant(ctx, B, *P, kmode, fp32, true, bin.nq_avg);
     cudaStream_t st = ctx->stream;
     if (split) {
       const int b = j.branch;
       st = fp32 ? ctx->s32[b] : ctx->s64[b];
       // program-kernel slot scratch: one region per branch
       ctx->scratch = (fp32 || b > 0) ? &ctx->gscratch_br[(fp32 ? nbr : 0) + b] : &ctx->gscratch;
-      if (!fp32 && allow_fp32) a.max_bps = ctx->fp64_bps;
+      if (!fp32 && mode32 >= 0) a.max_bps = ctx->fp64_bps;
+      if (fp32) a.max_bps = ctx->fp32_bps;
     }
     ctx->launch_stream = st;
     const size_t li = pr.recs.size();
     if (pr.timed) CK(cudaEventRecordWithFlags(ctx->lev[2 * li], st, evflags));
-    s = run_eri(ctx, B, *P, mode, fp32, a, bin.total[sp], bin.nq_avg, &v);
+    s = run_eri(ctx, B, *P, kmode, fp32, a, bin.total[sp], bin.nq_avg, &v);
     if (s != LGX_OK) return s;
     if (pr.timed) CK(cudaEventRecordWithFlags(ctx->lev[2 * li + 1], st, evflags));
     pr.integrals += bin.integrals[sp];
     ++pr.launches;
-    pr.recs.push_back({int(j.bi), sp, fp32, v});
+    pr.recs.push_back({int(j.bi), sp, fp32, v, kmode});
   }
   if (split) {
     for (int b = 0; b < nbr; ++b) {
@@ -1538,12 +1582,16 @@ lgx_status finish_bins(lgx_context* ctx, BasisDev& B, int deriv, bool allow_fp32
     const int lq[4] = {bin.la, bin.lb, bin.lc, bin.ld};
     for (int k = 0; k < 4; ++k) nsph *= pure[k] ? 2 * lq[k] + 1 : ncart(lq[k]);
     // VRR + post stage + transform, then the prologue and the digestion,
-    // which run in the launch's precision too
-    const double flops = double(np) * (double(P->host.vrr_flops) + prologue_flops(P->host.mmax)) +
-                         q * (double(P->host.post_flops) +
-                              nsets * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure) +
-                              nsets * 12.0 * nsph);
-    if (r.fp32) f32 += flops; else f64 += flops;
+    // which run in the launch's precision too (the FP64 Boys share of the
+    // mixed scheme's FP32 kernels on the FP64 pipe)
+    const bool b64 = mode_b64(r.mode);
+    const double flops =
+        double(np) * (double(P->host.vrr_flops) + prologue_flops(P->host.mmax, b64)) +
+        q * (double(P->host.post_flops) + nsets * sph_flops(bin.la, bin.lb, bin.lc, bin.ld, pure) +
+             nsets * 12.0 * nsph);
+    const double flops_on64 = r.fp32 ? double(np) * prologue_flops64(P->host.mmax, b64) : flops;
+    f64 += flops_on64;
+    f32 += flops - flops_on64;
     lgx_launch_stats ls{};
     ls.la = bin.la; ls.lb = bin.lb; ls.lc = bin.lc; ls.ld = bin.ld;
     ls.fp32 = r.fp32 ? 1 : 0;
@@ -1554,6 +1602,7 @@ lgx_status finish_bins(lgx_context* ctx, BasisDev& B, int deriv, bool allow_fp32
     ls.prim_quartets = (long long)np;
     ls.integrals = (long long)(q * nsph);
     ls.flops = flops;
+    ls.flops_fp64 = flops_on64;
     ls.ms = -1.0;
     if (pr.timed) {
       float ms = 0;
@@ -1594,12 +1643,12 @@ bool class_profile() {
   return prof;
 }
 
-lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, bool allow_fp32,
+lgx_status run_bins(lgx_context* ctx, BasisDev& B, int mode, int deriv, int mode32,
                     EriArgs base, lgx_jk_stats* stats) {
   PassRecs pr;
-  lgx_status s = enqueue_bins(ctx, B, mode, deriv, allow_fp32, base, pr);
+  lgx_status s = enqueue_bins(ctx, B, mode, deriv, mode32, base, pr);
   if (s != LGX_OK) return s;
-  return finish_bins(ctx, B, deriv, allow_fp32, pr, stats);
+  return finish_bins(ctx, B, deriv, mode32 >= 0, pr, stats);
 }
 
 // Cartesian component index and exponents in the standard order
@@ -2074,6 +2123,7 @@ lgx_status lgx_create(lgx_context** out, int device) {
     if (const char* e = getenv("LGX_GRAPHS")) c->use_graphs = (e[0] != '0');
     if (const char* e = getenv("LGX_OVERLAP")) c->overlap = (e[0] != '0');
     if (const char* e = getenv("LGX_FP64_BPS")) c->fp64_bps = std::max(0, atoi(e));
+    if (const char* e = getenv("LGX_FP32_BPS")) c->fp32_bps = std::max(0, atoi(e));
     if (const char* e = getenv("LGX_BRANCHES")) c->branches = std::max(1, atoi(e));
     if (const char* e = getenv("LGX_BRANCH_POLICY")) c->branch_policy = std::min(2, std::max(0, atoi(e)));
     if (const char* e = getenv("LGX_TUNE_MIN")) c->tune_min = std::max(1LL, atoll(e));
@@ -2269,8 +2319,8 @@ static lgx_status compute_batch(lgx_context* ctx, const int32_t* quartets, int64
   if (!quartets || n < 0 || !out) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
   if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
   if (deriv < 0 || deriv > kMaxDeriv) return fail(ctx, LGX_ERR_INVALID_ARG, "bad deriv");
-  if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
-  if (mode == LGX_MIXED && deriv) return fail(ctx, LGX_ERR_INVALID_ARG, "mixed mode is deriv 0");
+  if (!valid_mode(mode)) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
+  if (mixed_mode(mode) && deriv) return fail(ctx, LGX_ERR_INVALID_ARG, "mixed mode is deriv 0");
   CK(cudaSetDevice(ctx->device));
   BasisDev& B = ctx->basis;
   size_t need = 0;
@@ -2287,7 +2337,7 @@ static lgx_status compute_batch(lgx_context* ctx, const int32_t* quartets, int64
   }
   if (need > out_capacity) return fail(ctx, LGX_ERR_TOO_LARGE, "output buffer too small");
   lgx_status s;
-  if (mode == LGX_MIXED) {
+  if (mixed_mode(mode)) {
     s = ensure_schwarz(ctx, B);
     if (s != LGX_OK) return s;
   }
@@ -2306,8 +2356,8 @@ static lgx_status compute_batch(lgx_context* ctx, const int32_t* quartets, int64
   }
   CK(cudaMemsetAsync(d_out, 0, std::max<size_t>(need, 1) * sizeof(double), ctx->stream));
   s = run_explicit(ctx, B, quartets, n, deriv, kModeStore,
-                   mode == LGX_MIXED ? mixed_thresh : 0.0, offsets, d_out, d_isnull, eps, 0,
-                   nullptr);
+                   mixed_mode(mode) ? mixed_thresh : 0.0, offsets, d_out, d_isnull, eps, 0,
+                   nullptr, mixed_mode(mode) ? fp32_kernel_mode(ctx, mode, kModeStore) : kModeStore);
   if (s != LGX_OK) return s;
   if (!device_out) {
     CK(cudaMemcpyAsync(out, d_out, need * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2341,12 +2391,15 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
                             double thresh, int mode, double mixed, lgx_jk_stats* stats) {
   if (!dD || !dJ || !dK) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
   if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
-  if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
+  if (!valid_mode(mode)) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
   CK(cudaSetDevice(ctx->device));
   BasisDev& B = ctx->basis;
   lgx_status s = ensure_schwarz(ctx, B);
   if (s != LGX_OK) return s;
-  s = build_bins(ctx, B, thresh, mode, mode == LGX_MIXED ? mixed : 0.0);
+  // both mixed modes split the quartets alike; they differ in the kernels
+  const bool mixedp = mixed_mode(mode);
+  const int mode32 = fp32_kernel_mode(ctx, mode, kModeJK);
+  s = build_bins(ctx, B, thresh, mixedp ? LGX_MIXED : LGX_FP64, mixedp ? mixed : 0.0);
   if (s != LGX_OK) return s;
   const double eps = std::numeric_limits<double>::epsilon();
   s = ensure_pairs(ctx, B, std::log(eps), 0);
@@ -2356,7 +2409,7 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
   const size_t nn = size_t(B.nbf) * B.nbf;
   CK(ctx->Jacc.ensure(nn * sizeof(double)));
   CK(ctx->Kacc.ensure(nn * sizeof(double)));
-  if (mode == LGX_MIXED) CK(ctx->Df.ensure(nn * sizeof(float)));
+  if (mixedp) CK(ctx->Df.ensure(nn * sizeof(float)));
   EriArgs a{};
   a.precision = eps;
   a.ln_prec = std::log(eps);
@@ -2366,15 +2419,15 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
   a.Jacc = ctx->Jacc.as<double>();
   a.Kacc = ctx->Kacc.as<double>();
   a.nbf = B.nbf;
-  if (mode == LGX_MIXED) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
-  s = tune_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a);
+  if (mixedp) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
+  s = tune_bins(ctx, B, kModeJK, 0, mode32, a);
   if (s != LGX_OK) return s;
   // the pass: zero the accumulators, FP32 copy of D, every class bin, J/K
   auto enqueue = [&](PassRecs& pr) -> lgx_status {
     CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
     CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
-    if (mode == LGX_MIXED) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
-    lgx_status r = enqueue_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, pr);
+    if (mixedp) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
+    lgx_status r = enqueue_bins(ctx, B, kModeJK, 0, mode32, a, pr);
     if (r != LGX_OK) return r;
     CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
                           ctx->stream));
@@ -2388,7 +2441,7 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
                       ctx->primcount.p, ctx->scratch_sig()};
   for (int i = 0; i < 9; ++i) key.ptr[i] = kp[i];
   key.thresh = thresh;
-  key.mixed = mode == LGX_MIXED ? mixed : 0.0;
+  key.mixed = mixedp ? mixed : 0.0;
   key.mode = mode;
   key.version = ctx->version;
   const bool graphable = ctx->use_graphs;
@@ -2402,7 +2455,7 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
   }
   CK(cudaEventRecord(ctx->ev3, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  s = finish_bins(ctx, B, 0, mode == LGX_MIXED, ctx->jk_recs, stats);
+  s = finish_bins(ctx, B, 0, mixedp, ctx->jk_recs, stats);
   if (s != LGX_OK) return s;
   float pass_ms = 0;
   CK(cudaEventElapsedTime(&pass_ms, ctx->ev2, ctx->ev3));
@@ -2496,7 +2549,7 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!dD || !dJ || !dK) return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
   if (ctx->basis.nshell == 0) return fail(ctx, LGX_ERR_NO_BASIS, "no basis set");
-  if (mode != LGX_FP64 && mode != LGX_MIXED) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
+  if (!valid_mode(mode)) return fail(ctx, LGX_ERR_INVALID_ARG, "bad mode");
   BasisDev& B = ctx->basis;
   if (B.nbf > LGX_NOALLOC_MAX_NBF)
     return fail(ctx, LGX_ERR_TOO_LARGE,
@@ -2504,9 +2557,12 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
                     " exceeds LGX_NOALLOC_MAX_NBF = " + std::to_string(LGX_NOALLOC_MAX_NBF));
   const double eps = std::numeric_limits<double>::epsilon();
   const BinCache& C = ctx->bins;
-  const double mixed_key = mode == LGX_MIXED ? mixed : 0.0;
+  const bool mixedp = mixed_mode(mode);
+  const int mode32 = fp32_kernel_mode(ctx, mode, kModeJK);
+  const double mixed_key = mixedp ? mixed : 0.0;
   if (!B.schwarz_ok || !B.pairs_ok || B.pairs_lnprec != std::log(eps) || B.pairs_method != 0 ||
-      !C.valid || C.thresh != thresh || C.mode != mode || C.mixed != mixed_key ||
+      !C.valid || C.thresh != thresh || C.mode != (mixedp ? LGX_MIXED : LGX_FP64) ||
+      C.mixed != mixed_key ||
       C.subset_version != ctx->subset_version)
     return fail(ctx, LGX_ERR_INVALID_ARG,
                 "lgx_jk_device_noalloc: basis state not prepared for these settings; call "
@@ -2533,7 +2589,7 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   CK(cudaEventRecord(ctx->ev2, ctx->stream));
   CK(cudaMemsetAsync(Jacc, 0, nn * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(Kacc, 0, nn * sizeof(double), ctx->stream));
-  if (mode == LGX_MIXED) CK(launch_d2f(dD, Df, (long long)nn, ctx->stream));
+  if (mixedp) CK(launch_d2f(dD, Df, (long long)nn, ctx->stream));
   EriArgs a{};
   a.precision = eps;
   a.ln_prec = std::log(eps);
@@ -2543,7 +2599,7 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   a.Jacc = Jacc;
   a.Kacc = Kacc;
   a.nbf = B.nbf;
-  s = run_bins(ctx, B, kModeJK, 0, mode == LGX_MIXED, a, stats);
+  s = run_bins(ctx, B, kModeJK, 0, mode32, a, stats);
   if (s != LGX_OK) return s;
   CK(launch_jk_finalize(Jacc, Kacc, dJ, dK, B.nbf, ctx->stream));
   CK(cudaEventRecord(ctx->ev3, ctx->stream));
@@ -2602,8 +2658,8 @@ lgx_status lgx_boys(lgx_context* ctx, int variant, const double* T, int64_t n, i
                     double* F) {
   if (!ctx) return LGX_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(ctx->mu);
-  if (variant < 0 || variant > 3) return fail(ctx, LGX_ERR_INVALID_ARG, "bad Boys variant");
-  const int mmax_cap = (variant == 1 || variant == 3) ? 6 : kBoysMaxM;
+  if (variant < 0 || variant > 5) return fail(ctx, LGX_ERR_INVALID_ARG, "bad Boys variant");
+  const int mmax_cap = (variant == 1 || variant == 3 || variant == 5) ? 6 : kBoysMaxM;
   if (mmax < 0 || mmax > mmax_cap)
     return fail(ctx, LGX_ERR_INVALID_ARG, "mmax out of range for this evaluator");
   if (n < 0 || (n > 0 && (!T || !F))) return fail(ctx, LGX_ERR_INVALID_ARG, "bad arrays");
@@ -2676,9 +2732,9 @@ lgx_status lgx_jk_grad(lgx_context* ctx, const double* D, double* gJ, double* gK
   a.gJ = ctx->gJ.as<double>();
   a.gK = ctx->gK.as<double>();
   a.nbf = B.nbf;
-  s = tune_bins(ctx, B, kModeGrad, 1, false, a);
+  s = tune_bins(ctx, B, kModeGrad, 1, -1, a);
   if (s != LGX_OK) return s;
-  s = run_bins(ctx, B, kModeGrad, 1, false, a, stats);
+  s = run_bins(ctx, B, kModeGrad, 1, -1, a, stats);
   if (s != LGX_OK) return s;
   CK(cudaMemcpyAsync(gJ, ctx->gJ.p, 3 * natoms * sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));

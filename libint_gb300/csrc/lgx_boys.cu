@@ -12,6 +12,11 @@ __device__ void rk_boys_to(int variant, const double* tay, const float* tab32, d
                            double* out) {
   if (variant == 1) {
     rk_boys<MMAX>(tay, T, 1.0, out);
+  } else if (variant == 5) {  // FP64 evaluator, rounded as rk_prim_b64 does
+    double f[MMAX + 1];
+    rk_boys<MMAX>(tay, T, 1.0, f);
+#pragma unroll
+    for (int m = 0; m <= MMAX; ++m) out[m] = double(d2f_int(f[m]));
   } else {
     float f[MMAX + 1];
     rk_boys<MMAX>(tab32, float(T), 1.0f, f);
@@ -33,6 +38,10 @@ __global__ void boys_eval_kernel(const double* tab, const double* tay, const flo
     float f[kBoysMaxM + 1];
     boys_to_stage(tab32, float(T), mmax, 1.0f, f);
     for (int m = 0; m <= mmax; ++m) out[m] = double(f[m]);
+  } else if (variant == 4) {  // FP64 evaluator with FP32 output (mixed scheme)
+    float f[kBoysMaxM + 1];
+    boys_to_stage(tab, inv_odd, T, mmax, 1.0f, f);
+    for (int m = 0; m <= mmax; ++m) out[m] = double(f[m]);
   } else {
     switch (mmax) {
       case 0: rk_boys_to<0>(variant, tay, tab32, T, out); break;
@@ -50,8 +59,9 @@ __global__ void boys_eval_kernel(const double* tab, const double* tay, const flo
 }  // namespace
 
 // variant: 0 program kernel FP64, 1 register kernel FP64 (mmax <= 6),
-// 2 program kernel FP32, 3 register kernel FP32 (mmax <= 6); the caller
-// checks the ranges.
+// 2 program kernel FP32, 3 register kernel FP32 (mmax <= 6), 4 and 5 the
+// FP64 evaluators of 0 and 1 rounded to FP32 (the mixed scheme's FP32
+// kernels); the caller checks the ranges.
 cudaError_t launch_boys_eval(const double* tab, const double* tay, const float* tab32,
                              const double* inv_odd, int variant, const double* T, long long n,
                              int mmax, double* F, cudaStream_t st) {

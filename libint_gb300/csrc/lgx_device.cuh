@@ -58,6 +58,24 @@ __device__ __forceinline__ double f2d_int(float x) {
   return __longlong_as_double((long long)(sign | (exp64 << 52) | mant));
 }
 
+// double -> float, rounded to nearest even, with integer operations only
+// (no FP64-pipe instruction): exact rounding for results in the normal
+// float range; smaller magnitudes (|x| < 2^-126) give a signed zero and
+// larger ones a signed infinity.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  const int e = int((u >> 52) & 0x7ffu) - 1023 + 127;
+  const unsigned long long mant = u & 0xfffffffffffffull;
+  // keep 23 of the 52 mantissa bits: add half an ulp minus one, plus the
+  // lowest kept bit (ties to even); a carry out of the mantissa bumps e
+  const unsigned long long r = (mant + 0xfffffffull + ((mant >> 29) & 1ull)) >> 29;
+  const unsigned bits = ((unsigned)e << 23) + (unsigned)r;  // r = 2^23 carries into e
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255 || bits >= 0x7f800000u) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | bits);
+}
+
 // double(n) for a small non-negative integer n < 2^20 with integer
 // operations only.
 __device__ __forceinline__ double i2d_int(int n) {
@@ -96,6 +114,14 @@ struct __align__(16) PrimPairJK32 {
   float4 pa;
 };
 static_assert(sizeof(PrimPairJK32) == 32, "PrimPairJK32 layout");
+
+// FP64 companion of a PrimPairJK32 record (same index): the pair centre P
+// and the exponent sum zeta, for the FP64 Boys argument of the mixed scheme.
+struct __align__(16) PrimPairJK64 {
+  double P[3];
+  double zeta;
+};
+static_assert(sizeof(PrimPairJK64) == 32, "PrimPairJK64 layout");
 
 // A shell pair with its primitive-pair range (pair list, shell.h:1079-1329).
 struct PairRec {

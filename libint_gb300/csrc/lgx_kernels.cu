@@ -81,7 +81,8 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, P
 // FP32 J/K records: record r takes primitive pair src[r] & 0x7fffffff,
 // oriented on its second centre when the sign bit is set.
 __global__ void jk_records_kernel(const PrimPairRec* __restrict__ pp, const int* __restrict__ src,
-                                  long long n, PrimPairJK32* __restrict__ out) {
+                                  long long n, PrimPairJK32* __restrict__ out,
+                                  PrimPairJK64* __restrict__ out64) {
   const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (r >= n) return;
   const unsigned v = unsigned(src[r]);
@@ -92,13 +93,20 @@ __global__ void jk_records_kernel(const PrimPairRec* __restrict__ pp, const int*
   o.pa = sw ? make_float4(q.fPA2[0], q.fPA2[1], q.fPA2[2], q.fnonsph)
             : make_float4(q.fPA1[0], q.fPA1[1], q.fPA1[2], q.fnonsph);
   out[r] = o;
+  PrimPairJK64 o64;
+  o64.P[0] = q.P[0];
+  o64.P[1] = q.P[1];
+  o64.P[2] = q.P[2];
+  o64.zeta = q.zeta;
+  out64[r] = o64;
 }
 
 cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
-                              PrimPairJK32* out, cudaStream_t st) {
+                              PrimPairJK32* out, PrimPairJK64* out64, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int block = 256;
-  jk_records_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(pp, src, n, out);
+  jk_records_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(pp, src, n, out,
+                                                                           out64);
   return cudaGetLastError();
 }
 
@@ -144,6 +152,8 @@ cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int bloc
     switch (mode) {
       case kModeStore: return launch_eri_t<float, kModeStore>(a, grid, block, smem, st);
       case kModeJK: return launch_eri_t<float, kModeJK>(a, grid, block, smem, st);
+      case kModeStoreB64: return launch_eri_t<float, kModeStoreB64>(a, grid, block, smem, st);
+      case kModeJKB64: return launch_eri_t<float, kModeJKB64>(a, grid, block, smem, st);
     }
   }
   return cudaErrorInvalidValue;
@@ -446,6 +456,8 @@ int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem) {
     switch (mode) {
       case kModeStore: return occ_t<float, kModeStore>(block, smem);
       case kModeJK: return occ_t<float, kModeJK>(block, smem);
+      case kModeStoreB64: return occ_t<float, kModeStoreB64>(block, smem);
+      case kModeJKB64: return occ_t<float, kModeJKB64>(block, smem);
     }
   }
   return 1;

@@ -9,8 +9,21 @@ enum KernelMode : int {
   kModeStore = 0,    // write shell sets in libint buffer order
   kModeSchwarz = 1,  // K(pair) = sqrt(max |(ab|ab)|)
   kModeJK = 2,       // digest into J/K accumulators (deriv 0)
-  kModeGrad = 3      // digest first derivatives into gJ/gK (deriv 1)
+  kModeGrad = 3,     // digest first derivatives into gJ/gK (deriv 1)
+  // FP32 kernels of the mixed scheme with the Boys function in FP64: the
+  // argument T = rho |P - Q|^2, F_m(T) (Taylor / asymptotic branch, e^{-T}
+  // and the downward recursion) in FP64 from the FP64 pair data, then the
+  // VRR / HRR / contraction in FP32; otherwise as kModeJK / kModeStore
+  kModeJKB64 = 4,
+  kModeStoreB64 = 5
 };
+__host__ __device__ constexpr bool mode_jk(int m) { return m == kModeJK || m == kModeJKB64; }
+__host__ __device__ constexpr bool mode_store(int m) {
+  return m == kModeStore || m == kModeStoreB64;
+}
+__host__ __device__ constexpr bool mode_b64(int m) {
+  return m == kModeJKB64 || m == kModeStoreB64;
+}
 
 // Explicit work item: one shell quartet in canonical orientation.
 struct QuartetItem {
@@ -87,6 +100,7 @@ struct EriArgs {
   const PairRec* pairs;
   const PrimPairRec* pprims;
   const PrimPairJK32* jk32;  // J/K bins: coalesced FP32 records (may be null)
+  const PrimPairJK64* jk64;  // J/K bins: their FP64 P and zeta (same layout)
   const unsigned char* pair_swap;  // per pair: 1 if its canonical bra1 is s2
   DevProg prog;
   const double* boys;     // [kBoysRows][kBoysCols] F_m(T_k)

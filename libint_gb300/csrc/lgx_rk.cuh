@@ -212,6 +212,54 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
   return true;
 }
 
+// One primitive quartet into acc (FP32 VRR) with the Boys function in FP64
+// (the kModeJKB64 / kModeStoreB64 kernels of the mixed scheme).  The
+// screening, prefactor and VRR geometry are the FP32 ones of rk_prim above;
+// T = rho |P - Q|^2 is formed in FP64 from the pairs' FP64 centres and
+// exponent sums (1/(zeta + eta) is the FP32 value refined by one Newton
+// step, relative error below 1e-13), F_m(T) comes from the FP64 evaluator
+// (Taylor with the downward recursion and e^{-T}, or the asymptotic branch)
+// and is rounded to FP32 with integer operations before the FP32 pfac.
+template <class C>
+__device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<float>& q,
+                                            const PrimF32& bp, const PrimF32& kp, const double* Pb,
+                                            double zb, const double* Pk, double zk, float* acc) {
+  if (!(bp.k.w + kp.k.w > a.fln_prec)) return false;
+  const float zeta = bp.k.y, eta = kp.k.y;
+  const float gpq = zeta + eta;
+  const float rs = rsqrtf(gpq);
+  const float oogpq = rs * rs;
+  const float pfac = bp.k.x * kp.k.x * rs;
+  if (fabsf(pfac) < a.fprecision) return false;
+  const double g64 = zb + zk;
+  double r64 = f2d_int(oogpq);
+  r64 = fma(r64, fma(-g64, r64, 1.0), r64);
+  const double X = Pb[0] - Pk[0], Y = Pb[1] - Pk[1], Z = Pb[2] - Pk[2];
+  const double T64 = (zb * zk) * r64 * fma(X, X, fma(Y, Y, Z * Z));
+  double F64[C::kMmax + 1];
+  rk_boys<C::kMmax>(a.boys_tay, T64, 1.0, F64);
+  float F[C::kMmax + 1];
+#pragma unroll
+  for (int m = 0; m <= C::kMmax; ++m) F[m] = d2f_int(F64[m]) * pfac;
+  const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
+  const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
+  const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
+              PQz = PA[2] - QC[2] + q.AC[2];
+  rk::Geo<float> g;
+  const float ez = eta * oogpq, zz = zeta * oogpq;
+  g.PAx = PA[0]; g.PAy = PA[1]; g.PAz = PA[2];
+  g.QCx = QC[0]; g.QCy = QC[1]; g.QCz = QC[2];
+  g.WPx = -ez * PQx; g.WPy = -ez * PQy; g.WPz = -ez * PQz;
+  g.WQx = zz * PQx; g.WQy = zz * PQy; g.WQz = zz * PQz;
+  g.oo2z = 0.5f * bp.k.z;
+  g.roz = ez;
+  g.oo2e = 0.5f * kp.k.z;
+  g.roe = zz;
+  g.oo2ze = 0.5f * oogpq;
+  C::template vrr<float>(F, g, acc);
+  return true;
+}
+
 template <typename T>
 __device__ __forceinline__ T rk_shfl_xor(unsigned mask, T v, int o, int width);
 template <>
@@ -304,7 +352,23 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
                                : rk_pp32(a.pprims[q.bra_pp + ib], q.bsw);
         const PrimF32 kp = rec ? rk_rec32(a.jk32 + krec.x + ik * krec.y)
                                : rk_pp32(a.pprims[q.ket_pp + ik], q.ksw);
-        kept += rk_prim<C, ATT>(a, q, bp, kp, acc) ? 1 : 0;
+        if constexpr (mode_b64(MODE)) {
+          double Pb[3], Pk[3], zb, zk;
+          if (rec) {
+            const PrimPairJK64& b64 = a.jk64[brec.x + ib * brec.y];
+            const PrimPairJK64& k64 = a.jk64[krec.x + ik * krec.y];
+            Pb[0] = b64.P[0]; Pb[1] = b64.P[1]; Pb[2] = b64.P[2]; zb = b64.zeta;
+            Pk[0] = k64.P[0]; Pk[1] = k64.P[1]; Pk[2] = k64.P[2]; zk = k64.zeta;
+          } else {
+            const PrimPairRec& b64 = a.pprims[q.bra_pp + ib];
+            const PrimPairRec& k64 = a.pprims[q.ket_pp + ik];
+            Pb[0] = b64.P[0]; Pb[1] = b64.P[1]; Pb[2] = b64.P[2]; zb = b64.zeta;
+            Pk[0] = k64.P[0]; Pk[1] = k64.P[1]; Pk[2] = k64.P[2]; zk = k64.zeta;
+          }
+          kept += rk_prim_b64<C>(a, q, bp, kp, Pb, zb, Pk, zk, acc) ? 1 : 0;
+        } else {
+          kept += rk_prim<C, ATT>(a, q, bp, kp, acc) ? 1 : 0;
+        }
       } else {
         kept += rk_prim<C, ATT>(a, q, ib, ik, acc) ? 1 : 0;
       }
@@ -323,7 +387,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
       }
     }
     if (g == 0) my_prims += (unsigned long long)kept;
-    if (MODE == kModeStore && a.is_null && g == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
+    if (mode_store(MODE) && a.is_null && g == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
     if (kept == 0) {
       if (MODE == kModeSchwarz && g == 0) a.kschwarz[outoff] = 0.0;
       continue;
@@ -337,7 +401,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
 #pragma unroll
       for (int e = 0; e < C::kNsph; ++e) mx = fmax(mx, fabs(rk_f64(v[e])));
       if (g == 0) a.kschwarz[outoff] = sqrt(mx);
-    } else if (MODE == kModeStore) {
+    } else if (mode_store(MODE)) {
       const int fl = flags >> 2;
       const bool sbk = fl & 1, stb = (fl >> 1) & 1, stk = (fl >> 2) & 1;
       int perm[4];
@@ -359,7 +423,7 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
         for (int t = 0; t < 4; ++t) it[perm[t]] = ci[t];
         o[((it[0] * tn[1] + it[1]) * tn[2] + it[2]) * tn[3] + it[3]] = rk_f64(v[e]);
       }
-    } else if (MODE == kModeJK) {
+    } else if (mode_jk(MODE)) {
       const T deg = T((q.sh[0] == q.sh[1] ? 1 : 2) * (q.sh[2] == q.sh[3] ? 1 : 2) *
                       (bpair == kpair ? 1 : 2));
       const int nbf = a.nbf;

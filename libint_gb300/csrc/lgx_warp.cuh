@@ -42,19 +42,26 @@ __device__ __forceinline__ double small_int<double>(int n) { return i2d_int(n); 
 template <>
 __device__ __forceinline__ float small_int<float>(int n) { return float(n); }
 
-// FP64 Boys F_0..F_mmax(T) * pfac into F (runtime mmax).
+// An FP64 Boys value times the prefactor, as staged: FP64, or (the mixed
+// scheme's FP32 kernels) rounded to FP32 first with integer operations.
+__device__ __forceinline__ double boys_out(double f, double pfac) { return f * pfac; }
+__device__ __forceinline__ float boys_out(double f, float pfac) { return d2f_int(f) * pfac; }
+
+// FP64 Boys F_0..F_mmax(T) * pfac into F (runtime mmax); TO = double for the
+// FP64 kernels, float for the FP32 kernels with the Boys function in FP64.
+template <typename TO>
 __device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
                                               const double* __restrict__ inv_odd, double T,
-                                              int mmax, double pfac, double* __restrict__ F) {
+                                              int mmax, TO pfac, TO* __restrict__ F) {
   if (T > kBoysTmax) {
     const double eT = exp(-T);
     const double rs = rsqrt(T);
     double f = 0.88622692545275801365 * rs;
-    F[0] = f * pfac;
+    F[0] = boys_out(f, pfac);
     const double oo2T = 0.5 * (rs * rs);
     for (int m = 0; m < mmax; ++m) {
       f = ((2 * m + 1) * f - eT) * oo2T;
-      F[m + 1] = f * pfac;
+      F[m + 1] = boys_out(f, pfac);
     }
     return;
   }
@@ -68,13 +75,13 @@ __device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
   s = fma(s, -d * (1.0 / 3.0), __ldg(row + 2));
   s = fma(s, -d * (1.0 / 2.0), __ldg(row + 1));
   s = fma(s, -d, __ldg(row + 0));
-  F[mmax] = s * pfac;
+  F[mmax] = boys_out(s, pfac);
   if (mmax > 0) {
     const double eT = exp(-T);
     const double twoT = 2.0 * T;
     for (int m = mmax - 1; m >= 0; --m) {
       s = fma(twoT, s, eT) * __ldg(inv_odd + m);
-      F[m] = s * pfac;
+      F[m] = boys_out(s, pfac);
     }
   }
 }
@@ -212,7 +219,7 @@ __device__ __forceinline__ T sel3(int d, T x, T y, T z) {
 // of T).  Returns false if screened out.
 // ATT: instantiation for the attenuated operators (a.op = erf / erfc); the
 // Coulomb instantiations carry none of that code.
-template <bool ATT>
+template <bool ATT, bool B64 = false>
 __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<double>& g, int idx,
                                          double npbraket, double* st) {
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
@@ -260,7 +267,11 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
   return true;
 }
 
-template <bool ATT>
+// B64: the mixed scheme's Boys function in FP64 (kModeJKB64 /
+// kModeStoreB64): T = rho |P - Q|^2 from the FP64 pair data, with
+// 1/(zeta + eta) the FP32 value refined by one Newton step (relative error
+// below 1e-13), and F_m(T) from the FP64 evaluator, rounded to FP32.
+template <bool ATT, bool B64 = false>
 __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<float>& g, int idx,
                                          double npbraket, float* st) {
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
@@ -281,7 +292,14 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<flo
               PQz = PA[2] - QC[2] + g.AC[2];
   const float rho = zeta * eta * oogpq;
   const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
-  if constexpr (ATT) {
+  if constexpr (B64) {
+    const double g64 = bp.zeta + kp.zeta;
+    double r64 = f2d_int(oogpq);
+    r64 = fma(r64, fma(-g64, r64, 1.0), r64);
+    const double X = bp.P[0] - kp.P[0], Y = bp.P[1] - kp.P[1], Z = bp.P[2] - kp.P[2];
+    const double T64 = (bp.zeta * kp.zeta) * r64 * fma(X, X, fma(Y, Y, Z * Z));
+    boys_to_stage(a.boys, a.inv_odd, T64, a.prog.mmax, pfac, st + kStF);
+  } else if constexpr (ATT) {
     if (a.op != 1) boys_to_stage(a.boys32, T, a.prog.mmax, pfac, st + kStF);
     attenuate<float>(a, T, rho, a.prog.mmax, pfac, st + kStF);
   } else {
@@ -438,7 +456,7 @@ __device__ __forceinline__ void vrr_consume(const DevProg& P, const T* __restric
 
 // Steps 1-2: contracted (e0|f0) accumulators in slots[0, nacc).  Returns the
 // number of primitive quartets that survived screening.
-template <typename T, bool ATT = false>
+template <typename T, bool ATT = false, bool B64 = false>
 __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __restrict__ slots,
                                 T* __restrict__ stage, int lane) {
   const DevProg& P = a.prog;
@@ -452,7 +470,8 @@ __device__ int contract_quartet(const EriArgs& a, const QuartetGeom<T>& g, T* __
     // lane r < R prepares primitive quartet base + r in its own staging row
     const int idx = base + lane;
     bool keep = false;
-    if (lane < R && idx < nq) keep = prologue<ATT>(a, g, idx, npbraket, stage + lane * kStage);
+    if (lane < R && idx < nq)
+      keep = prologue<ATT, B64>(a, g, idx, npbraket, stage + lane * kStage);
     const unsigned ballot = __ballot_sync(0xffffffffu, keep);
     __syncwarp();
     kept += __popc(ballot);
@@ -788,9 +807,10 @@ __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
       }
       QuartetGeom<T> g;
       load_geom<T>(a, bpair, kpair, flags & 1, (flags >> 1) & 1, g);
-      const int kept = contract_quartet<T, PostAtten<Post>::value>(a, g, slots, stage, lane);
+      const int kept =
+          contract_quartet<T, PostAtten<Post>::value, mode_b64(MODE)>(a, g, slots, stage, lane);
       my_prims += kept;
-      if (MODE == kModeStore && a.is_null && lane == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
+      if (mode_store(MODE) && a.is_null && lane == 0) a.is_null[orig] = kept == 0 ? 1 : 0;
       if (kept == 0) {
         if (MODE == kModeSchwarz && lane == 0) a.kschwarz[outoff] = 0.0;
         continue;
@@ -799,7 +819,7 @@ __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
       const int degi = (g.sh[0] == g.sh[1] ? 1 : 2) * (g.sh[2] == g.sh[3] ? 1 : 2) *
                        (same_pair ? 1 : 2);
       if constexpr (Post::kGenerated) {
-        static_assert(MODE == kModeJK, "generated post stages serve the J/K digestion");
+        static_assert(mode_jk(MODE), "generated post stages serve the J/K digestion");
         // (e0|f0) -> (a'b'|f0) per f column, then -> (a'b'|c'd') per a'b' column
         T* bo = slots + Post::kNacc;
         Post::template bra<T>(slots, bo, g.AB, lane);
@@ -828,7 +848,7 @@ __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
             for (int e = lane; e < nsph4; e += 32) mx = fmax(mx, fabs(to_f64(V[e])));
             mx = warp_max(mx);
             if (lane == 0) a.kschwarz[outoff] = sqrt(mx);
-          } else if (MODE == kModeJK) {
+          } else if (mode_jk(MODE)) {
             digest_jk<T>(a, g, dims, V, small_int<T>(degi), lane);
           } else if (MODE == kModeGrad) {
             double sj, sk;

@@ -83,3 +83,18 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch):
     monkeypatch.setenv("RANK", "1")
     args = bench.argparse.Namespace(workload="h2o32_cc-pvdz", steps=1, warmup=1, gpus=2)
     assert bench.run_reference(args) == 0
+
+
+def test_kernel_roofline_blends_peaks_for_fp64_boys_launch():
+    # an FP32 launch of the mixed scheme does part of its work (the Boys
+    # function and its argument) in FP64: its peak is the time at peak of
+    # both shares
+    import bench
+    launches = [{"class": (1, 0, 1, 0), "fp32": 1, "kernel": "register", "ms_avg": 10.0,
+                 "flops": 1.0e11, "flops_fp64": 1.0e9, "prim_quartets": 1, "quartets": 1}]
+    peaks = {"fp64": 1.0, "fp32": 64.0}
+    r = bench.kernel_roofline(launches, peaks, "w", "mixed")
+    t_min = 1.0e9 / 1.0e12 + 0.99e11 / 64.0e12
+    assert r["bound"] == "fp64+fp32 pipes"
+    assert abs(r["peak"] - 1.0e11 / t_min / 1e12) < 1e-12
+    assert abs(r["frac"] - (1.0e11 / 0.010 / 1e12) / r["peak"]) < 1e-12

@@ -6,9 +6,13 @@ same fixture at 1e-14).
 Bounds: FP64 evaluators 1e-14 relative (the Taylor truncation on the 1/32
 grid is below 5e-17; the register evaluator's asymptotic branch drops
 e^{-T} above T = 50, at most 1.7e-15 relative for m <= 6).  FP32 evaluators:
-|dF_m| <= 6e-8 (1 + T) F_{m+1}(T) + 1e-6 F_m(T), where the first term is the
-rounding of T to FP32 (dF_m/dT = -F_{m+1}) and the second the FP32 Taylor
-step, exponential and downward recursion."""
+|dF_m| <= 6e-8 (1 + T) F_{m+1}(T) + 8e-7 (mmax + 2) F_m(T) + 1e-44, where
+the first term is the rounding of T to FP32 (dF_m/dT = -F_{m+1}); the second
+the FP32 Taylor step, exponential and two roundings per recursion step, and
+above T = 50 the 2-ulp error of rsqrtf carried (2m + 1)-fold through the
+upward recursion; the third the FP32 denormal range (F_m below 1.2e-38 at
+large T and m).  A float32 emulation of both evaluators stays within it
+over T in [0, 2000]."""
 import numpy as np
 import pytest
 
@@ -49,7 +53,7 @@ def test_fp32_boys_within_stated_bound(gpu_ctx, oracle_mod, variant, mmax):
     T = np.concatenate([g["T"], rng.uniform(0, 50, 2000), rng.uniform(50, 1000, 300)])
     ref = _ref_dense(oracle_mod, T, mmax + 1)
     F = gpu_ctx.boys(T, mmax, variant)
-    bound = 6e-8 * (1.0 + T)[:, None] * ref[:, 1:] + 1e-6 * ref[:, :-1]
+    bound = 6e-8 * (1.0 + T)[:, None] * ref[:, 1:] + 8e-7 * (mmax + 2) * ref[:, :-1] + 1e-44
     err = np.abs(F - ref[:, :-1])
     assert np.all(err <= bound), float(np.max(err / bound))
 
@@ -62,3 +66,18 @@ def test_boys_rejects_bad_arguments(gpu_ctx, lgx):
     with pytest.raises(lgx.LgxError):
         gpu_ctx.boys(np.array([1.0]), 7, 1)  # register evaluators stop at m = 6
     assert gpu_ctx.boys(np.array([0.0]), 0, 0)[0, 0] == 1.0
+
+
+@pytest.mark.parametrize("v64,vb,mmax", [(0, 4, 16), (1, 5, 6)])
+def test_mixed_scheme_boys_is_fp64_rounded_to_fp32(gpu_ctx, v64, vb, mmax):
+    # the LGX_MIXED scheme's FP32 kernels take the FP64 evaluator's values
+    # rounded to nearest FP32 (integer-only conversion): exactly numpy's
+    # float32 rounding of the FP64 values, wherever those are FP32 normals
+    rng = np.random.default_rng(13)
+    T = np.concatenate([load("boys.npz")["T"], rng.uniform(0, 60, 4000),
+                        rng.uniform(60, 2000, 500)])
+    F64 = gpu_ctx.boys(T, mmax, v64)
+    Fb = gpu_ctx.boys(T, mmax, vb)
+    normal = np.abs(F64) >= np.finfo(np.float32).tiny
+    np.testing.assert_array_equal(Fb[normal], F64[normal].astype(np.float32).astype(np.float64))
+    assert np.all(Fb[~normal] == 0.0)

@@ -133,10 +133,11 @@ def test_config2_h2o32_fp64_jk_and_sampled_quartets(lgx, oracle_mod, h2o32):
     compare_batch(lgx, oracle_mod, ctx, ob, bs, q)
 
 
-def test_config3_h2o32_mixed_errors(lgx, oracle_mod, h2o32):
+@pytest.mark.parametrize("mode", [1, 2])  # LGX_MIXED (FP64 Boys), LGX_MIXED_FP32_BOYS
+def test_config3_h2o32_mixed_errors(lgx, oracle_mod, h2o32, mode):
     bs, ob, D, ctx, K = h2o32
     J64, K64, _ = ctx.jk(D, 1e-12)
-    Jm, Km, st = ctx.jk(D, 1e-12, mode=1, mixed_thresh=1e-4)
+    Jm, Km, st = ctx.jk(D, 1e-12, mode=mode, mixed_thresh=1e-4)
     assert st.quartets_fp32 > 5 * st.quartets_fp64 > 0
     e64, em = lgx.jk_energies(D, J64, K64), lgx.jk_energies(D, Jm, Km)
     assert abs(e64[0] - em[0]) <= 1e-8 and abs(e64[1] - em[1]) <= 1e-8
@@ -145,9 +146,9 @@ def test_config3_h2o32_mixed_errors(lgx, oracle_mod, h2o32):
     q32 = screened_sample(K, 100000, 1e-12, rng, lo=1e-12, hi=1e-4)
     q64 = screened_sample(K, 20000, 1e-4, rng)
     a, b, c, d = q32.T
-    compare_batch(lgx, oracle_mod, ctx, ob, bs, q32, mode=1,
+    compare_batch(lgx, oracle_mod, ctx, ob, bs, q32, mode=mode,
                   tol=lambda x: max(1e-12, 1e-5 * x), bound=K[a, b] * K[c, d])
-    compare_batch(lgx, oracle_mod, ctx, ob, bs, q64, mode=1)
+    compare_batch(lgx, oracle_mod, ctx, ob, bs, q64, mode=mode)
 
 
 def test_config4_tz_h2o4_fp64_and_mixed(lgx, oracle_mod):
