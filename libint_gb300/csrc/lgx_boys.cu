@@ -12,9 +12,9 @@ __device__ void rk_boys_to(int variant, const double* tay, const float* tab32, d
                            double* out) {
   if (variant == 1) {
     rk_boys<MMAX>(tay, T, 1.0, out);
-  } else if (variant == 5) {  // FP64 evaluator, rounded as rk_prim_b64 does
+  } else if (variant == 5) {  // rk_prim_b64's FP64 evaluator, rounded as it does
     double f[MMAX + 1];
-    rk_boys<MMAX>(tay, T, 1.0, f);
+    rk_boys_b64<MMAX>(tay, T, float(T), f);
 #pragma unroll
     for (int m = 0; m <= MMAX; ++m) out[m] = double(d2f_int(f[m]));
   } else {

@@ -16,11 +16,14 @@ namespace lgx {
 //   F_{m+1} = (2m+1)/(2T) F_m with the e^{-T} terms dropped; the relative
 //   error of that, the regularised upper incomplete gamma Q(m+1/2, T), is
 //   below 2e-16 for m <= 5 and 1.7e-15 for m = 6 at T = 50.
+// FP64 evaluation once the branch and the grid point are chosen: asym
+// selects the asymptotic branch; otherwise k is the grid point and md =
+// T_k - T.
 template <int MMAX>
-__device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T, double pfac,
-                                        double* F) {
+__device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, double T, bool asym,
+                                             int k, double md, double pfac, double* F) {
   static_assert(MMAX <= 6, "asymptotic branch without e^{-T} is exact to 2e-15 only for m <= 6");
-  if (T > kBoysTmax) {
+  if (asym) {
     const double rs = rsqrt(T);
     const double oo2T = 0.5 * (rs * rs);
     double f = (0.88622692545275801365 * pfac) * rs;
@@ -32,11 +35,6 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T
     }
     return;
   }
-  // nearest grid point: adding 1.5*2^52 rounds T*32 to an integer held in
-  // the low mantissa bits (read back with an integer move)
-  const double t32 = fma(T, kBoysInvDT, 6755399441055744.0);
-  const int k = __double2loint(t32);
-  const double md = fma(t32 - 6755399441055744.0, kBoysDT, -T);  // = -(T - T_k)
   const double* row = tay + (k * (kBoysMaxM + 1)) * kBoysTaylorStride;
   if (MMAX <= 2) {
 #pragma unroll
@@ -69,6 +67,34 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T
       F[m] = s;
     }
   }
+}
+
+template <int MMAX>
+__device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T, double pfac,
+                                        double* F) {
+  // nearest grid point: adding 1.5*2^52 rounds T*32 to an integer held in
+  // the low mantissa bits (read back with an integer move)
+  const double t32 = fma(T, kBoysInvDT, 6755399441055744.0);
+  const int k = __double2loint(t32);
+  const double md = fma(t32 - 6755399441055744.0, kBoysDT, -T);  // = -(T - T_k)
+  rk_boys_core<MMAX>(tay, T, T > kBoysTmax, k, md, pfac, F);
+}
+
+// The mixed scheme's FP64 Boys function of an FP32 quartet, given the FP64
+// argument T and its FP32 value Tf (which the FP32 prologue has): the branch
+// and the grid point come from Tf (integer and FP32 operations), only the
+// offset md = T_k - T in FP64.  Tf and T differ by ~1e-6 relative at most,
+// so the grid point may be the neighbour of T's nearest one (|md| <= 1/64 +
+// 3e-5: Taylor remainder still below 5e-17), and near T = 50 either branch
+// is exact (the asymptotic one drops Q(m+1/2, T) < 2e-15); Tf <= 50 gives
+// k <= 1600 < kBoysRows.
+template <int MMAX>
+__device__ __forceinline__ void rk_boys_b64(const double* __restrict__ tay, double T, float Tf,
+                                            double* F) {
+  const bool asym = Tf > float(kBoysTmax);
+  const int k = asym ? 0 : __float2int_rn(Tf * float(kBoysInvDT));
+  const double md = fma(i2d_int(k), kBoysDT, -T);
+  rk_boys_core<MMAX>(tay, T, asym, k, md, 1.0, F);
 }
 
 template <int MMAX>

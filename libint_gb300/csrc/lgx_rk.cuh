@@ -216,10 +216,12 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
 // (the kModeJKB64 / kModeStoreB64 kernels of the mixed scheme).  The
 // screening, prefactor and VRR geometry are the FP32 ones of rk_prim above;
 // T = rho |P - Q|^2 is formed in FP64 from the pairs' FP64 centres and
-// exponent sums (1/(zeta + eta) is the FP32 value refined by one Newton
-// step, relative error below 1e-13), F_m(T) comes from the FP64 evaluator
-// (Taylor with the downward recursion and e^{-T}, or the asymptotic branch)
-// and is rounded to FP32 with integer operations before the FP32 pfac.
+// exponent sums, with rho = zeta eta / (zeta + eta) the FP32 value refined by
+// one Newton step on (zeta + eta) rho - zeta eta = 0 (relative error below
+// 1e-13); F_m(T) comes from the FP64 evaluator (Taylor with the downward
+// recursion and e^{-T}, or the asymptotic branch; the branch and grid point
+// from the FP32 T, rk_boys_b64) and is rounded to FP32 with integer
+// operations before the FP32 pfac.
 template <class C>
 __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<float>& q,
                                             const PrimF32& bp, const PrimF32& kp, const double* Pb,
@@ -231,20 +233,21 @@ __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<fl
   const float oogpq = rs * rs;
   const float pfac = bp.k.x * kp.k.x * rs;
   if (fabsf(pfac) < a.fprecision) return false;
-  const double g64 = zb + zk;
-  double r64 = f2d_int(oogpq);
-  r64 = fma(r64, fma(-g64, r64, 1.0), r64);
-  const double X = Pb[0] - Pk[0], Y = Pb[1] - Pk[1], Z = Pb[2] - Pk[2];
-  const double T64 = (zb * zk) * r64 * fma(X, X, fma(Y, Y, Z * Z));
-  double F64[C::kMmax + 1];
-  rk_boys<C::kMmax>(a.boys_tay, T64, 1.0, F64);
-  float F[C::kMmax + 1];
-#pragma unroll
-  for (int m = 0; m <= C::kMmax; ++m) F[m] = d2f_int(F64[m]) * pfac;
   const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
   const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
               PQz = PA[2] - QC[2] + q.AC[2];
+  const float rho = zeta * eta * oogpq;
+  const float Tf = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
+  const double r0 = f2d_int(rho);
+  const double rho64 = fma(-fma(zb + zk, r0, -(zb * zk)), f2d_int(oogpq), r0);
+  const double X = Pb[0] - Pk[0], Y = Pb[1] - Pk[1], Z = Pb[2] - Pk[2];
+  const double T64 = rho64 * fma(X, X, fma(Y, Y, Z * Z));
+  double F64[C::kMmax + 1];
+  rk_boys_b64<C::kMmax>(a.boys_tay, T64, Tf, F64);
+  float F[C::kMmax + 1];
+#pragma unroll
+  for (int m = 0; m <= C::kMmax; ++m) F[m] = d2f_int(F64[m]) * pfac;
   rk::Geo<float> g;
   const float ez = eta * oogpq, zz = zeta * oogpq;
   g.PAx = PA[0]; g.PAy = PA[1]; g.PAz = PA[2];

@@ -70,14 +70,23 @@ def test_boys_rejects_bad_arguments(gpu_ctx, lgx):
 
 @pytest.mark.parametrize("v64,vb,mmax", [(0, 4, 16), (1, 5, 6)])
 def test_mixed_scheme_boys_is_fp64_rounded_to_fp32(gpu_ctx, v64, vb, mmax):
-    # the LGX_MIXED scheme's FP32 kernels take the FP64 evaluator's values
-    # rounded to nearest FP32 (integer-only conversion): exactly numpy's
-    # float32 rounding of the FP64 values, wherever those are FP32 normals
+    # the LGX_MIXED scheme's FP32 kernels take FP64 Boys values rounded to
+    # nearest FP32 (integer-only conversion).  The program kernels' values
+    # are exactly numpy's float32 rounding of the FP64 evaluator's (wherever
+    # those are FP32 normals); the register kernels pick the Taylor grid
+    # point from the FP32 argument, so their FP64 value may differ in the
+    # last FP64 bits and, rarely, round to the neighbouring float32
     rng = np.random.default_rng(13)
     T = np.concatenate([load("boys.npz")["T"], rng.uniform(0, 60, 4000),
                         rng.uniform(60, 2000, 500)])
     F64 = gpu_ctx.boys(T, mmax, v64)
     Fb = gpu_ctx.boys(T, mmax, vb)
     normal = np.abs(F64) >= np.finfo(np.float32).tiny
-    np.testing.assert_array_equal(Fb[normal], F64[normal].astype(np.float32).astype(np.float64))
-    assert np.all(Fb[~normal] == 0.0)
+    want = F64[normal].astype(np.float32)
+    got = Fb[normal].astype(np.float32)
+    if vb == 4:
+        np.testing.assert_array_equal(got, want)
+    else:
+        ulps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+        assert ulps.max() <= 1 and np.mean(ulps == 0) > 0.999, (ulps.max(), np.mean(ulps == 0))
+    assert np.all(Fb[~normal & (np.abs(F64) < 0.5 * np.finfo(np.float32).tiny)] == 0.0)
