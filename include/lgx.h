@@ -276,6 +276,18 @@ lgx_status lgx_jk_device(lgx_context* ctx, const double* dD, double* dJ,
                          double* dK, double schwarz_thresh, int mode,
                          double mixed_thresh, lgx_jk_stats* stats);
 
+/* Density-weighted screening of every later J/K pass on the context (lgx_jk,
+ * lgx_jk_device, lgx_jk_device_noalloc), as compute_2body_fock does it
+ * (tests/hartree-fock/hartree-fock++.cc:1581-1684): with Dnorm1234 the
+ * largest infinity norm of the six shell blocks of D that a quartet touches
+ * (compute_shellblock_norm, :939-957), a quartet that passed the Schwarz
+ * test is skipped when Dnorm1234 * K12 * K34 < precision, and the others
+ * have their primitives screened at precision / Dnorm1234 instead of the
+ * machine epsilon (Engine::set_precision per shell set), never below the
+ * epsilon the primitive-pair data are built with.  precision = 0 (the
+ * default) turns it off; the gradient pass does not use it. */
+lgx_status lgx_set_fock_precision(lgx_context* ctx, double precision);
+
 /* No counterpart in the reference.  lgx_jk_device for callers that must not
  * allocate device memory while they run: code inside a region where
  * cudaMalloc is not allowed or would stall (for example while another

@@ -78,6 +78,11 @@ class JKBuilder {
       throw std::invalid_argument("JKBuilder::set_operator: unsupported operator");
     check(lgx_set_operator(ctx_, opc, omega));
   }
+  /// Density-weighted screening of later J/K builds, as compute_2body_fock's
+  /// `precision` argument (hartree-fock++.cc:1640-1684): quartets with
+  /// max shell-block |D| * K12 * K34 below `precision` are skipped and the
+  /// others' primitives screened at precision / max |D|; 0 turns it off.
+  void set_fock_precision(double precision) { check(lgx_set_fock_precision(ctx_, precision)); }
 
  private:
   lgx_context* ctx_ = nullptr;

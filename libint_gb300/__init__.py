@@ -321,6 +321,14 @@ class Context:
                                        _lgx.ptr(F)), "lgx_boys")
         return F
 
+    def set_fock_precision(self, precision: float = 0.0):
+        """Density-weighted screening of later J/K passes (lgx_set_fock_precision):
+        skip quartets with Dnorm1234 K12 K34 < precision and screen the
+        primitives of the rest at precision / Dnorm1234, as the reference's
+        compute_2body_fock does; 0 turns it off."""
+        self._check(self._lib.lgx_set_fock_precision(self._h, float(precision)),
+                    "lgx_set_fock_precision")
+
     def set_watchdog(self, max_chunks: int = -1):
         """Bound on the work chunks a program-kernel warp may take per launch
         before the call fails with LGX_ERR_WATCHDOG (lgx_set_watchdog);

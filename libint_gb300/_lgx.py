@@ -90,6 +90,7 @@ SIGNATURES = {
     "lgx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "lgx_set_operator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
     "lgx_set_watchdog": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    "lgx_set_fock_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "lgx_boys": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int64, ctypes.c_int,
                                 _dp]),
     "lgx_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),

@@ -30,6 +30,8 @@ cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J
 size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
+cudaError_t launch_shell_block_norm(const DevBasis& b, const double* D, int nbf, double* out,
+                                    cudaStream_t st);
 cudaError_t launch_boys_eval(const double* tab, const double* tay, const float* tab32,
                              const double* inv_odd, int variant, const double* T, long long n,
                              int mmax, double* F, cudaStream_t st);
@@ -105,6 +107,7 @@ struct BasisDev {
   int pairs_method = -1;
   // Schwarz
   std::vector<double> Kpair;  // per pair index
+  DBuf Kd;                    // Kpair on the device
   bool schwarz_ok = false;
   bool std_pure = true;  // every shell has pure == (l >= 2)
   double avg_npp = 1;    // mean primitive pairs per shell pair
@@ -241,6 +244,10 @@ struct lgx_context {
   // per pair index, empty: every pair) and a version bumped on each change
   std::vector<unsigned char> pair_subset;
   unsigned long long subset_version = 0;
+  // density-weighted screening of the J/K passes (lgx_set_fock_precision):
+  // Fock precision (0: off) and the shell-block norms of D it uses
+  double fock_prec = 0.0;
+  DBuf Dsh;
   // two-body operator of every pass (lgx_set_operator): LGX_OP_* and omega
   int op = LGX_OP_COULOMB;
   double omega = 0.0;
@@ -1064,13 +1071,13 @@ lgx_status ensure_schwarz(lgx_context* ctx, BasisDev& B) {
     q[4 * p + 2] = B.hpairs[p].s1;
     q[4 * p + 3] = B.hpairs[p].s2;
   }
-  DBuf dK;
-  CK(dK.ensure(npairs * sizeof(double)));
+  // kept on the device too: the density-weighted J/K screening reads it
+  CK(B.Kd.ensure(npairs * sizeof(double)));
   s = run_explicit(ctx, B, q.data(), npairs, 0, kModeSchwarz, 0.0, nullptr, nullptr, nullptr,
-                   0.0, 0, dK.as<double>());
+                   0.0, 0, B.Kd.as<double>());
   if (s != LGX_OK) return s;
   B.Kpair.resize(npairs);
-  CK(cudaMemcpyAsync(B.Kpair.data(), dK.p, npairs * sizeof(double), cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(B.Kpair.data(), B.Kd.p, npairs * sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   s = check_errflag(ctx);
@@ -2410,6 +2417,8 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
   CK(ctx->Jacc.ensure(nn * sizeof(double)));
   CK(ctx->Kacc.ensure(nn * sizeof(double)));
   if (mixedp) CK(ctx->Df.ensure(nn * sizeof(float)));
+  const bool dscreen = ctx->fock_prec > 0.0;
+  if (dscreen) CK(ctx->Dsh.ensure(size_t(B.nshell) * B.nshell * sizeof(double)));
   EriArgs a{};
   a.precision = eps;
   a.ln_prec = std::log(eps);
@@ -2419,7 +2428,14 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
   a.Jacc = ctx->Jacc.as<double>();
   a.Kacc = ctx->Kacc.as<double>();
   a.nbf = B.nbf;
+  if (dscreen) {
+    a.dsh = ctx->Dsh.as<double>();
+    a.kpair = B.Kd.as<double>();
+    a.fock_prec = ctx->fock_prec;
+    a.ln_fock = std::log(ctx->fock_prec);
+  }
   if (mixedp) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
+  if (dscreen) CK(launch_shell_block_norm(B.dev, dD, B.nbf, ctx->Dsh.as<double>(), ctx->stream));
   s = tune_bins(ctx, B, kModeJK, 0, mode32, a);
   if (s != LGX_OK) return s;
   // the pass: zero the accumulators, FP32 copy of D, every class bin, J/K
@@ -2427,6 +2443,7 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
     CK(cudaMemsetAsync(ctx->Jacc.p, 0, nn * sizeof(double), ctx->stream));
     CK(cudaMemsetAsync(ctx->Kacc.p, 0, nn * sizeof(double), ctx->stream));
     if (mixedp) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
+    if (dscreen) CK(launch_shell_block_norm(B.dev, dD, B.nbf, ctx->Dsh.as<double>(), ctx->stream));
     lgx_status r = enqueue_bins(ctx, B, kModeJK, 0, mode32, a, pr);
     if (r != LGX_OK) return r;
     CK(launch_jk_finalize(ctx->Jacc.as<double>(), ctx->Kacc.as<double>(), dJ, dK, B.nbf,
@@ -2567,6 +2584,11 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
     return fail(ctx, LGX_ERR_INVALID_ARG,
                 "lgx_jk_device_noalloc: basis state not prepared for these settings; call "
                 "lgx_jk_device (or lgx_jk) once with the same threshold and mode first");
+  const bool dscreen = ctx->fock_prec > 0.0;
+  if (dscreen && ctx->Dsh.n < size_t(B.nshell) * B.nshell * sizeof(double))
+    return fail(ctx, LGX_ERR_INVALID_ARG,
+                "lgx_jk_device_noalloc: density screening not prepared; call lgx_jk_device "
+                "once with the same settings first");
   CK(cudaSetDevice(ctx->device));
   unsigned char* scratch = nullptr;
   lgx_status s = noalloc_scratch(ctx, &scratch);
@@ -2599,6 +2621,13 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
   a.Jacc = Jacc;
   a.Kacc = Kacc;
   a.nbf = B.nbf;
+  if (dscreen) {
+    a.dsh = ctx->Dsh.as<double>();
+    a.kpair = B.Kd.as<double>();
+    a.fock_prec = ctx->fock_prec;
+    a.ln_fock = std::log(ctx->fock_prec);
+    CK(launch_shell_block_norm(B.dev, dD, B.nbf, ctx->Dsh.as<double>(), ctx->stream));
+  }
   s = run_bins(ctx, B, kModeJK, 0, mode32, a, stats);
   if (s != LGX_OK) return s;
   CK(launch_jk_finalize(Jacc, Kacc, dJ, dK, B.nbf, ctx->stream));
@@ -2678,6 +2707,17 @@ lgx_status lgx_boys(lgx_context* ctx, int variant, const double* T, int64_t n, i
                       ctx->boysF.as<double>(), ctx->stream));
   CK(cudaMemcpyAsync(F, ctx->boysF.p, nf * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_set_fock_precision(lgx_context* ctx, double precision) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!(precision >= 0.0) || !std::isfinite(precision))
+    return fail(ctx, LGX_ERR_INVALID_ARG, "Fock precision must be finite and >= 0");
+  if (precision == ctx->fock_prec) return LGX_OK;
+  ctx->fock_prec = precision;
+  ++ctx->version;  // a launch argument of the captured pass
   return LGX_OK;
 }
 

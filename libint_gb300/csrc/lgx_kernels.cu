@@ -110,6 +110,33 @@ cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n
   return cudaGetLastError();
 }
 
+// Infinity norms of the shell blocks of D (compute_shellblock_norm,
+// tests/hartree-fock/hartree-fock++.cc:939-957): out[s1 * ns + s2] =
+// max |D(i, j)| over the functions i of shell s1 and j of shell s2.
+__global__ void shell_block_norm_kernel(DevBasis b, const double* __restrict__ D, int nbf,
+                                        double* __restrict__ out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int ns = b.nshell;
+  if (t >= (long long)ns * ns) return;
+  const int s1 = int(t / ns), s2 = int(t - (long long)s1 * ns);
+  const int o1 = b.bf_off[s1], o2 = b.bf_off[s2];
+  const int n1 = b.pure[s1] ? 2 * b.l[s1] + 1 : ncart_of(b.l[s1]);
+  const int n2 = b.pure[s2] ? 2 * b.l[s2] + 1 : ncart_of(b.l[s2]);
+  double m = 0.0;
+  for (int i = 0; i < n1; ++i)
+    for (int j = 0; j < n2; ++j) m = fmax(m, fabs(D[(size_t)(o1 + i) * nbf + o2 + j]));
+  out[t] = m;
+}
+
+cudaError_t launch_shell_block_norm(const DevBasis& b, const double* D, int nbf, double* out,
+                                    cudaStream_t st) {
+  const long long n = (long long)b.nshell * b.nshell;
+  if (n == 0) return cudaSuccess;
+  const int block = 256;
+  shell_block_norm_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(b, D, nbf, out);
+  return cudaGetLastError();
+}
+
 // J = (Jacc + Jacc^T)/4, K = (Kacc + Kacc^T)/8 (hartree-fock++.cc:1766 with
 // the G = 2J - K split).
 __global__ void jk_finalize_kernel(const double* Jacc, const double* Kacc, double* J, double* K,

@@ -148,11 +148,55 @@ struct EriArgs {
   double* gJ;
   double* gK;
   int nbf;
+  // density-weighted screening of the J/K passes (fock_prec > 0): shell-
+  // block infinity norms of D (nshell x nshell), Schwarz factor per pair,
+  // ln(fock_prec)
+  const double* dsh;
+  const double* kpair;
+  double fock_prec;
+  double ln_fock;
   // watchdog: a bounded number of work chunks per warp
   long long max_chunks;
   int* error_flag;
   // statistics: primitive quartets computed (one atomic per thread)
   unsigned long long* prim_count;
 };
+
+// Primitive-screening thresholds of one shell quartet (Engine::set_precision:
+// precision and its logarithm, with FP32 copies).
+struct PrimScreen {
+  double prec, ln_prec;
+  float fprec, fln_prec;
+};
+
+// The thresholds of the pass, or with density-weighted screening
+// (EriArgs::fock_prec > 0) those of compute_2body_fock
+// (tests/hartree-fock/hartree-fock++.cc:1640-1684): Dnorm1234 = the largest
+// infinity norm of the six shell blocks of D the quartet touches; the quartet
+// is skipped when Dnorm1234 K12 K34 < fock_prec (returns false), else its
+// primitives are screened at fock_prec / Dnorm1234 (FP32 quotient and
+// logarithm; not below the precision the pair data were built with).
+__device__ __forceinline__ bool quartet_screen(const EriArgs& a, const int* sh, int bpair,
+                                               int kpair, PrimScreen& s) {
+  s.prec = a.precision;
+  s.ln_prec = a.ln_prec;
+  s.fprec = a.fprecision;
+  s.fln_prec = a.fln_prec;
+  if (!(a.fock_prec > 0.0)) return true;
+  const int ns = a.basis.nshell;
+  const double* d = a.dsh;
+  const double dn = fmax(fmax(fmax(d[sh[0] * ns + sh[1]], d[sh[0] * ns + sh[2]]),
+                              fmax(d[sh[1] * ns + sh[2]], d[sh[0] * ns + sh[3]])),
+                         fmax(d[sh[1] * ns + sh[3]], d[sh[2] * ns + sh[3]]));
+  if (dn * __ldg(a.kpair + bpair) * __ldg(a.kpair + kpair) < a.fock_prec) return false;
+  const float q = float(a.fock_prec) / float(dn);
+  if (q > s.fprec) {
+    s.fprec = q;
+    s.prec = f2d_int(q);
+    s.fln_prec = float(a.ln_fock) - __logf(float(dn));
+    s.ln_prec = f2d_int(s.fln_prec);
+  }
+  return true;
+}
 
 }  // namespace lgx

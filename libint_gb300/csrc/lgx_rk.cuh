@@ -121,15 +121,15 @@ __device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, 
 // the IEEE bit patterns, so neither costs an FP64 instruction.
 template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double>& q, int ib,
-                                        int ik, double* acc) {
+                                        int ik, const PrimScreen& scr, double* acc) {
   const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
-  if (!(bp.fln_scr + kp.fln_scr > a.fln_prec)) return false;
+  if (!(bp.fln_scr + kp.fln_scr > scr.fln_prec)) return false;
   const double zeta = bp.zeta, eta = kp.zeta;
   const double gpq = zeta + eta;
   const double rs = rsqrt(gpq);
   const double pfac = bp.Kc * kp.Kc * rs;
-  if ((__double_as_longlong(pfac) & 0x7fffffffffffffffll) < __double_as_longlong(a.precision))
+  if ((__double_as_longlong(pfac) & 0x7fffffffffffffffll) < __double_as_longlong(scr.prec))
     return false;
   const double oogpq = rs * rs;
   const double PQx = bp.P[0] - kp.P[0], PQy = bp.P[1] - kp.P[1], PQz = bp.P[2] - kp.P[2];
@@ -180,14 +180,15 @@ __device__ __forceinline__ PrimF32 rk_pp32(const PrimPairRec& r, bool sw) {
 // One primitive quartet into acc (FP32).  AC = A - C of the quartet.
 template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>& q,
-                                        const PrimF32& bp, const PrimF32& kp, float* acc) {
-  if (!(bp.k.w + kp.k.w > a.fln_prec)) return false;
+                                        const PrimF32& bp, const PrimF32& kp,
+                                        const PrimScreen& scr, float* acc) {
+  if (!(bp.k.w + kp.k.w > scr.fln_prec)) return false;
   const float zeta = bp.k.y, eta = kp.k.y;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
   const float pfac = bp.k.x * kp.k.x * rs;
-  if (fabsf(pfac) < a.fprecision) return false;
+  if (fabsf(pfac) < scr.fprec) return false;
   const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
   const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
@@ -225,14 +226,15 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
 template <class C>
 __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<float>& q,
                                             const PrimF32& bp, const PrimF32& kp, const double* Pb,
-                                            double zb, const double* Pk, double zk, float* acc) {
-  if (!(bp.k.w + kp.k.w > a.fln_prec)) return false;
+                                            double zb, const double* Pk, double zk,
+                                            const PrimScreen& scr, float* acc) {
+  if (!(bp.k.w + kp.k.w > scr.fln_prec)) return false;
   const float zeta = bp.k.y, eta = kp.k.y;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
   const float pfac = bp.k.x * kp.k.x * rs;
-  if (fabsf(pfac) < a.fprecision) return false;
+  if (fabsf(pfac) < scr.fprec) return false;
   const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
   const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
@@ -339,6 +341,10 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
     }
     RkQuartet<T> q;
     rk_load<T>(a, bpair, kpair, flags & 1, (flags >> 1) & 1, q);
+    // the G lanes of a quartet agree, so a skipped quartet leaves the group
+    // together
+    PrimScreen scr;
+    if (!quartet_screen(a, q.sh, bpair, kpair, scr) && mode_jk(MODE)) continue;
     T acc[C::kNacc];
 #pragma unroll
     for (int i = 0; i < C::kNacc; ++i) acc[i] = T(0);
@@ -368,12 +374,12 @@ __global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
             Pb[0] = b64.P[0]; Pb[1] = b64.P[1]; Pb[2] = b64.P[2]; zb = b64.zeta;
             Pk[0] = k64.P[0]; Pk[1] = k64.P[1]; Pk[2] = k64.P[2]; zk = k64.zeta;
           }
-          kept += rk_prim_b64<C>(a, q, bp, kp, Pb, zb, Pk, zk, acc) ? 1 : 0;
+          kept += rk_prim_b64<C>(a, q, bp, kp, Pb, zb, Pk, zk, scr, acc) ? 1 : 0;
         } else {
-          kept += rk_prim<C, ATT>(a, q, bp, kp, acc) ? 1 : 0;
+          kept += rk_prim<C, ATT>(a, q, bp, kp, scr, acc) ? 1 : 0;
         }
       } else {
-        kept += rk_prim<C, ATT>(a, q, ib, ik, acc) ? 1 : 0;
+        kept += rk_prim<C, ATT>(a, q, ib, ik, scr, acc) ? 1 : 0;
       }
       ib += gb;
       ik += gk;

@@ -168,6 +168,7 @@ struct QuartetGeom {
   bool bra_sw, ket_sw;
   T A[3], C[3];  // FP64 kernels: absolute centres of bra1 / ket1
   T AB[3], CD[3], AC[3];
+  PrimScreen scr;  // primitive-screening thresholds of the quartet
 };
 
 template <typename T>
@@ -185,6 +186,10 @@ __device__ __forceinline__ void load_geom(const EriArgs& a, int bpair, int kpair
   g.nkpp = kp.npp;
   g.bra_sw = bsw;
   g.ket_sw = ksw;
+  g.scr.prec = a.precision;
+  g.scr.ln_prec = a.ln_prec;
+  g.scr.fprec = a.fprecision;
+  g.scr.fln_prec = a.fln_prec;
   if constexpr (sizeof(T) == 8) {
     for (int x = 0; x < 3; ++x) {
       const double A = a.basis.O[3 * g.sh[0] + x], B = a.basis.O[3 * g.sh[1] + x];
@@ -225,7 +230,7 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
   const PrimPairRec& bp = a.pprims[g.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[g.ket_pp + ik];
-  if (!(bp.ln_scr + kp.ln_scr > a.ln_prec)) return false;
+  if (!(bp.ln_scr + kp.ln_scr > g.scr.ln_prec)) return false;
   const double zeta = bp.zeta, eta = kp.zeta;
   const double gpq = zeta + eta;
   const double rs = rsqrt(gpq);
@@ -233,7 +238,7 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
   const double pfac = bp.Kc * kp.Kc * rs;
   double mag = fabs(pfac);
   if (a.screening == 1) mag *= fmax(1.0, double(bp.fnonsph) * double(kp.fnonsph)) * npbraket;
-  if (mag < a.precision) return false;
+  if (mag < g.scr.prec) return false;
   const double PQx = bp.P[0] - kp.P[0], PQy = bp.P[1] - kp.P[1], PQz = bp.P[2] - kp.P[2];
   const double rho = zeta * eta * oogpq;
   const double T = rho * fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
@@ -277,7 +282,7 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<flo
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
   const PrimPairRec& bp = a.pprims[g.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[g.ket_pp + ik];
-  if (!(bp.fln_scr + kp.fln_scr > a.fln_prec)) return false;
+  if (!(bp.fln_scr + kp.fln_scr > g.scr.fln_prec)) return false;
   const float zeta = bp.fzeta, eta = kp.fzeta;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
@@ -285,7 +290,7 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<flo
   const float pfac = bp.fKc * kp.fKc * rs;
   float mag = fabsf(pfac);
   if (a.screening == 1) mag *= fmaxf(1.0f, bp.fnonsph * kp.fnonsph) * float(npbraket);
-  if (mag < a.fprecision) return false;
+  if (mag < g.scr.fprec) return false;
   const float* PA = g.bra_sw ? bp.fPA2 : bp.fPA1;
   const float* QC = g.ket_sw ? kp.fPA2 : kp.fPA1;
   const float PQx = PA[0] - QC[0] + g.AC[0], PQy = PA[1] - QC[1] + g.AC[1],
@@ -807,6 +812,7 @@ __global__ void __launch_bounds__(128) eri_warp_kernel(EriArgs a) {
       }
       QuartetGeom<T> g;
       load_geom<T>(a, bpair, kpair, flags & 1, (flags >> 1) & 1, g);
+      if (mode_jk(MODE) && !quartet_screen(a, g.sh, bpair, kpair, g.scr)) continue;
       const int kept =
           contract_quartet<T, PostAtten<Post>::value, mode_b64(MODE)>(a, g, slots, stage, lane);
       my_prims += kept;

@@ -992,15 +992,37 @@ void orc_jk_acc_destroy(orc_jk_acc* a) { delete a; }
 // flag per canonical pair index, or NULL for every pair) restricts the
 // kets: with the bra list and the mask holding the same pairs, each
 // unordered quartet of that pair subset is digested exactly once.
+// fock_precision > 0 adds compute_2body_fock's density-weighted screening
+// (quartet skipped when Dnorm1234 K12 K34 < fock_precision, primitives
+// screened at fock_precision / Dnorm1234, not below the machine epsilon).
 int64_t orc_jk_acc_pairs(orc_jk_acc* acc, const orc_basis* bs, const int* bf_off,
                          const double* Ks, double thresh, const double* D,
                          const int64_t* pairs, int64_t npairs, const unsigned char* ket_mask,
-                         int64_t* n_integrals) {
+                         double fock_precision, int64_t* n_integrals) {
   if (!acc || !bs || npairs < 0) return -1;
   const int ns = bs->nshell;
   const int nbf = acc->nbf;
   int64_t nq = 0, nint = 0;
   const double eps = std::numeric_limits<double>::epsilon();
+  // density-weighted screening (compute_2body_fock, hartree-fock++.cc:
+  // 1640-1684): shell-block infinity norms of D
+  std::vector<double> Dsh;
+  if (fock_precision > 0) {
+    Dsh.assign(size_t(ns) * ns, 0.0);
+    std::vector<int> off(ns);
+    for (int s = 0, o = 0; s < ns; ++s) {
+      off[s] = o;
+      o += nfunc(bs, s);
+    }
+    for (int a = 0; a < ns; ++a)
+      for (int b = 0; b < ns; ++b) {
+        double m = 0;
+        for (int i = 0; i < nfunc(bs, a); ++i)
+          for (int j = 0; j < nfunc(bs, b); ++j)
+            m = std::max(m, std::abs(D[size_t(off[a] + i) * nbf + off[b] + j]));
+        Dsh[size_t(a) * ns + b] = m;
+      }
+  }
 #pragma omp parallel num_threads(acc->nt) reduction(+ : nq, nint)
   {
 #ifdef _OPENMP
@@ -1022,11 +1044,19 @@ int64_t orc_jk_acc_pairs(orc_jk_acc* acc, const orc_basis* bs, const int* bf_off
         for (int s4 = 0; s4 <= s4max; ++s4) {
           if (K12 * Ks[size_t(s3) * ns + s4] < thresh) continue;
           if (ket_mask && !ket_mask[int64_t(s3) * (s3 + 1) / 2 + s4]) continue;
+          double prec = eps;
+          if (fock_precision > 0) {
+            auto dn = [&](int x, int y) { return Dsh[size_t(x) * ns + y]; };
+            const double d = std::max({dn(s1, s2), dn(s1, s3), dn(s2, s3), dn(s1, s4), dn(s2, s4),
+                                       dn(s3, s4)});
+            if (d * K12 * Ks[size_t(s3) * ns + s4] < fock_precision) continue;
+            prec = std::max(eps, fock_precision / d);
+          }
           const int n1 = nfunc(bs, s1), n2 = nfunc(bs, s2), n3 = nfunc(bs, s3),
                     n4 = nfunc(bs, s4);
           buf.resize(size_t(n1) * n2 * n3 * n4);
           const int tgt[4] = {s1, s2, s3, s4};
-          const int nv = compute_quartet(bs, tgt, 0, eps, 0, w, buf.data());
+          const int nv = compute_quartet(bs, tgt, 0, prec, 0, w, buf.data());
           ++nq;
           nint += int64_t(n1) * n2 * n3 * n4;
           if (nv == 0) continue;
@@ -1079,7 +1109,7 @@ int64_t orc_jk_sample(const orc_basis* bs, const int* bf_off, int nbf,
   orc_jk_acc* acc = orc_jk_acc_create(nbf, nthreads);
   if (!acc) return -1;
   const int64_t nq = orc_jk_acc_pairs(acc, bs, bf_off, Ks, thresh, D, pairs.data(),
-                                      int64_t(pairs.size()), nullptr, n_integrals);
+                                      int64_t(pairs.size()), nullptr, 0.0, n_integrals);
   orc_jk_acc_reduce(acc, J, K);
   orc_jk_acc_destroy(acc);
   return nq;

@@ -89,14 +89,16 @@ int64_t orc_jk(const orc_basis* bs, const int* bf_off, int nbf,
 // shell pairs (canonical pair indices s1 (s1+1)/2 + s2, s2 <= s1; returns
 // the computed quartets and their integral count), reduce into J/K (adds
 // the symmetrised sums), destroy.  ket_mask: NULL, or one flag per pair
-// index restricting the ket pairs.
+// index restricting the ket pairs; fock_precision > 0: compute_2body_fock's
+// density-weighted screening (hartree-fock++.cc:1640-1684), 0: off.
 typedef struct orc_jk_acc orc_jk_acc;
 orc_jk_acc* orc_jk_acc_create(int nbf, int nthreads);
 void orc_jk_acc_destroy(orc_jk_acc* acc);
 int64_t orc_jk_acc_pairs(orc_jk_acc* acc, const orc_basis* bs, const int* bf_off,
                          const double* Kschwarz, double schwarz_thresh, const double* D,
                          const int64_t* bra_pairs, int64_t n_bra_pairs,
-                         const unsigned char* ket_mask, int64_t* n_integrals);
+                         const unsigned char* ket_mask, double fock_precision,
+                         int64_t* n_integrals);
 void orc_jk_acc_reduce(const orc_jk_acc* acc, double* J, double* K);
 
 // Counts of the screened pass: unique quartets with K12 K34 >= thresh and

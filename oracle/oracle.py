@@ -251,7 +251,8 @@ class JKAccumulator:
         lib.orc_jk_acc_pairs.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Basis), _ip, _dp,
                                          ctypes.c_double, _dp,
                                          ctypes.POINTER(ctypes.c_int64), ctypes.c_int64,
-                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+                                         ctypes.c_void_p, ctypes.c_double,
+                                         ctypes.POINTER(ctypes.c_int64)]
         lib.orc_jk_acc_reduce.argtypes = [ctypes.c_void_p, _dp, _dp]
         self._lib = lib
         self.nbf = int(nbf)
@@ -259,11 +260,13 @@ class JKAccumulator:
         if not self._h:
             raise ValueError("orc_jk_acc_create failed")
 
-    def add_pairs(self, basis: OracleBasis, D, Kschwarz, thresh, pairs, ket_subset=False):
+    def add_pairs(self, basis: OracleBasis, D, Kschwarz, thresh, pairs, ket_subset=False,
+                  fock_precision=0.0):
         """Adds the quartets of bra pairs `pairs` (canonical pair indices
         s1 (s1 + 1) / 2 + s2, s2 <= s1) with every ket pair up to the bra, or
         with `ket_subset` only the kets among `pairs` (each unordered quartet
-        of the subset once); returns (n_quartets, n_integrals)."""
+        of the subset once), with compute_2body_fock's density-weighted
+        screening when fock_precision > 0; returns (n_quartets, n_integrals)."""
         D = np.ascontiguousarray(D, np.float64)
         Ks = np.ascontiguousarray(Kschwarz, np.float64)
         p = np.ascontiguousarray(pairs, np.int64)
@@ -278,7 +281,7 @@ class JKAccumulator:
                                         _ptr(Ks, ctypes.c_double), ctypes.c_double(thresh),
                                         _ptr(D, ctypes.c_double), _ptr(p, ctypes.c_int64),
                                         len(p), None if mask is None else mask.ctypes.data,
-                                        ctypes.byref(nint))
+                                        ctypes.c_double(fock_precision), ctypes.byref(nint))
         if nq < 0:
             raise ValueError("orc_jk_acc_pairs: bad arguments")
         return int(nq), int(nint.value)

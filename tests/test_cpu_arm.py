@@ -149,3 +149,62 @@ def test_reference_arm_loads_no_gpu_library():
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["config"]["integrals_per_pass"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+
+
+def test_oracle_density_screening_matches_direct_loop(oracle_mod):
+    # compute_2body_fock's density-weighted screening restated in a plain
+    # loop (hartree-fock++.cc:1640-1684): the accumulator with fock_precision
+    # must give the same J/K
+    from oracle import inputs
+    atoms = inputs.water_cluster(2, 1, 1, spacing=3.0, jitter=0.2, seed=21)
+    ob = inputs.load_basis("cc-pVDZ", atoms)
+    K = oracle_mod.schwarz(ob)
+    rng = np.random.default_rng(22)
+    D = inputs.random_density(ob.nbf, 10, seed=23)
+    D *= np.exp(rng.uniform(-12, 0, ob.nbf))[:, None]  # a wide range of block norms
+    D = 0.5 * (D + D.T)
+    fock = 1e-9
+    ns = ob.nshell
+    off, nf = ob.bf_off, ob.nfunc
+    Dsh = np.array([[np.abs(D[off[a]:off[a] + nf[a], off[b]:off[b] + nf[b]]).max()
+                     for b in range(ns)] for a in range(ns)])
+    J = np.zeros_like(D); Kx = np.zeros_like(D)
+    eps = np.finfo(float).eps
+    nq = skipped = 0
+    for s1 in range(ns):
+        for s2 in range(s1 + 1):
+            for s3 in range(s1 + 1):
+                for s4 in range((s2 if s3 == s1 else s3) + 1):
+                    if K[s1, s2] * K[s3, s4] < 1e-12:
+                        continue
+                    d = max(Dsh[s1, s2], Dsh[s1, s3], Dsh[s2, s3], Dsh[s1, s4], Dsh[s2, s4],
+                            Dsh[s3, s4])
+                    if d * K[s1, s2] * K[s3, s4] < fock:
+                        skipped += 1
+                        continue
+                    nq += 1
+                    v = oracle_mod.compute_quartet(ob, s1, s2, s3, s4, precision=max(eps, fock / d))
+                    if v is None:
+                        continue
+                    v = v[0]
+                    deg = ((1 if s1 == s2 else 2) * (1 if s3 == s4 else 2) *
+                           (1 if (s1 == s3 and s2 == s4) else 2))
+                    a = slice(off[s1], off[s1] + nf[s1]); b = slice(off[s2], off[s2] + nf[s2])
+                    c = slice(off[s3], off[s3] + nf[s3]); e = slice(off[s4], off[s4] + nf[s4])
+                    w = deg * v
+                    J[a, b] += np.einsum("ijkl,kl->ij", w, D[c, e])
+                    J[c, e] += np.einsum("ijkl,ij->kl", w, D[a, b])
+                    Kx[a, c] += np.einsum("ijkl,jl->ik", w, D[b, e])
+                    Kx[b, e] += np.einsum("ijkl,ik->jl", w, D[a, c])
+                    Kx[a, e] += np.einsum("ijkl,jk->il", w, D[b, c])
+                    Kx[b, c] += np.einsum("ijkl,il->jk", w, D[a, e])
+    J = 0.25 * (J + J.T)
+    Kx = 0.125 * (Kx + Kx.T)
+    assert skipped > 0 and nq > 0
+    acc = oracle_mod.JKAccumulator(ob.nbf, 2)
+    got_nq, _ = acc.add_pairs(ob, D, K, 1e-12, np.arange(ns * (ns + 1) // 2), fock_precision=fock)
+    Jo, Ko = acc.reduce()
+    acc.close()
+    assert got_nq == nq
+    np.testing.assert_allclose(Jo, J, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(Ko, Kx, rtol=0, atol=1e-13)

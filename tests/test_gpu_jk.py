@@ -230,3 +230,41 @@ def test_jk_graph_replay_matches_eager(lgx, water2, monkeypatch):
         monkeypatch.delenv("LGX_GRAPHS")
         assert np.max(np.abs(J2 - Jr)) < 1e-12 and np.max(np.abs(K2 - Kr)) < 1e-12
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_density_weighted_screening_vs_oracle(lgx, oracle_mod, mode):
+    # compute_2body_fock's density-weighted screening (lgx_set_fock_precision)
+    # against the oracle's restatement of it, on a density whose shell blocks
+    # span many orders of magnitude so that the screening skips quartets
+    atoms = lgx.water_cluster(2, 2, 2, spacing=3.0, jitter=0.2, seed=31)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    rng = np.random.default_rng(32)
+    D = lgx.random_density(bs.nbf, 40, seed=33)
+    D *= np.exp(rng.uniform(-14, 0, bs.nbf))[:, None]
+    D = 0.5 * (D + D.T)
+    fock = 1e-10
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    ctx = lgx.Context(0)
+    ctx.set_basis(bs)
+    K = ctx.schwarz()
+    ns = len(bs)
+    acc = oracle_mod.JKAccumulator(ob.nbf)
+    acc.add_pairs(ob, D, K, 1e-12, np.arange(ns * (ns + 1) // 2), fock_precision=fock)
+    Jo, Ko = acc.reduce()
+    acc.close()
+    J0, K0, _ = ctx.jk(D, 1e-12, mode=mode)
+    ctx.set_fock_precision(fock)
+    J, Kx, _ = ctx.jk(D, 1e-12, mode=mode)
+    J2, K2, _ = ctx.jk(D, 1e-12, mode=mode)  # the replayed pass graph
+    ctx.set_fock_precision(0.0)
+    J3, K3, _ = ctx.jk(D, 1e-12, mode=mode)
+    ctx.close()
+    tol = 1e-10 if mode == 0 else 1e-8
+    assert np.max(np.abs(J - Jo)) < tol and np.max(np.abs(Kx - Ko)) < tol
+    assert np.array_equal(J, J2) or np.max(np.abs(J - J2)) < 1e-12
+    # screening changes the result, and switching it off restores the plain pass
+    assert np.max(np.abs(J - J0)) > 0
+    assert np.max(np.abs(J3 - J0)) < 1e-12 and np.max(np.abs(K3 - K0)) < 1e-12
+    eo, e = lgx.jk_energies(D, Jo, Ko), lgx.jk_energies(D, J, Kx)
+    assert abs(eo[0] - e[0]) < 1e-8 and abs(eo[1] - e[1]) < 1e-8
