@@ -18,15 +18,16 @@ namespace lgx {
 //   below 2e-16 for m <= 5 and 1.7e-15 for m = 6 at T = 50.
 // FP64 evaluation once the branch and the grid point are chosen: asym
 // selects the asymptotic branch; otherwise k is the grid point and md =
-// T_k - T.
-template <int MMAX>
+// T_k - T.  PF: multiply by pfac (the mixed scheme's FP32 kernels apply
+// their prefactor in FP32, so they skip the FP64 products by 1).
+template <int MMAX, bool PF = true>
 __device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, double T, bool asym,
                                              int k, double md, double pfac, double* F) {
   static_assert(MMAX <= 6, "asymptotic branch without e^{-T} is exact to 2e-15 only for m <= 6");
   if (asym) {
     const double rs = rsqrt(T);
     const double oo2T = 0.5 * (rs * rs);
-    double f = (0.88622692545275801365 * pfac) * rs;
+    double f = PF ? (0.88622692545275801365 * pfac) * rs : 0.88622692545275801365 * rs;
     F[0] = f;
 #pragma unroll
     for (int m = 0; m < MMAX; ++m) {
@@ -43,14 +44,14 @@ __device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, dou
       double s = __ldg(c + 6);
 #pragma unroll
       for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
-      F[m] = s * pfac;
+      F[m] = PF ? s * pfac : s;
     }
   } else {
     const double* c = row + MMAX * kBoysTaylorStride;
     double s = __ldg(c + 6);
 #pragma unroll
     for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
-    s *= pfac;
+    if (PF) s *= pfac;
     F[MMAX] = s;
     double e = 1.0 / 720.0;
     e = fma(e, md, 1.0 / 120.0);
@@ -59,7 +60,7 @@ __device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, dou
     e = fma(e, md, 0.5);
     e = fma(e, md, 1.0);
     e = fma(e, md, 1.0);
-    const double eTp = (__ldg(row + 7) * pfac) * e;  // pfac e^{-T}
+    const double eTp = PF ? (__ldg(row + 7) * pfac) * e : __ldg(row + 7) * e;  // pfac e^{-T}
     const double twoT = 2.0 * T;
 #pragma unroll
     for (int m = MMAX - 1; m >= 0; --m) {
@@ -94,7 +95,7 @@ __device__ __forceinline__ void rk_boys_b64(const double* __restrict__ tay, doub
   const bool asym = Tf > float(kBoysTmax);
   const int k = asym ? 0 : __float2int_rn(Tf * float(kBoysInvDT));
   const double md = fma(i2d_int(k), kBoysDT, -T);
-  rk_boys_core<MMAX>(tay, T, asym, k, md, 1.0, F);
+  rk_boys_core<MMAX, false>(tay, T, asym, k, md, 1.0, F);
 }
 
 template <int MMAX>
