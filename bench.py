@@ -45,6 +45,7 @@ WORKLOADS = {
     "h2o16_cc-pvdz": ((4, 2, 2), "cc-pVDZ", 1e-12, "(H2O)16 cc-pVDZ 4x2x2 grid, Schwarz 1e-12"),
     "h2o4_cc-pvdz": ((2, 2, 1), "cc-pVDZ", 0.0, "(H2O)4 cc-pVDZ 2x2x1 grid, no screening"),
     "h2o8_cc-pvtz": ((2, 2, 2), "cc-pVTZ", 1e-12, "(H2O)8 cc-pVTZ 2x2x2 grid, Schwarz 1e-12"),
+    "h2o16_cc-pvtz": ((4, 2, 2), "cc-pVTZ", 1e-12, "(H2O)16 cc-pVTZ 4x2x2 grid, Schwarz 1e-12"),
 }
 DEFAULT_WORKLOAD = "h2o64_cc-pvtz"
 MIXED_THRESH = 1e-4
@@ -861,6 +862,34 @@ def run_rows(args):
     return 0
 
 
+def run_profile_pass(args):
+    """--profile-pass MODES: one J/K pass of the workload per precision mode
+    (0 FP64, 1 mixed, 2 mixed with FP32 Boys), with default launch shapes
+    (no tuning), serial class launches and no pass graph, so that each class
+    kernel is launched once per mode and a profiler can pick one launch by
+    name; prints every launch's device time."""
+    os.environ["LGX_TUNE"] = "0"
+    os.environ["LGX_OVERLAP"] = "0"
+    os.environ["LGX_GRAPHS"] = "0"
+    import torch
+    import libint_gb300 as lg
+    atoms, bs, D, thresh, desc = build_inputs(args.workload)
+    ctx = lg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx.set_basis(bs)
+    dD = torch.tensor(D, device="cuda")
+    dJ, dK = torch.empty_like(dD), torch.empty_like(dD)
+    out = {"workload": desc, "nbf": bs.nbf, "passes": []}
+    for mode in [int(x) for x in args.profile_pass.split(",")]:
+        st = ctx.jk_device(dD.data_ptr(), dJ.data_ptr(), dK.data_ptr(), thresh, mode, MIXED_THRESH)
+        out["passes"].append({"mode": mode, "pass_ms": st.pass_ms,
+                              "launches": [{k: r[k] for k in ("class", "fp32", "kernel", "ms",
+                                                              "quartets", "prim_quartets")}
+                                           for r in ctx.last_pass_launches()]})
+    ctx.close()
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -880,6 +909,8 @@ def main():
                     help="skip the pair-subset comparison with the oracle")
     ap.add_argument("--primitive-api", action="store_true",
                     help="time the generated-library entry (libint2_build_eri*) instead")
+    ap.add_argument("--profile-pass", default=None, metavar="MODES",
+                    help="one untuned, serial J/K pass per listed precision mode (profiling)")
     ap.add_argument("--rows", action="store_true",
                     help="time the widened rows (DF tensors, deriv 2, erfc J/K) instead")
     args = ap.parse_args()
@@ -887,6 +918,8 @@ def main():
         return run_primitive_api(args)
     if args.rows:
         return run_rows(args)
+    if args.profile_pass:
+        return run_profile_pass(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

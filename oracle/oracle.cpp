@@ -415,9 +415,14 @@ struct Quartet {
 };
 
 // The full Engine::compute2 restatement. Returns values per set, 0 if all
-// primitive quartets were screened.
+// primitive quartets were screened.  pair_precision > 0: the primitive
+// pairs are built at that (tighter) precision instead of `precision`, as
+// when a caller passes ShellPair data precomputed at its maximal engine
+// precision (engine.impl.h:1259-1276; hartree-fock++.cc:1386-1425), and
+// only the primitive quartets are screened at `precision`.
 int compute_quartet(const orc_basis* bs, const int* tgt, int deriv,
-                    double precision, int method, Work& w, double* out) {
+                    double precision, int method, Work& w, double* out,
+                    double pair_precision = 0.0) {
   const CartTable& ct = cart_table();
   const int tl[4] = {bs->l[tgt[0]], bs->l[tgt[1]], bs->l[tgt[2]], bs->l[tgt[3]]};
   Quartet q;
@@ -435,9 +440,10 @@ int compute_quartet(const orc_basis* bs, const int* tgt, int deriv,
   const int mmax = L + deriv;
   const double ln_prec =
       precision > 0 ? std::log(precision) : std::numeric_limits<double>::lowest();
+  const double ln_pair = pair_precision > 0 ? std::log(pair_precision) : ln_prec;
 
-  const int npb = pair_init(sh[0], sh[1], ln_prec, method, w.ppb);
-  const int npk = pair_init(sh[2], sh[3], ln_prec, method, w.ppk);
+  const int npb = pair_init(sh[0], sh[1], ln_pair, method, w.ppb);
+  const int npk = pair_init(sh[2], sh[3], ln_pair, method, w.ppk);
   const double* A = sh[0].O;
   const double* B = sh[1].O;
   const double* C = sh[2].O;
@@ -898,6 +904,16 @@ int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
   return compute_quartet(bs, tgt, deriv, precision, method, w, out);
 }
 
+// As orc_compute_quartet (deriv 0 or 1), with the primitive pairs built at
+// pair_precision and the primitive quartets screened at precision.
+int orc_compute_quartet_pairs(const orc_basis* bs, int s1, int s2, int s3, int s4, int deriv,
+                              double precision, double pair_precision, int method, double* out) {
+  if (deriv < 0 || deriv > 1) return -1;
+  thread_local Work w;
+  const int tgt[4] = {s1, s2, s3, s4};
+  return compute_quartet(bs, tgt, deriv, precision, method, w, out, pair_precision);
+}
+
 // Batched Engine::compute over an explicit list (4 shell indices per
 // quartet, caller order), OpenMP over quartets: set q is written at
 // out + offsets[q] (nsets sets back to back); is_null[q] = 1 when every
@@ -1056,7 +1072,9 @@ int64_t orc_jk_acc_pairs(orc_jk_acc* acc, const orc_basis* bs, const int* bf_off
                     n4 = nfunc(bs, s4);
           buf.resize(size_t(n1) * n2 * n3 * n4);
           const int tgt[4] = {s1, s2, s3, s4};
-          const int nv = compute_quartet(bs, tgt, 0, prec, 0, w, buf.data());
+          // primitive pairs at the machine epsilon (the GPU path's pair data;
+          // compute_2body_fock passes pairs precomputed at a tighter precision)
+          const int nv = compute_quartet(bs, tgt, 0, prec, 0, w, buf.data(), eps);
           ++nq;
           nint += int64_t(n1) * n2 * n3 * n4;
           if (nv == 0) continue;

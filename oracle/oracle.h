@@ -72,6 +72,12 @@ typedef struct {
 int orc_compute_quartet(const orc_basis* bs, int s1, int s2, int s3, int s4,
                         int deriv, double precision, int method, double* out);
 
+// As orc_compute_quartet (deriv 0 or 1) with the primitive pairs built at
+// pair_precision (precomputed ShellPair data, engine.impl.h:1259-1276) and
+// the primitive quartets screened at precision.
+int orc_compute_quartet_pairs(const orc_basis* bs, int s1, int s2, int s3, int s4, int deriv,
+                              double precision, double pair_precision, int method, double* out);
+
 // Schwarz factors K(s1,s2) = sqrt(max|(s1 s2|s1 s2)|) (precision 0).
 void orc_schwarz(const orc_basis* bs, double* K, int nthreads);
 

@@ -166,15 +166,23 @@ def shellpair_init(l1, a1, c1, O1, l2, a2, c2, O2, ln_prec, method=0):
 
 
 def compute_quartet(basis: OracleBasis, s1, s2, s3, s4, deriv=0,
-                    precision=np.finfo(float).eps, method=0):
+                    precision=np.finfo(float).eps, method=0, pair_precision=0.0):
     """Engine::compute(s1,s2,s3,s4): list of nsets arrays (n1,n2,n3,n4), or
-    None when every primitive quartet was screened out."""
+    None when every primitive quartet was screened out.  pair_precision > 0
+    builds the primitive pairs at that precision (a caller's precomputed
+    ShellPair data) and screens only the primitive quartets at precision."""
     n = [int(basis.nfunc[s]) for s in (s1, s2, s3, s4)]
     nsets = {0: 1, 1: 12, 2: 78}[deriv]
     out = np.zeros(nsets * int(np.prod(n)))
-    r = _lib().orc_compute_quartet(ctypes.byref(basis._c), s1, s2, s3, s4, deriv,
-                                   ctypes.c_double(precision), method,
-                                   _ptr(out, ctypes.c_double))
+    if pair_precision > 0:
+        r = _lib().orc_compute_quartet_pairs(ctypes.byref(basis._c), s1, s2, s3, s4, deriv,
+                                             ctypes.c_double(precision),
+                                             ctypes.c_double(pair_precision), method,
+                                             _ptr(out, ctypes.c_double))
+    else:
+        r = _lib().orc_compute_quartet(ctypes.byref(basis._c), s1, s2, s3, s4, deriv,
+                                       ctypes.c_double(precision), method,
+                                       _ptr(out, ctypes.c_double))
     if r < 0:
         raise ValueError("oracle: bad arguments")
     if r == 0:

@@ -183,7 +183,10 @@ def test_oracle_density_screening_matches_direct_loop(oracle_mod):
                         skipped += 1
                         continue
                     nq += 1
-                    v = oracle_mod.compute_quartet(ob, s1, s2, s3, s4, precision=max(eps, fock / d))
+                    # pairs precomputed at the machine epsilon, quartets screened at
+                    # fock / Dnorm1234 (hartree-fock++.cc:1386-1425,1681-1684)
+                    v = oracle_mod.compute_quartet(ob, s1, s2, s3, s4, precision=max(eps, fock / d),
+                                                   pair_precision=eps)
                     if v is None:
                         continue
                     v = v[0]

@@ -260,7 +260,10 @@ def test_density_weighted_screening_vs_oracle(lgx, oracle_mod, mode):
     ctx.set_fock_precision(0.0)
     J3, K3, _ = ctx.jk(D, 1e-12, mode=mode)
     ctx.close()
-    tol = 1e-10 if mode == 0 else 1e-8
+    # both sides screen alike; the GPU forms fock / Dnorm1234 and its
+    # logarithm in FP32, so a primitive quartet at the threshold may go the
+    # other way, each such one worth about fock_precision
+    tol = 1e-9 if mode == 0 else 1e-8
     assert np.max(np.abs(J - Jo)) < tol and np.max(np.abs(Kx - Ko)) < tol
     assert np.array_equal(J, J2) or np.max(np.abs(J - J2)) < 1e-12
     # screening changes the result, and switching it off restores the plain pass
