@@ -489,12 +489,14 @@ def run_gpu(args):
             ctx.jk(D, thresh, lg._lgx.LGX_MIXED, MIXED_THRESH)
         barrier()
         te2e = 0.0
+        dev_e2e = 0.0  # device time of the same passes (CUDA events)
         for _ in range(args.e2e_steps):
             flush.zero_()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             J_h, K_h, st_e = ctx.jk(D, thresh, lg._lgx.LGX_MIXED, MIXED_THRESH)
             te2e += time.perf_counter() - t0
+            dev_e2e += st_e.pass_ms * 1e-3
         barrier()
     clocks = clk.summary()
 
@@ -633,7 +635,11 @@ def run_gpu(args):
                                          % (peaks["fp64"], peaks["fp32"]),
                           "flops_fp64": fl64, "flops_fp32": fl32},
         "e2e": {"value": ve2e, "unit": "ERI/s", "steps": args.e2e_steps,
-                "h2d_bytes_per_step": nbf * nbf * 8, "d2h_bytes_per_step": 2 * nbf * nbf * 8},
+                "h2d_bytes_per_step": nbf * nbf * 8, "d2h_bytes_per_step": 2 * nbf * nbf * 8,
+                "wall_over_device_same_steps": te2e / dev_e2e if dev_e2e > 0 else None,
+                "note": "host D in, host J/K out through lgx_jk, wall clock per call; "
+                        "the copies add milliseconds to a pass of seconds, so across "
+                        "different steps e2e and value differ by pass-to-pass noise"},
         "gpu_launches": int(stmx.launches) * args.steps + int(st64.launches) * args.fp64_steps
         + int(stfb.launches) * args.alt_steps + int(st_e.launches) * args.e2e_steps,
         "clocks": clocks,
