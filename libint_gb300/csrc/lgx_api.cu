@@ -2432,7 +2432,6 @@ lgx_status jk_device_locked(lgx_context* ctx, const double* dD, double* dJ, doub
     a.dsh = ctx->Dsh.as<double>();
     a.kpair = B.Kd.as<double>();
     a.fock_prec = ctx->fock_prec;
-    a.ln_fock = std::log(ctx->fock_prec);
   }
   if (mixedp) CK(launch_d2f(dD, ctx->Df.as<float>(), (long long)nn, ctx->stream));
   if (dscreen) CK(launch_shell_block_norm(B.dev, dD, B.nbf, ctx->Dsh.as<double>(), ctx->stream));
@@ -2625,7 +2624,6 @@ lgx_status lgx_jk_device_noalloc(lgx_context* ctx, const double* dD, double* dJ,
     a.dsh = ctx->Dsh.as<double>();
     a.kpair = B.Kd.as<double>();
     a.fock_prec = ctx->fock_prec;
-    a.ln_fock = std::log(ctx->fock_prec);
     CK(launch_shell_block_norm(B.dev, dD, B.nbf, ctx->Dsh.as<double>(), ctx->stream));
   }
   s = run_bins(ctx, B, kModeJK, 0, mode32, a, stats);

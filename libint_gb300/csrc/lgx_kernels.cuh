@@ -149,12 +149,10 @@ struct EriArgs {
   double* gK;
   int nbf;
   // density-weighted screening of the J/K passes (fock_prec > 0): shell-
-  // block infinity norms of D (nshell x nshell), Schwarz factor per pair,
-  // ln(fock_prec)
+  // block infinity norms of D (nshell x nshell), Schwarz factor per pair
   const double* dsh;
   const double* kpair;
   double fock_prec;
-  double ln_fock;
   // watchdog: a bounded number of work chunks per warp
   long long max_chunks;
   int* error_flag;
@@ -163,10 +161,14 @@ struct EriArgs {
 };
 
 // Primitive-screening thresholds of one shell quartet (Engine::set_precision:
-// precision and its logarithm, with FP32 copies).
+// precision and its logarithm, with FP32 copies).  ln64: the FP64 kernels
+// make the logarithmic test in FP64 (a precision above ~1e-15, whose
+// threshold can cut primitive quartets that matter); below that the FP32
+// test decides only about contributions under ~1e-14.
 struct PrimScreen {
   double prec, ln_prec;
   float fprec, fln_prec;
+  bool ln64;
 };
 
 // The thresholds of the pass, or with density-weighted screening
@@ -174,14 +176,19 @@ struct PrimScreen {
 // (tests/hartree-fock/hartree-fock++.cc:1640-1684): Dnorm1234 = the largest
 // infinity norm of the six shell blocks of D the quartet touches; the quartet
 // is skipped when Dnorm1234 K12 K34 < fock_prec (returns false), else its
-// primitives are screened at fock_prec / Dnorm1234 (FP32 quotient and
-// logarithm; not below the precision the pair data were built with).
+// primitives are screened at fock_prec / Dnorm1234 and its logarithm, both
+// in FP64 as Engine::set_precision forms them (not below the precision the
+// pair data were built with); the FP32 kernels compare with their FP32
+// roundings.  A primitive quartet at the threshold can carry up to ~100x
+// the threshold (pfac bounds only its (ss|ss) part), so the FP64 kernels'
+// decisions have to be the FP64 ones for their J/K to match compute_2body_fock.
 __device__ __forceinline__ bool quartet_screen(const EriArgs& a, const int* sh, int bpair,
                                                int kpair, PrimScreen& s) {
   s.prec = a.precision;
   s.ln_prec = a.ln_prec;
   s.fprec = a.fprecision;
   s.fln_prec = a.fln_prec;
+  s.ln64 = a.precision > 1e-15;
   if (!(a.fock_prec > 0.0)) return true;
   const int ns = a.basis.nshell;
   const double* d = a.dsh;
@@ -189,12 +196,13 @@ __device__ __forceinline__ bool quartet_screen(const EriArgs& a, const int* sh, 
                               fmax(d[sh[1] * ns + sh[2]], d[sh[0] * ns + sh[3]])),
                          fmax(d[sh[1] * ns + sh[3]], d[sh[2] * ns + sh[3]]));
   if (dn * __ldg(a.kpair + bpair) * __ldg(a.kpair + kpair) < a.fock_prec) return false;
-  const float q = float(a.fock_prec) / float(dn);
-  if (q > s.fprec) {
-    s.fprec = q;
-    s.prec = f2d_int(q);
-    s.fln_prec = float(a.ln_fock) - __logf(float(dn));
-    s.ln_prec = f2d_int(s.fln_prec);
+  const double q = a.fock_prec / dn;  // dn > 0: a zero norm failed the test above
+  if (q > s.prec) {
+    s.prec = q;
+    s.ln_prec = log(q);
+    s.fprec = __double2float_rn(q);
+    s.fln_prec = __double2float_rn(s.ln_prec);
+    s.ln64 = true;
   }
   return true;
 }

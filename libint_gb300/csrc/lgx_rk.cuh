@@ -116,15 +116,18 @@ __device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, 
 }
 
 // One primitive quartet into acc (FP64).  Returns false when screened out.
-// The ln-screen runs on the FP32 copies (it only decides whether a
-// primitive quartet below ~1e-16 contributes) and the pfac screen compares
-// the IEEE bit patterns, so neither costs an FP64 instruction.
+// At the default precision the ln-screen runs on the FP32 copies (it only
+// decides whether a primitive quartet below ~1e-16 contributes) and the
+// pfac screen compares the IEEE bit patterns, so neither costs an FP64
+// instruction; at a coarser precision (scr.ln64) the ln-screen is FP64.
 template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double>& q, int ib,
                                         int ik, const PrimScreen& scr, double* acc) {
   const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
-  if (!(bp.fln_scr + kp.fln_scr > scr.fln_prec)) return false;
+  if (scr.ln64 ? !(bp.ln_scr + kp.ln_scr > scr.ln_prec)
+               : !(bp.fln_scr + kp.fln_scr > scr.fln_prec))
+    return false;
   const double zeta = bp.zeta, eta = kp.zeta;
   const double gpq = zeta + eta;
   const double rs = rsqrt(gpq);
@@ -284,10 +287,24 @@ __device__ __forceinline__ float rk_D(const EriArgs& a, size_t i, float*) {
   return __ldg(a.Df + i);
 }
 
+// Blocks per SM the compiler has to allow for (__launch_bounds__; 0 = no
+// minimum, the compiler's own register target).  The mixed scheme's FP32
+// kernels of the smallest classes wait on FP64 results (the Boys function)
+// and gain from more resident warps: 8 blocks of 128 threads (at most 64
+// registers).  The FP64 instances with L >= 5 get 1: left to its own target
+// the compiler gives several of them 32 registers and 25-57 KB of spills per
+// thread (local memory the context has to reserve for every resident
+// thread), with 1 they keep up to 255 registers and spill 4-21 KB.
+template <typename T, int L, int MODE>
+constexpr int rk_min_blocks() {
+  return (sizeof(T) == 4 && mode_b64(MODE) && L <= 2) ? 8 : (sizeof(T) == 8 && L >= 5 ? 1 : 0);
+}
+
 // ATT: attenuated operator (erf / erfc, EriArgs::op), J/K mode only; the
 // Coulomb instances (ATT = false) carry none of its code.
 template <typename T, int LA, int LB, int LC, int LD, int MODE, bool ATT = false>
-__global__ void __launch_bounds__(128) rk_kernel(EriArgs a) {
+__global__ void __launch_bounds__(128, (rk_min_blocks<T, LA + LB + LC + LD, MODE>()))
+    rk_kernel(EriArgs a) {
   using C = rk::Cls<LA, LB, LC, LD>;
   constexpr int N0 = C::kN0, N1 = C::kN1, N2 = C::kN2, N3 = C::kN3;
   const int G = a.group;

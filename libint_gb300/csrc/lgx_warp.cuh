@@ -190,6 +190,7 @@ __device__ __forceinline__ void load_geom(const EriArgs& a, int bpair, int kpair
   g.scr.ln_prec = a.ln_prec;
   g.scr.fprec = a.fprecision;
   g.scr.fln_prec = a.fln_prec;
+  g.scr.ln64 = a.precision > 1e-15;
   if constexpr (sizeof(T) == 8) {
     for (int x = 0; x < 3; ++x) {
       const double A = a.basis.O[3 * g.sh[0] + x], B = a.basis.O[3 * g.sh[1] + x];

@@ -94,6 +94,25 @@ def test_water_cc_pvdz_quartets(lgx, oracle_mod):
         assert np.max(np.abs(got - ref[0])) < TOL, q
 
 
+@pytest.mark.parametrize("precision", [1e-10, 1e-7])
+def test_coarse_precision_vs_oracle(lgx, oracle_mod, precision):
+    # Engine::set_precision above the default: the primitive quartets cut by
+    # the coarser threshold (engine.impl.h:1306-1766) must be the oracle's
+    # ones, or the sets differ by up to ~100x the threshold
+    atoms = lgx.water_cluster(1, 1, 1, seed=3)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    eng = lgx.Engine(lgx.Operator.coulomb, bs.max_nprim(), bs.max_l(), 0, precision=precision)
+    rng = np.random.default_rng(1)
+    for _ in range(60):
+        q = [int(x) for x in rng.integers(0, len(bs), 4)]
+        got = eng.compute(*[bs[i] for i in q])
+        ref = oracle_mod.compute_quartet(ob, *q, precision=precision)
+        assert (got is None) == (ref is None), q
+        if got is not None:
+            assert np.max(np.abs(got - ref[0])) < TOL, q
+
+
 def test_compute_2body_fock_vs_oracle(lgx, oracle_mod):
     # the binding's Engine.compute_2body_fock(D, basis) (python/src/libint2/
     # engine.cc:230-279) through one GPU J/K pass: G = 2J - K
