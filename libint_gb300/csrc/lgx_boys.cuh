@@ -19,10 +19,14 @@ namespace lgx {
 // FP64 evaluation once the branch and the grid point are chosen: asym
 // selects the asymptotic branch; otherwise k is the grid point and md =
 // T_k - T.  PF: multiply by pfac (the mixed scheme's FP32 kernels apply
-// their prefactor in FP32, so they skip the FP64 products by 1).
-template <int MMAX, bool PF = true>
+// their prefactor in FP32, so they skip the FP64 products by 1).  NT: terms
+// of the Taylor series and of the e^{T_k - T} series (7: remainder below
+// |md|^7/7! < 5e-17 of F_m; 5: below 7.8e-12, for values that are rounded
+// to FP32 next, whose half-ulp is 6e-8).
+template <int MMAX, bool PF = true, int NT = 7>
 __device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, double T, bool asym,
                                              int k, double md, double pfac, double* F) {
+  static_assert(NT >= 2 && NT <= 7, "the table holds 7 Taylor coefficients per m");
   static_assert(MMAX <= 6, "asymptotic branch without e^{-T} is exact to 2e-15 only for m <= 6");
   if (asym) {
     const double rs = rsqrt(T);
@@ -41,25 +45,24 @@ __device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, dou
 #pragma unroll
     for (int m = 0; m <= MMAX; ++m) {
       const double* c = row + m * kBoysTaylorStride;
-      double s = __ldg(c + 6);
+      double s = __ldg(c + NT - 1);
 #pragma unroll
-      for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
+      for (int i = NT - 2; i >= 0; --i) s = fma(s, md, __ldg(c + i));
       F[m] = PF ? s * pfac : s;
     }
   } else {
     const double* c = row + MMAX * kBoysTaylorStride;
-    double s = __ldg(c + 6);
+    double s = __ldg(c + NT - 1);
 #pragma unroll
-    for (int i = 5; i >= 0; --i) s = fma(s, md, __ldg(c + i));
+    for (int i = NT - 2; i >= 0; --i) s = fma(s, md, __ldg(c + i));
     if (PF) s *= pfac;
     F[MMAX] = s;
-    double e = 1.0 / 720.0;
-    e = fma(e, md, 1.0 / 120.0);
-    e = fma(e, md, 1.0 / 24.0);
-    e = fma(e, md, 1.0 / 6.0);
-    e = fma(e, md, 0.5);
-    e = fma(e, md, 1.0);
-    e = fma(e, md, 1.0);
+    // e^{md} = sum_{i < NT} md^i / i!, Horner from the top term
+    constexpr double inv_fact[7] = {1.0, 1.0, 0.5, 1.0 / 6.0, 1.0 / 24.0, 1.0 / 120.0,
+                                    1.0 / 720.0};
+    double e = inv_fact[NT - 1];
+#pragma unroll
+    for (int i = NT - 2; i >= 0; --i) e = fma(e, md, inv_fact[i]);
     const double eTp = PF ? (__ldg(row + 7) * pfac) * e : __ldg(row + 7) * e;  // pfac e^{-T}
     const double twoT = 2.0 * T;
 #pragma unroll
@@ -88,14 +91,16 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T
 // so the grid point may be the neighbour of T's nearest one (|md| <= 1/64 +
 // 3e-5: Taylor remainder still below 5e-17), and near T = 50 either branch
 // is exact (the asymptotic one drops Q(m+1/2, T) < 2e-15); Tf <= 50 gives
-// k <= 1600 < kBoysRows.
+// k <= 1600 < kBoysRows.  The values are rounded to FP32 next, so the
+// series stop at 5 terms: relative error below 7.8e-12 (|md| <= 1/64 +
+// 3e-5), four orders under the FP32 half-ulp.
 template <int MMAX>
 __device__ __forceinline__ void rk_boys_b64(const double* __restrict__ tay, double T, float Tf,
                                             double* F) {
   const bool asym = Tf > float(kBoysTmax);
   const int k = asym ? 0 : __float2int_rn(Tf * float(kBoysInvDT));
   const double md = fma(i2d_int(k), kBoysDT, -T);
-  rk_boys_core<MMAX, false>(tay, T, asym, k, md, 1.0, F);
+  rk_boys_core<MMAX, false, 5>(tay, T, asym, k, md, 1.0, F);
 }
 
 template <int MMAX>

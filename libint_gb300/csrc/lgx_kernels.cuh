@@ -161,15 +161,40 @@ struct EriArgs {
 };
 
 // Primitive-screening thresholds of one shell quartet (Engine::set_precision:
-// precision and its logarithm, with FP32 copies).  ln64: the FP64 kernels
-// make the logarithmic test in FP64 (a precision above ~1e-15, whose
-// threshold can cut primitive quartets that matter); below that the FP32
-// test decides only about contributions under ~1e-14.
+// precision and its logarithm, with FP32 copies).
 struct PrimScreen {
   double prec, ln_prec;
   float fprec, fln_prec;
-  bool ln64;
 };
+
+// Primitive-quartet screening decisions that are the FP64 ones at FP32 cost
+// (engine.impl.h:1306-1466: ln_scr12 + ln_scr34 > ln(precision), then
+// |prefactor| >= precision).  The FP32 sum of the pairs' logarithms (|value|
+// <= ~50: rounding below 1e-5) and the FP32 prefactor (below 1e-6 relative)
+// decide, except inside a band around the threshold (3e-5 in the logarithm,
+// 4e-6 relative in the prefactor), where the FP64 values of the two pairs'
+// records (PrimPairRec bidx, kidx) decide.  A primitive quartet at the
+// threshold can carry ~100x the threshold (the prefactor bounds only its
+// (ss|ss) part), so with a coarse precision (density-weighted screening) an
+// FP32 decision that went the other way would show in J/K.
+constexpr float kLnBand = 3e-5f;
+constexpr float kPfBand = 4e-6f;
+__device__ __forceinline__ bool ln_kept(const EriArgs& a, float fsum, long long bidx,
+                                        long long kidx, const PrimScreen& s) {
+  const float dl = fsum - s.fln_prec;
+  if (dl >= kLnBand) return true;
+  if (dl <= -kLnBand) return false;
+  return a.pprims[bidx].ln_scr + a.pprims[kidx].ln_scr > s.ln_prec;
+}
+// mag: the FP32 |prefactor| times scale (1, or the Conservative factor).
+__device__ __forceinline__ bool pf_kept(const EriArgs& a, float mag, double scale, long long bidx,
+                                        long long kidx, const PrimScreen& s) {
+  if (mag >= s.fprec * (1.0f + kPfBand)) return true;
+  if (mag < s.fprec * (1.0f - kPfBand)) return false;
+  const PrimPairRec& b = a.pprims[bidx];
+  const PrimPairRec& k = a.pprims[kidx];
+  return fabs(b.Kc * k.Kc * rsqrt(b.zeta + k.zeta)) * scale >= s.prec;
+}
 
 // The thresholds of the pass, or with density-weighted screening
 // (EriArgs::fock_prec > 0) those of compute_2body_fock
@@ -178,17 +203,14 @@ struct PrimScreen {
 // is skipped when Dnorm1234 K12 K34 < fock_prec (returns false), else its
 // primitives are screened at fock_prec / Dnorm1234 and its logarithm, both
 // in FP64 as Engine::set_precision forms them (not below the precision the
-// pair data were built with); the FP32 kernels compare with their FP32
-// roundings.  A primitive quartet at the threshold can carry up to ~100x
-// the threshold (pfac bounds only its (ss|ss) part), so the FP64 kernels'
-// decisions have to be the FP64 ones for their J/K to match compute_2body_fock.
+// pair data were built with); the primitive decisions are then the FP64
+// ones in every kernel (ln_kept, pf_kept).
 __device__ __forceinline__ bool quartet_screen(const EriArgs& a, const int* sh, int bpair,
                                                int kpair, PrimScreen& s) {
   s.prec = a.precision;
   s.ln_prec = a.ln_prec;
   s.fprec = a.fprecision;
   s.fln_prec = a.fln_prec;
-  s.ln64 = a.precision > 1e-15;
   if (!(a.fock_prec > 0.0)) return true;
   const int ns = a.basis.nshell;
   const double* d = a.dsh;
@@ -202,7 +224,6 @@ __device__ __forceinline__ bool quartet_screen(const EriArgs& a, const int* sh, 
     s.ln_prec = log(q);
     s.fprec = __double2float_rn(q);
     s.fln_prec = __double2float_rn(s.ln_prec);
-    s.ln64 = true;
   }
   return true;
 }

@@ -116,18 +116,15 @@ __device__ __forceinline__ void rk_load(const EriArgs& a, int bpair, int kpair, 
 }
 
 // One primitive quartet into acc (FP64).  Returns false when screened out.
-// At the default precision the ln-screen runs on the FP32 copies (it only
-// decides whether a primitive quartet below ~1e-16 contributes) and the
-// pfac screen compares the IEEE bit patterns, so neither costs an FP64
-// instruction; at a coarser precision (scr.ln64) the ln-screen is FP64.
+// The ln-screen runs on the FP32 copies with the FP64 values inside the
+// rounding band (ln_kept) and the pfac screen compares the IEEE bit
+// patterns, so neither costs an FP64 instruction outside the band.
 template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<double>& q, int ib,
                                         int ik, const PrimScreen& scr, double* acc) {
   const PrimPairRec& bp = a.pprims[q.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[q.ket_pp + ik];
-  if (scr.ln64 ? !(bp.ln_scr + kp.ln_scr > scr.ln_prec)
-               : !(bp.fln_scr + kp.fln_scr > scr.fln_prec))
-    return false;
+  if (!ln_kept(a, bp.fln_scr + kp.fln_scr, q.bra_pp + ib, q.ket_pp + ik, scr)) return false;
   const double zeta = bp.zeta, eta = kp.zeta;
   const double gpq = zeta + eta;
   const double rs = rsqrt(gpq);
@@ -181,17 +178,19 @@ __device__ __forceinline__ PrimF32 rk_pp32(const PrimPairRec& r, bool sw) {
 }
 
 // One primitive quartet into acc (FP32).  AC = A - C of the quartet.
+// bidx, kidx: the two primitive pairs' PrimPairRec indices (the FP64
+// values of the screening decisions inside the rounding band).
 template <class C, bool ATT>
 __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>& q,
-                                        const PrimF32& bp, const PrimF32& kp,
-                                        const PrimScreen& scr, float* acc) {
-  if (!(bp.k.w + kp.k.w > scr.fln_prec)) return false;
+                                        const PrimF32& bp, const PrimF32& kp, int bidx,
+                                        int kidx, const PrimScreen& scr, float* acc) {
+  if (!ln_kept(a, bp.k.w + kp.k.w, bidx, kidx, scr)) return false;
   const float zeta = bp.k.y, eta = kp.k.y;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
   const float pfac = bp.k.x * kp.k.x * rs;
-  if (fabsf(pfac) < scr.fprec) return false;
+  if (!pf_kept(a, fabsf(pfac), 1.0, bidx, kidx, scr)) return false;
   const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
   const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
@@ -229,15 +228,15 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
 template <class C>
 __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<float>& q,
                                             const PrimF32& bp, const PrimF32& kp, const double* Pb,
-                                            double zb, const double* Pk, double zk,
-                                            const PrimScreen& scr, float* acc) {
-  if (!(bp.k.w + kp.k.w > scr.fln_prec)) return false;
+                                            double zb, const double* Pk, double zk, int bidx,
+                                            int kidx, const PrimScreen& scr, float* acc) {
+  if (!ln_kept(a, bp.k.w + kp.k.w, bidx, kidx, scr)) return false;
   const float zeta = bp.k.y, eta = kp.k.y;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
   const float pfac = bp.k.x * kp.k.x * rs;
-  if (fabsf(pfac) < scr.fprec) return false;
+  if (!pf_kept(a, fabsf(pfac), 1.0, bidx, kidx, scr)) return false;
   const float PA[3] = {bp.pa.x, bp.pa.y, bp.pa.z};
   const float QC[3] = {kp.pa.x, kp.pa.y, kp.pa.z};
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
@@ -391,9 +390,10 @@ __global__ void __launch_bounds__(128, (rk_min_blocks<T, LA + LB + LC + LD, MODE
             Pb[0] = b64.P[0]; Pb[1] = b64.P[1]; Pb[2] = b64.P[2]; zb = b64.zeta;
             Pk[0] = k64.P[0]; Pk[1] = k64.P[1]; Pk[2] = k64.P[2]; zk = k64.zeta;
           }
-          kept += rk_prim_b64<C>(a, q, bp, kp, Pb, zb, Pk, zk, scr, acc) ? 1 : 0;
+          kept += rk_prim_b64<C>(a, q, bp, kp, Pb, zb, Pk, zk, q.bra_pp + ib, q.ket_pp + ik,
+                                 scr, acc) ? 1 : 0;
         } else {
-          kept += rk_prim<C, ATT>(a, q, bp, kp, scr, acc) ? 1 : 0;
+          kept += rk_prim<C, ATT>(a, q, bp, kp, q.bra_pp + ib, q.ket_pp + ik, scr, acc) ? 1 : 0;
         }
       } else {
         kept += rk_prim<C, ATT>(a, q, ib, ik, scr, acc) ? 1 : 0;

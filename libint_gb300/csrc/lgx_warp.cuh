@@ -190,7 +190,6 @@ __device__ __forceinline__ void load_geom(const EriArgs& a, int bpair, int kpair
   g.scr.ln_prec = a.ln_prec;
   g.scr.fprec = a.fprecision;
   g.scr.fln_prec = a.fln_prec;
-  g.scr.ln64 = a.precision > 1e-15;
   if constexpr (sizeof(T) == 8) {
     for (int x = 0; x < 3; ++x) {
       const double A = a.basis.O[3 * g.sh[0] + x], B = a.basis.O[3 * g.sh[1] + x];
@@ -231,7 +230,7 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
   const PrimPairRec& bp = a.pprims[g.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[g.ket_pp + ik];
-  if (!(bp.ln_scr + kp.ln_scr > g.scr.ln_prec)) return false;
+  if (!ln_kept(a, bp.fln_scr + kp.fln_scr, g.bra_pp + ib, g.ket_pp + ik, g.scr)) return false;
   const double zeta = bp.zeta, eta = kp.zeta;
   const double gpq = zeta + eta;
   const double rs = rsqrt(gpq);
@@ -283,15 +282,16 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<flo
   const int ib = idx / g.nkpp, ik = idx - ib * g.nkpp;
   const PrimPairRec& bp = a.pprims[g.bra_pp + ib];
   const PrimPairRec& kp = a.pprims[g.ket_pp + ik];
-  if (!(bp.fln_scr + kp.fln_scr > g.scr.fln_prec)) return false;
+  if (!ln_kept(a, bp.fln_scr + kp.fln_scr, g.bra_pp + ib, g.ket_pp + ik, g.scr)) return false;
   const float zeta = bp.fzeta, eta = kp.fzeta;
   const float gpq = zeta + eta;
   const float rs = rsqrtf(gpq);
   const float oogpq = rs * rs;
   const float pfac = bp.fKc * kp.fKc * rs;
-  float mag = fabsf(pfac);
-  if (a.screening == 1) mag *= fmaxf(1.0f, bp.fnonsph * kp.fnonsph) * float(npbraket);
-  if (mag < g.scr.fprec) return false;
+  const double scale =
+      a.screening == 1 ? fmax(1.0, double(bp.fnonsph) * double(kp.fnonsph)) * npbraket : 1.0;
+  if (!pf_kept(a, fabsf(pfac) * float(scale), scale, g.bra_pp + ib, g.ket_pp + ik, g.scr))
+    return false;
   const float* PA = g.bra_sw ? bp.fPA2 : bp.fPA1;
   const float* QC = g.ket_sw ? kp.fPA2 : kp.fPA1;
   const float PQx = PA[0] - QC[0] + g.AC[0], PQy = PA[1] - QC[1] + g.AC[1],

@@ -74,8 +74,9 @@ def test_mixed_scheme_boys_is_fp64_rounded_to_fp32(gpu_ctx, v64, vb, mmax):
     # nearest FP32 (integer-only conversion).  The program kernels' values
     # are exactly numpy's float32 rounding of the FP64 evaluator's (wherever
     # those are FP32 normals); the register kernels pick the Taylor grid
-    # point from the FP32 argument, so their FP64 value may differ in the
-    # last FP64 bits and, rarely, round to the neighbouring float32
+    # point from the FP32 argument and stop the series at 5 terms (relative
+    # error below 7.8e-12), so their value may, rarely, round to the
+    # neighbouring float32
     rng = np.random.default_rng(13)
     T = np.concatenate([load("boys.npz")["T"], rng.uniform(0, 60, 4000),
                         rng.uniform(60, 2000, 500)])
