@@ -150,6 +150,21 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4],
                                 int deriv, double precision, int screening,
                                 double* out, size_t out_capacity, int* nsets,
                                 int* nvalues, int* is_null);
+/* lgx_compute_shellset (deriv 0 or 1) with the caller's precomputed
+ * ShellPair data of Engine::compute2(s1, s2, s3, s4, sp12, sp34)
+ * (engine.h:787-791): the reference uses a given ShellPair, instead of
+ * recomputing it at the engine precision, when its ln_prec is at most
+ * ln(precision) (engine.impl.h:1259-1276).  pair_ln_prec[0] / [1]: the
+ * ln_prec the bra (shells 0, 1) / ket (shells 2, 3) primitive pairs are
+ * screened at (ShellPair::init with `screening`, shell.h:1138-1256); the
+ * primitive quartets are screened at `precision` as in
+ * lgx_compute_shellset.  The caller passes ln(precision) for a pair it
+ * does not supply. */
+lgx_status lgx_compute_shellset_pairs(lgx_context* ctx, const lgx_shell shells[4],
+                                      int deriv, double precision, int screening,
+                                      const double pair_ln_prec[2], double* out,
+                                      size_t out_capacity, int* nsets, int* nvalues,
+                                      int* is_null);
 
 /* ------------------------------------ generated-library entry (Libint_t) */
 

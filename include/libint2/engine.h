@@ -288,12 +288,18 @@ class Engine {
     if (braket_rank() != 2) throw std::invalid_argument("Engine::compute: braket needs 2 shells");
     return compute_impl(s1, Shell::unit(), s2, Shell::unit());
   }
-  /// Engine::compute2<op, braket, deriv> (engine.h:787-791); the optional
-  /// ShellPair data is not needed by the GPU path.
+  /// Engine::compute2<op, braket, deriv> (engine.h:787-791).  Precomputed
+  /// ShellPair data of the bra / ket (xx_xx, deriv 0 or 1) is used as the
+  /// reference uses it (engine.impl.h:1259-1276): when its ln_prec is at
+  /// most ln(precision) its primitive pairs are the ones screened (the GPU
+  /// rebuilds them at that ln_prec: the data of ShellPair::init with the
+  /// engine's Original / Conservative method), else they are recomputed at
+  /// the engine precision; a ShellPair of another screening method is
+  /// rejected, as the reference asserts.  Deriv 2 recomputes them.
   template <Operator op, BraKet bk, size_t deriv>
   const target_ptr_vec& compute2(const Shell& s1, const Shell& s2, const Shell& s3,
-                                 const Shell& s4, const ShellPair* = nullptr,
-                                 const ShellPair* = nullptr) {
+                                 const Shell& s4, const ShellPair* sp12 = nullptr,
+                                 const ShellPair* sp34 = nullptr) {
     static_assert((op == Operator::coulomb || op == Operator::erf_coulomb ||
                    op == Operator::erfc_coulomb) &&
                       (bk == BraKet::xx_xx || bk == BraKet::xs_xx || bk == BraKet::xs_xs),
@@ -301,6 +307,17 @@ class Engine {
                   "implemented on the GPU path");
     if (int(deriv) != deriv_order_ || bk != braket_ || op != oper_)
       throw std::invalid_argument("Engine::compute2: deriv_order, operator or braket mismatch");
+    for (const ShellPair* sp : {sp12, sp34})
+      if (sp && sp->screening_method_ != screening_)
+        throw std::invalid_argument(
+            "Engine::compute2: received ShellPair initialized for an incompatible screening "
+            "method");
+    if ((sp12 || sp34) && bk == BraKet::xx_xx && deriv_order_ < 2) {
+      const double pl[2] = {
+          sp12 && sp12->ln_prec <= ln_precision_ ? double(sp12->ln_prec) : ln_precision_,
+          sp34 && sp34->ln_prec <= ln_precision_ ? double(sp34->ln_prec) : ln_precision_};
+      return compute_impl(s1, s2, s3, s4, pl);
+    }
     return compute_impl(s1, s2, s3, s4);
   }
 
@@ -318,8 +335,9 @@ class Engine {
   std::vector<value_type> buf_;
   target_ptr_vec targets_;
 
+  // pair_ln: NULL, or the ln_prec of the bra / ket primitive pairs
   const target_ptr_vec& compute_impl(const Shell& s1, const Shell& s2, const Shell& s3,
-                                     const Shell& s4) {
+                                     const Shell& s4, const double* pair_ln = nullptr) {
     if (!initialized_) throw using_default_initialized();
     const Shell* sh[4] = {&s1, &s2, &s3, &s4};
     lgx_shell d[4];
@@ -350,9 +368,11 @@ class Engine {
                         : (oper_ == Operator::erfc_coulomb ? LGX_OP_ERFC_COULOMB : LGX_OP_COULOMB);
     if (lgx_set_operator(rt.ctx, opc, omega_) != LGX_OK)
       throw std::runtime_error(std::string("libint2::Engine::compute: ") + lgx_last_error(rt.ctx));
-    const lgx_status st = lgx_compute_shellset(rt.ctx, d, deriv_order_, precision_, method,
-                                               buf_.data(), buf_.size(), &nsets, &nvalues,
-                                               &is_null);
+    const lgx_status st =
+        pair_ln ? lgx_compute_shellset_pairs(rt.ctx, d, deriv_order_, precision_, method, pair_ln,
+                                             buf_.data(), buf_.size(), &nsets, &nvalues, &is_null)
+                : lgx_compute_shellset(rt.ctx, d, deriv_order_, precision_, method, buf_.data(),
+                                       buf_.size(), &nsets, &nvalues, &is_null);
     if (st == LGX_ERR_LMAX_EXCEEDED) throw lmax_exceeded("eri", LGX_MAX_L, size_t(lmax_));
     if (st != LGX_OK)
       throw std::runtime_error(std::string("libint2::Engine::compute: ") + lgx_last_error(rt.ctx));

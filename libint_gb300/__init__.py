@@ -338,16 +338,26 @@ class Context:
 
     # ------------------------------------------------------------ engine
     def compute_shellset(self, shells, deriv=0, precision=np.finfo(float).eps,
-                         screening=ScreeningMethod.Original):
+                         screening=ScreeningMethod.Original, pair_ln_prec=None):
+        """One shell set (list of nsets arrays, or None when fully screened).
+        pair_ln_prec: None, or (bra, ket) ln_prec of caller-precomputed
+        ShellPair data (lgx_compute_shellset_pairs; deriv 0 or 1)."""
         arr = (_lgx.LgxShell * 4)(*[s._c() for s in shells])
         nsets = {0: 1, 1: 12, 2: 78}[int(deriv)]
         nv = int(np.prod([s.size() for s in shells]))
         out = np.zeros(nsets * nv)
         ns, nvals, isnull = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        st = self._lib.lgx_compute_shellset(self._h, arr, int(deriv), float(precision),
-                                            int(screening), _lgx.ptr(out), out.size,
-                                            ctypes.byref(ns), ctypes.byref(nvals),
-                                            ctypes.byref(isnull))
+        if pair_ln_prec is None:
+            st = self._lib.lgx_compute_shellset(self._h, arr, int(deriv), float(precision),
+                                                int(screening), _lgx.ptr(out), out.size,
+                                                ctypes.byref(ns), ctypes.byref(nvals),
+                                                ctypes.byref(isnull))
+        else:
+            pl = np.asarray(pair_ln_prec, dtype=np.float64).reshape(2)
+            st = self._lib.lgx_compute_shellset_pairs(self._h, arr, int(deriv), float(precision),
+                                                      int(screening), _lgx.ptr(pl),
+                                                      _lgx.ptr(out), out.size, ctypes.byref(ns),
+                                                      ctypes.byref(nvals), ctypes.byref(isnull))
         self._check(st, "lgx_compute_shellset")
         if isnull.value:
             return None

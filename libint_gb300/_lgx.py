@@ -101,6 +101,12 @@ SIGNATURES = {
                                             ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int)]),
+    "lgx_compute_shellset_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(LgxShell),
+                                                  ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                  _dp, _dp, ctypes.c_size_t,
+                                                  ctypes.POINTER(ctypes.c_int),
+                                                  ctypes.POINTER(ctypes.c_int),
+                                                  ctypes.POINTER(ctypes.c_int)]),
     "lgx_compute_primitive_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                  ctypes.POINTER(LgxPrimQuartet), ctypes.c_int,

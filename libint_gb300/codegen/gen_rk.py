@@ -44,6 +44,25 @@ VARIANTS = [("double", "kModeJK", RK_MAX_L, False), ("float", "kModeJK", RK_MAX_
             ("double", "kModeJK", RK_MAX_L, True), ("float", "kModeJK", RK_MAX_L, True)]
 N_UNITS = 24  # instantiation translation units (compiled in parallel)
 
+# __launch_bounds__ minimum blocks per SM of the J/K register kernels (0: the
+# compiler's own register target), per (precision, mode, class).  Kernels not
+# listed get 1 for FP64 classes with L >= 5 (left to itself the compiler
+# gives several of them 32 registers and 25-57 KB of spills per thread; with
+# 1 their serial (H2O)64 cc-pVTZ launches ran 14-29% faster), else 0.  The
+# listed ones: the spill-free settings that beat the compiler's choice by
+# 7-11% in a sweep of 0, 1, 3, 4, 6, 8 over tuned serial passes of
+# (H2O)64 cc-pVTZ.  Caps that make the FP32 kernels spill were faster in
+# serial passes but slower inside the graph pass, where the spills compete
+# for L2 with the concurrent launches ((ps|ps) of the mixed scheme at 8:
+# 434 GB of DRAM traffic and +40% time), so none is listed.
+MIN_BLOCKS = {
+    ("float", "kModeJK", (1, 0, 3, 0)): 4,
+    ("float", "kModeJK", (2, 0, 2, 0)): 4,
+    ("float", "kModeJKB64", (0, 0, 3, 3)): 3,
+}
+MODE_IDS = {"kModeStore": 0, "kModeSchwarz": 1, "kModeJK": 2, "kModeJKB64": 4,
+            "kModeStoreB64": 5}
+
 
 def comps(l):
     return [(lx, ly, l - lx - ly) for lx in range(l, -1, -1) for ly in range(l - lx, -1, -1)]
@@ -394,6 +413,20 @@ def main(out=OUT_DEFAULT):
     for c in classes:
         parts.append(gen_class(*c))
         parts.append("")
+    parts.append("// __launch_bounds__ minimum blocks per SM of the listed register kernels")
+    parts.append("// (gen_rk.py MIN_BLOCKS); -1: not listed.")
+    parts.append("constexpr int min_blocks_table(bool fp32, int mode, int la, int lb, int lc, "
+                 "int ld) {")
+    parts.append("  switch (((fp32 ? 1 : 0) * 8 + mode) * 4096 + ((la * 8 + lb) * 8 + lc) * 8 + "
+                 "ld) {")
+    for (prec, mode, c), v in sorted(MIN_BLOCKS.items()):
+        key = ((1 if prec == "float" else 0) * 8 + MODE_IDS[mode]) * 4096 + \
+            ((c[0] * 8 + c[1]) * 8 + c[2]) * 8 + c[3]
+        parts.append("    case %d: return %d;  // %s %s (%d%d|%d%d)" % (key, v, prec, mode, *c))
+    parts.append("    default: return -1;")
+    parts.append("  }")
+    parts.append("}")
+    parts.append("")
     parts.append("}  // namespace rk")
     parts.append("}  // namespace lgx")
     text = "\n".join(parts) + "\n"

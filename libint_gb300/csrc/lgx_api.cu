@@ -27,6 +27,7 @@ cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npair
                               double ln_prec, int method, cudaStream_t st);
 cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J,
                                double* K, int nbf, cudaStream_t st);
+cudaError_t launch_drop_pairs(PrimPairRec* pp, int n, double ln_prec, cudaStream_t st);
 size_t stage_bytes_per_warp(bool fp32, int rows);
 int eri_blocks_per_sm(int mode, bool fp32, int block, size_t smem);
 cudaError_t launch_d2f(const double* src, float* dst, long long n, cudaStream_t st);
@@ -2176,16 +2177,15 @@ lgx_status lgx_destroy(lgx_context* ctx) {
   return LGX_OK;
 }
 
-lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int deriv,
-                                double precision, int screening, double* out,
-                                size_t out_capacity, int* nsets, int* nvalues, int* is_null) {
-  if (!ctx) return LGX_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(ctx->mu);
-  if (!shells || !out || !nsets || !nvalues || !is_null)
-    return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
-  if (deriv == 2)
-    return shellset_deriv2(ctx, shells, precision, screening, out, out_capacity, nsets, nvalues,
-                           is_null);
+}  // extern "C"
+
+namespace {
+// One shell set (deriv 0 / 1) of four caller shells; pair_ln: NULL, or the
+// screening logarithms of the bra (shells 0, 1) and ket (shells 2, 3)
+// primitive pairs (a caller's ShellPair data) in place of ln(precision).
+lgx_status shellset_locked(lgx_context* ctx, const lgx_shell shells[4], int deriv,
+                           double precision, int screening, const double* pair_ln, double* out,
+                           size_t out_capacity, int* nsets, int* nvalues, int* is_null) {
   if (deriv < 0 || deriv > kMaxDeriv)
     return fail(ctx, LGX_ERR_INVALID_ARG, "deriv must be 0, 1 or 2");
   if (screening != LGX_SCREEN_ORIGINAL && screening != LGX_SCREEN_CONSERVATIVE)
@@ -2215,8 +2215,23 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int
   if (s != LGX_OK) return s;
   const double ln_prec =
       precision > 0 ? std::log(precision) : -std::numeric_limits<double>::max();
-  s = ensure_pairs(ctx, ctx->small, ln_prec, screening);
-  if (s != LGX_OK) return s;
+  if (!pair_ln) {
+    s = ensure_pairs(ctx, ctx->small, ln_prec, screening);
+    if (s != LGX_OK) return s;
+  } else {
+    // the table at the tighter of the two, then the other pair cut to its own
+    // (the small basis holds shells 0..3: pairs (1, 0) and (3, 2))
+    BasisDev& B = ctx->small;
+    const double lb = pair_ln[0], lk = pair_ln[1];
+    s = ensure_pairs(ctx, B, std::min(lb, lk), screening);
+    if (s != LGX_OK) return s;
+    const PairRec& pb = B.hpairs[pidx(1, 0)];
+    const PairRec& pk = B.hpairs[pidx(3, 2)];
+    PrimPairRec* pp = B.pprims.as<PrimPairRec>();
+    if (lb > lk) CK(launch_drop_pairs(pp + pb.pp_off, pb.npp, lb, ctx->stream));
+    if (lk > lb) CK(launch_drop_pairs(pp + pk.pp_off, pk.npp, lk, ctx->stream));
+    B.pairs_ok = lb == lk;  // a cut table is not reused
+  }
   CK(ctx->out.ensure(size_t(nv * ns) * sizeof(double)));
   CK(ctx->isnull.ensure(sizeof(int)));
   const int32_t q[4] = {0, 1, 2, 3};
@@ -2234,6 +2249,40 @@ lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int
   *nvalues = int(nv);
   *is_null = nul;
   return LGX_OK;
+}
+}  // namespace
+
+extern "C" {
+
+lgx_status lgx_compute_shellset(lgx_context* ctx, const lgx_shell shells[4], int deriv,
+                                double precision, int screening, double* out,
+                                size_t out_capacity, int* nsets, int* nvalues, int* is_null) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!shells || !out || !nsets || !nvalues || !is_null)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (deriv == 2)
+    return shellset_deriv2(ctx, shells, precision, screening, out, out_capacity, nsets, nvalues,
+                           is_null);
+  return shellset_locked(ctx, shells, deriv, precision, screening, nullptr, out, out_capacity,
+                         nsets, nvalues, is_null);
+}
+
+lgx_status lgx_compute_shellset_pairs(lgx_context* ctx, const lgx_shell shells[4], int deriv,
+                                      double precision, int screening,
+                                      const double pair_ln_prec[2], double* out,
+                                      size_t out_capacity, int* nsets, int* nvalues,
+                                      int* is_null) {
+  if (!ctx) return LGX_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!shells || !out || !nsets || !nvalues || !is_null || !pair_ln_prec)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "null argument");
+  if (deriv != 0 && deriv != 1)
+    return fail(ctx, LGX_ERR_INVALID_ARG, "caller pair data: deriv must be 0 or 1");
+  if (std::isnan(pair_ln_prec[0]) || std::isnan(pair_ln_prec[1]))
+    return fail(ctx, LGX_ERR_INVALID_ARG, "pair precision is NaN");
+  return shellset_locked(ctx, shells, deriv, precision, screening, pair_ln_prec, out,
+                         out_capacity, nsets, nvalues, is_null);
 }
 
 double lgx_solid_coeff(int l, int m, int lx, int ly, int lz) {

@@ -197,6 +197,23 @@ cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npair
   return cudaGetLastError();
 }
 
+// Drops the primitive pairs of one shell pair (n records) whose screening
+// logarithm is below ln_prec: the pair table built at a tighter precision,
+// cut to a caller's ShellPair data at ln_prec (shell.h:1138-1256).
+__global__ void drop_pairs_kernel(PrimPairRec* pp, int n, double ln_prec) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n && pp[t].ln_scr < ln_prec) {
+    pp[t].ln_scr = -1.0e300;
+    pp[t].fln_scr = -3.0e38f;
+  }
+}
+
+cudaError_t launch_drop_pairs(PrimPairRec* pp, int n, double ln_prec, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  drop_pairs_kernel<<<(n + 127) / 128, 128, 0, st>>>(pp, n, ln_prec);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J, double* K,
                                int nbf, cudaStream_t st) {
   const long long n = (long long)nbf * nbf;

@@ -287,22 +287,21 @@ __device__ __forceinline__ float rk_D(const EriArgs& a, size_t i, float*) {
 }
 
 // Blocks per SM the compiler has to allow for (__launch_bounds__; 0 = no
-// minimum, the compiler's own register target).  The mixed scheme's FP32
-// kernels of the smallest classes wait on FP64 results (the Boys function)
-// and gain from more resident warps: 8 blocks of 128 threads (at most 64
-// registers).  The FP64 instances with L >= 5 get 1: left to its own target
-// the compiler gives several of them 32 registers and 25-57 KB of spills per
-// thread (local memory the context has to reserve for every resident
-// thread), with 1 they keep up to 255 registers and spill 4-21 KB.
-template <typename T, int L, int MODE>
+// minimum, the compiler's own register target): the measured per-class
+// choice of the generator's table for the J/K kernels; otherwise 1 for the
+// FP64 classes with L >= 5, where the compiler left to itself gives several
+// instances 32 registers and 25-57 KB of spills per thread (local memory the
+// context reserves for every resident thread), else 0.
+template <typename T, int LA, int LB, int LC, int LD, int MODE, bool ATT>
 constexpr int rk_min_blocks() {
-  return (sizeof(T) == 4 && mode_b64(MODE) && L <= 2) ? 8 : (sizeof(T) == 8 && L >= 5 ? 1 : 0);
+  constexpr int t = ATT ? -1 : rk::min_blocks_table(sizeof(T) == 4, MODE, LA, LB, LC, LD);
+  return t >= 0 ? t : (sizeof(T) == 8 && LA + LB + LC + LD >= 5 ? 1 : 0);
 }
 
 // ATT: attenuated operator (erf / erfc, EriArgs::op), J/K mode only; the
 // Coulomb instances (ATT = false) carry none of its code.
 template <typename T, int LA, int LB, int LC, int LD, int MODE, bool ATT = false>
-__global__ void __launch_bounds__(128, (rk_min_blocks<T, LA + LB + LC + LD, MODE>()))
+__global__ void __launch_bounds__(128, (rk_min_blocks<T, LA, LB, LC, LD, MODE, ATT>()))
     rk_kernel(EriArgs a) {
   using C = rk::Cls<LA, LB, LC, LD>;
   constexpr int N0 = C::kN0, N1 = C::kN1, N2 = C::kN2, N3 = C::kN3;

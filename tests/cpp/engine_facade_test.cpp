@@ -104,6 +104,29 @@ int main(int argc, char** argv) {
     const size_t n = obs[q[0]].size() * obs[q[1]].size() * obs[q[2]].size() * obs[q[3]].size();
     for (size_t i = 0; i < n; ++i) put(r[0][i]);
   }
+  // precomputed ShellPair data, as compute_2body_fock passes it: pairs at
+  // the machine epsilon, the engine at 1e-10 (deriv 0 and 1)
+  {
+    const double ln_eps = std::log(std::numeric_limits<double>::epsilon());
+    libint2::Engine p0(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 0, 1e-10);
+    libint2::Engine p1(libint2::Operator::coulomb, obs.max_nprim(), obs.max_l(), 1, 1e-10);
+    for (const auto& q : q1) {
+      libint2::ShellPair sp12(obs[q[0]], obs[q[1]], ln_eps), sp34(obs[q[2]], obs[q[3]], ln_eps);
+      const size_t n =
+          obs[q[0]].size() * obs[q[1]].size() * obs[q[2]].size() * obs[q[3]].size();
+      const auto& r0 = p0.compute2<libint2::Operator::coulomb, libint2::BraKet::xx_xx, 0>(
+          obs[q[0]], obs[q[1]], obs[q[2]], obs[q[3]], &sp12, &sp34);
+      put(r0[0] == nullptr ? 0.0 : 1.0);
+      if (r0[0] != nullptr)
+        for (size_t i = 0; i < n; ++i) put(r0[0][i]);
+      const auto& r1 = p1.compute2<libint2::Operator::coulomb, libint2::BraKet::xx_xx, 1>(
+          obs[q[0]], obs[q[1]], obs[q[2]], obs[q[3]], &sp12, &sp34);
+      put(r1[0] == nullptr ? 0.0 : 1.0);
+      if (r1[0] != nullptr)
+        for (unsigned s = 0; s < p1.nshellsets(); ++s)
+          for (size_t i = 0; i < n; ++i) put(r1[s][i]);
+    }
+  }
   libint2::finalize();
   std::cout << "ok" << std::endl;
   return 0;

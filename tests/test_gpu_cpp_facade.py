@@ -95,4 +95,17 @@ def test_cpp_engine_facade(lgx, oracle_mod, tmp_path):
             pos += ref.size
     finally:
         oracle_mod.set_operator(0)
+    # compute2 with ShellPair data at the machine epsilon, engine at 1e-10
+    eps = float(np.finfo(float).eps)
+    for q in [(5, 3, 8, 0), (3, 5, 5, 9), (0, 14, 5, 3)]:
+        for deriv in (0, 1):
+            ref = oracle_mod.compute_quartet(ob, *q, deriv=deriv, precision=1e-10,
+                                             pair_precision=eps)
+            assert (vals[pos] == 0.0) == (ref is None)
+            pos += 1
+            if ref is None:
+                continue
+            r = np.concatenate([x.reshape(-1) for x in ref])
+            assert np.max(np.abs(vals[pos:pos + r.size] - r)) < 1e-12
+            pos += r.size
     assert pos == vals.size

@@ -113,6 +113,39 @@ def test_coarse_precision_vs_oracle(lgx, oracle_mod, precision):
             assert np.max(np.abs(got - ref[0])) < TOL, q
 
 
+def test_precomputed_shellpair_data_vs_oracle(lgx, oracle_mod, gpu_ctx):
+    # Engine::compute2 with ShellPair data precomputed at the machine epsilon
+    # and the engine at 1e-10 (engine.impl.h:1259-1276; compute_2body_fock
+    # passes such pairs, hartree-fock++.cc:1386-1425): the primitive pairs at
+    # eps, the primitive quartets screened at 1e-10 -- the oracle's
+    # pair_precision path
+    atoms = lgx.water_cluster(1, 1, 1, seed=3)
+    bs = lgx.BasisSet("cc-pVDZ", atoms)
+    ob = oracle_mod.OracleBasis.from_basis(bs)
+    eps, prec = np.finfo(float).eps, 1e-10
+    rng = np.random.default_rng(2)
+    ndiff = 0
+    for _ in range(60):
+        q = [int(x) for x in rng.integers(0, len(bs), 4)]
+        sh = [bs[i] for i in q]
+        for deriv in (0, 1):
+            got = gpu_ctx.compute_shellset(sh, deriv, prec, pair_ln_prec=(np.log(eps), np.log(eps)))
+            ref = oracle_mod.compute_quartet(ob, *q, deriv, precision=prec, pair_precision=eps)
+            assert (got is None) == (ref is None), q
+            if got is None:
+                continue
+            assert max(float(np.max(np.abs(g - r))) for g, r in zip(got, ref)) < TOL, (q, deriv)
+            plain = gpu_ctx.compute_shellset(sh, deriv, prec)
+            if plain is None or max(float(np.max(np.abs(g - p))) for g, p in zip(got, plain)) > 0:
+                ndiff += 1
+    print("sets that differ from pairs built at the engine precision:", ndiff)
+    # both at the engine precision: the plain call exactly
+    sh = [bs[i] for i in (3, 1, 4, 0)]
+    a = gpu_ctx.compute_shellset(sh, 0, prec, pair_ln_prec=(np.log(prec), np.log(prec)))
+    b = gpu_ctx.compute_shellset(sh, 0, prec)
+    assert (a is None and b is None) or np.array_equal(a[0], b[0])
+
+
 def test_compute_2body_fock_vs_oracle(lgx, oracle_mod):
     # the binding's Engine.compute_2body_fock(D, basis) (python/src/libint2/
     # engine.cc:230-279) through one GPU J/K pass: G = 2J - K
