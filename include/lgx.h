@@ -103,10 +103,16 @@ lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega);
  * evaluated on the GPU by exactly the device function a class kernel uses:
  * variant 0 the program kernels' FP64 evaluator (mmax <= 16), 1 the
  * register kernels' FP64 evaluator (mmax <= 6), 2 and 3 their FP32
- * counterparts, 4 and 5 the FP64 evaluators of 0 and 1 with each value
- * rounded to FP32, as the LGX_MIXED scheme's FP32 kernels use them (all
- * results widened to double).  The batch counterpart of
- * libint's FmEval_Taylor / FmEval_Chebyshev7 eval(F, T, mmax)
+ * counterparts, 4 and 5 the LGX_MIXED scheme's FP64 evaluators of the
+ * program and register kernels (5-term series, T as a double-float pair,
+ * each value rounded to FP32; mmax <= 16 and <= 6), 6 the register
+ * kernels' whole LGX_MIXED path from primitive-pair data: T then holds 8
+ * values per argument (Pb.x, Pb.y, Pb.z, zeta, Pk.x, Pk.y, Pk.z, eta;
+ * |P| <= 1e4, 1e-10 <= zeta <= 1e10) and the argument is rho |Pb - Pk|^2,
+ * rho = zeta eta / (zeta + eta), formed as those kernels form it
+ * (double-float records and arithmetic).  All results widened to double.
+ * The batch counterpart of libint's FmEval_Taylor / FmEval_Chebyshev7
+ * eval(F, T, mmax)
  * (include/libint2/boys.h:345-454,679-821), so the evaluators can be
  * checked against libint's reference values on their own. */
 lgx_status lgx_boys(lgx_context* ctx, int variant, const double* T, int64_t n, int mmax,

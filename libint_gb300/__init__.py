@@ -314,10 +314,14 @@ class Context:
 
     def boys(self, T, mmax: int, variant: int = 0):
         """F_0..F_mmax(T) for an array of T from the device evaluator
-        `variant` (lgx_boys: 0/1 FP64 program/register kernel, 2/3 FP32)."""
-        T = np.ascontiguousarray(T, np.float64).reshape(-1)
-        F = np.zeros((len(T), int(mmax) + 1))
-        self._check(self._lib.lgx_boys(self._h, int(variant), _lgx.ptr(T), len(T), int(mmax),
+        `variant` (lgx_boys: 0/1 FP64 program/register kernel, 2/3 FP32,
+        4/5 FP64 rounded to FP32; 6: T is an (n, 8) array of pair data
+        Pb.xyz, zeta, Pk.xyz, eta, the mixed register kernels' whole path)."""
+        T = np.ascontiguousarray(T, np.float64)
+        n = T.shape[0] if int(variant) == 6 else T.size
+        T = T.reshape(-1)
+        F = np.zeros((n, int(mmax) + 1))
+        self._check(self._lib.lgx_boys(self._h, int(variant), _lgx.ptr(T), n, int(mmax),
                                        _lgx.ptr(F)), "lgx_boys")
         return F
 

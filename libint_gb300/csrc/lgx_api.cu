@@ -23,8 +23,8 @@ namespace lgx {
 cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int block,
                        size_t smem, cudaStream_t st);
 cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npairs,
-                              PrimPairRec* pp, const int* pp_pair, long long npp,
-                              double ln_prec, int method, cudaStream_t st);
+                              PrimPairRec* pp, PrimPairJKds* ppds, const int* pp_pair,
+                              long long npp, double ln_prec, int method, cudaStream_t st);
 cudaError_t launch_jk_finalize(const double* Jacc, const double* Kacc, double* J,
                                double* K, int nbf, cudaStream_t st);
 cudaError_t launch_drop_pairs(PrimPairRec* pp, int n, double ln_prec, cudaStream_t st);
@@ -42,7 +42,7 @@ cudaError_t rk_launch(bool fp32, int mode, bool att, int la, int lb, int lc, int
                       long long work, int nsm, cudaStream_t st);
 bool rk_available(bool fp32, int mode, bool att, int la, int lb, int lc, int ld);
 cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
-                              PrimPairJK32* out, PrimPairJK64* out64, cudaStream_t st);
+                              PrimPairJK32* out, PrimPairJKds* outds, cudaStream_t st);
 cudaError_t post_launch(bool fp32, int mode, int la, int lb, int lc, int ld, const EriArgs& a,
                         int grid, int block, size_t smem, cudaStream_t st);
 int post_blocks_per_sm(bool fp32, int mode, int la, int lb, int lc, int ld, int block,
@@ -101,7 +101,7 @@ struct BasisDev {
   std::vector<PairRec> hpairs;
   std::vector<unsigned char> hswap;
   long long npp = 0;
-  DBuf pairs, pprims, pp_pair, pair_swap;
+  DBuf pairs, pprims, ppds, pp_pair, pair_swap;
   bool pairs_ok = false;
   unsigned long long pairs_version = 0;  // bumped whenever pprims is rewritten
   double pairs_lnprec = 0;
@@ -134,7 +134,7 @@ struct BinCache {
   DBuf class_lists;                 // pair ids of every pair class, sorted
   std::vector<long long> class_off; // offsets of each class in class_lists
   // FP32 records per list position (PrimPairJK32 layout) and their source
-  DBuf rec_idx, rec_src, recs, recs64;
+  DBuf rec_idx, rec_src, recs, recsds;
   long long nrec = 0;
   unsigned long long rec_version = ~0ull;  // pairs_version the records hold
   std::vector<std::unique_ptr<BinHost>> bins;
@@ -565,6 +565,7 @@ lgx_status upload_basis(lgx_context* ctx, BasisDev& B, int nshell, const int32_t
   CK(B.pairs.ensure(npairs * sizeof(PairRec)));
   CK(B.pp_pair.ensure(off * sizeof(int)));
   CK(B.pprims.ensure(off * sizeof(PrimPairRec)));
+  CK(B.ppds.ensure(off * sizeof(PrimPairJKds)));
   CK(B.pair_swap.ensure(npairs));
   CK(cudaMemcpyAsync(B.pairs.p, B.hpairs.data(), npairs * sizeof(PairRec),
                      cudaMemcpyHostToDevice, ctx->stream));
@@ -581,7 +582,7 @@ lgx_status ensure_jk_records(lgx_context* ctx, BasisDev& B) {
   BinCache& C = ctx->bins;
   if (C.rec_version == B.pairs_version) return LGX_OK;
   CK(launch_jk_records(B.pprims.as<PrimPairRec>(), C.rec_src.as<int>(), C.nrec,
-                       C.recs.as<PrimPairJK32>(), C.recs64.as<PrimPairJK64>(), ctx->stream));
+                       C.recs.as<PrimPairJK32>(), C.recsds.as<PrimPairJKds>(), ctx->stream));
   C.rec_version = B.pairs_version;
   return LGX_OK;
 }
@@ -589,8 +590,8 @@ lgx_status ensure_jk_records(lgx_context* ctx, BasisDev& B) {
 lgx_status ensure_pairs(lgx_context* ctx, BasisDev& B, double ln_prec, int method) {
   if (B.pairs_ok && B.pairs_lnprec == ln_prec && B.pairs_method == method) return LGX_OK;
   CK(launch_shellpairs(B.dev, B.pairs.as<PairRec>(), int(B.hpairs.size()),
-                       B.pprims.as<PrimPairRec>(), B.pp_pair.as<int>(), B.npp, ln_prec,
-                       method, ctx->stream));
+                       B.pprims.as<PrimPairRec>(), B.ppds.as<PrimPairJKds>(),
+                       B.pp_pair.as<int>(), B.npp, ln_prec, method, ctx->stream));
   B.pairs_ok = true;
   ++B.pairs_version;
   B.pairs_lnprec = ln_prec;
@@ -678,6 +679,7 @@ void fill_common(const lgx_context* ctx, const BasisDev& B, EriArgs& a) {
   a.basis = B.dev;
   a.pairs = B.pairs.as<PairRec>();
   a.pprims = B.pprims.as<PrimPairRec>();
+  a.ppds = B.ppds.as<PrimPairJKds>();
   a.pair_swap = B.pair_swap.as<unsigned char>();
   a.boys = ctx->boys.as<double>();
   a.boys_tay = ctx->boys_tay.as<double>();
@@ -1163,7 +1165,7 @@ lgx_status build_bins(lgx_context* ctx, BasisDev& B, double thresh, int mode, do
     CK(C.rec_idx.ensure(idx.size() * sizeof(int2)));
     CK(C.rec_src.ensure(std::max<size_t>(1, src.size()) * sizeof(int)));
     CK(C.recs.ensure(std::max<size_t>(1, src.size()) * sizeof(PrimPairJK32)));
-    CK(C.recs64.ensure(std::max<size_t>(1, src.size()) * sizeof(PrimPairJK64)));
+    CK(C.recsds.ensure(std::max<size_t>(1, src.size()) * sizeof(PrimPairJKds)));
     CK(cudaMemcpyAsync(C.rec_idx.p, idx.data(), idx.size() * sizeof(int2),
                        cudaMemcpyHostToDevice, ctx->stream));
     if (!src.empty())
@@ -1314,7 +1316,7 @@ int tune_key(const BinHost& bin, int deriv, int mode, bool fp32, int op) {
 void bin_args(const BinCache& C, const BinHost& bin, int sp, EriArgs& a) {
   a.implicit = 1;
   a.jk32 = C.recs.as<PrimPairJK32>();
-  a.jk64 = C.recs64.as<PrimPairJK64>();
+  a.jkds = C.recsds.as<PrimPairJKds>();
   a.bin.bra_rec = C.rec_idx.as<int2>() + C.class_off[bin.bra_class];
   a.bin.ket_rec = C.rec_idx.as<int2>() + C.class_off[bin.ket_class];
   a.bin.bra_pairs = C.class_lists.as<int>() + C.class_off[bin.bra_class];
@@ -2734,20 +2736,32 @@ lgx_status lgx_boys(lgx_context* ctx, int variant, const double* T, int64_t n, i
                     double* F) {
   if (!ctx) return LGX_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(ctx->mu);
-  if (variant < 0 || variant > 5) return fail(ctx, LGX_ERR_INVALID_ARG, "bad Boys variant");
-  const int mmax_cap = (variant == 1 || variant == 3 || variant == 5) ? 6 : kBoysMaxM;
+  if (variant < 0 || variant > 6) return fail(ctx, LGX_ERR_INVALID_ARG, "bad Boys variant");
+  const int mmax_cap = (variant == 1 || variant == 3 || variant >= 5) ? 6 : kBoysMaxM;
   if (mmax < 0 || mmax > mmax_cap)
     return fail(ctx, LGX_ERR_INVALID_ARG, "mmax out of range for this evaluator");
   if (n < 0 || (n > 0 && (!T || !F))) return fail(ctx, LGX_ERR_INVALID_ARG, "bad arrays");
   if (n == 0) return LGX_OK;
-  for (int64_t i = 0; i < n; ++i)  // the table lookup needs 0 <= T (NaN rejected too)
-    if (!(T[i] >= 0.0) || !std::isfinite(T[i]))
-      return fail(ctx, LGX_ERR_INVALID_ARG, "Boys argument T must be finite and >= 0");
+  const int64_t nin = variant == 6 ? 8 * n : n;  // variant 6: pair data per argument
+  if (variant == 6) {
+    // |P| <= 1e4 bohr, 1e-10 <= zeta <= 1e10: the double-float records'
+    // range (and a Boys argument that stays finite)
+    for (int64_t i = 0; i < n; ++i)
+      for (int c = 0; c < 8; ++c) {
+        const double v = T[8 * i + c];
+        const bool ok = (c % 4 == 3) ? (v >= 1e-10 && v <= 1e10) : (std::fabs(v) <= 1e4);
+        if (!ok) return fail(ctx, LGX_ERR_INVALID_ARG, "pair data out of range");
+      }
+  } else {
+    for (int64_t i = 0; i < n; ++i)  // the table lookup needs 0 <= T (NaN rejected too)
+      if (!(T[i] >= 0.0) || !std::isfinite(T[i]))
+        return fail(ctx, LGX_ERR_INVALID_ARG, "Boys argument T must be finite and >= 0");
+  }
   CK(cudaSetDevice(ctx->device));
   const size_t nf = size_t(n) * (mmax + 1);
-  CK(ctx->boysT.ensure(size_t(n) * sizeof(double)));
+  CK(ctx->boysT.ensure(size_t(nin) * sizeof(double)));
   CK(ctx->boysF.ensure(nf * sizeof(double)));
-  CK(cudaMemcpyAsync(ctx->boysT.p, T, size_t(n) * sizeof(double), cudaMemcpyHostToDevice,
+  CK(cudaMemcpyAsync(ctx->boysT.p, T, size_t(nin) * sizeof(double), cudaMemcpyHostToDevice,
                      ctx->stream));
   CK(launch_boys_eval(ctx->boys.as<double>(), ctx->boys_tay.as<double>(), ctx->boys32.as<float>(),
                       ctx->inv_odd.as<double>(), variant, ctx->boysT.as<double>(), n, mmax,

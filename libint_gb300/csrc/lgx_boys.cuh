@@ -84,23 +84,25 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T
   rk_boys_core<MMAX>(tay, T, T > kBoysTmax, k, md, pfac, F);
 }
 
-// The mixed scheme's FP64 Boys function of an FP32 quartet, given the FP64
-// argument T and its FP32 value Tf (which the FP32 prologue has): the branch
-// and the grid point come from Tf (integer and FP32 operations), only the
-// offset md = T_k - T in FP64.  Tf and T differ by ~1e-6 relative at most,
-// so the grid point may be the neighbour of T's nearest one (|md| <= 1/64 +
-// 3e-5: Taylor remainder still below 5e-17), and near T = 50 either branch
-// is exact (the asymptotic one drops Q(m+1/2, T) < 2e-15); Tf <= 50 gives
-// k <= 1600 < kBoysRows.  The values are rounded to FP32 next, so the
-// series stop at 5 terms: relative error below 7.8e-12 (|md| <= 1/64 +
-// 3e-5), four orders under the FP32 half-ulp.
+// The mixed scheme's FP64 Boys function of an FP32 quartet, given its
+// argument T = T.hi + T.lo in double-float (ds_boys_arg): the branch and the
+// grid point come from T.hi; the offset md = T_k - T = (T_k - T.hi) - T.lo,
+// where T_k - T.hi is exact in FP32 (T_k = k/32 and T.hi are within a
+// factor 2 of each other for k >= 1, Sterbenz; 0 - T.hi for k = 0), both
+// parts converted to FP64 with integer operations and subtracted in FP64;
+// T itself in FP64 (one addition) for the asymptotic branch and the
+// recursion.  T.hi <= 50 gives k <= 1600 < kBoysRows, and near T = 50 either
+// branch is exact (the asymptotic one drops Q(m+1/2, T) < 2e-15).  The
+// values are rounded to FP32 next, so the series stop at 5 terms: relative
+// error below 7.8e-12 (|md| <= 1/64), four orders under the FP32 half-ulp.
 template <int MMAX>
-__device__ __forceinline__ void rk_boys_b64(const double* __restrict__ tay, double T, float Tf,
-                                            double* F) {
-  const bool asym = Tf > float(kBoysTmax);
-  const int k = asym ? 0 : __float2int_rn(Tf * float(kBoysInvDT));
-  const double md = fma(i2d_int(k), kBoysDT, -T);
-  rk_boys_core<MMAX, false, 5>(tay, T, asym, k, md, 1.0, F);
+__device__ __forceinline__ void rk_boys_b64(const double* __restrict__ tay, dsf T, double* F) {
+  const bool asym = T.hi > float(kBoysTmax);
+  const int k = asym ? 0 : __float2int_rn(T.hi * float(kBoysInvDT));
+  const float mdh = __fadd_rn(__fmul_rn(float(k), float(kBoysDT)), -T.hi);
+  const double md = f2d_int(mdh) - f2d_int(T.lo);
+  const double T64 = f2d_int(T.hi) + f2d_int(T.lo);
+  rk_boys_core<MMAX, false, 5>(tay, T64, asym, k, md, 1.0, F);
 }
 
 template <int MMAX>

@@ -115,13 +115,79 @@ struct __align__(16) PrimPairJK32 {
 };
 static_assert(sizeof(PrimPairJK32) == 32, "PrimPairJK32 layout");
 
-// FP64 companion of a PrimPairJK32 record (same index): the pair centre P
-// and the exponent sum zeta, for the FP64 Boys argument of the mixed scheme.
-struct __align__(16) PrimPairJK64 {
-  double P[3];
-  double zeta;
+// Double-float companion of a PrimPairJK32 record (same index), for the
+// mixed scheme's Boys argument: the pair centre P and the exponent sum
+// zeta, each as hi = the FP32 rounding of the FP64 value and lo = the FP32
+// rounding of the remainder (48 significant bits: |value - hi - lo| <=
+// 2^-48 |value|).
+struct __align__(16) PrimPairJKds {
+  float4 hi;  // P.x, P.y, P.z, zeta
+  float4 lo;
 };
-static_assert(sizeof(PrimPairJK64) == 32, "PrimPairJK64 layout");
+static_assert(sizeof(PrimPairJKds) == 32, "PrimPairJKds layout");
+
+// The double-float record of one primitive pair (centre P, exponent sum).
+__device__ __forceinline__ PrimPairJKds make_jkds(double px, double py, double pz, double zeta) {
+  const float hx = float(px), hy = float(py), hz = float(pz), hw = float(zeta);
+  PrimPairJKds r;
+  r.hi = make_float4(hx, hy, hz, hw);
+  r.lo = make_float4(float(px - double(hx)), float(py - double(hy)), float(pz - double(hz)),
+                     float(zeta - double(hw)));
+  return r;
+}
+
+// Double-float arithmetic ("ds": value = hi + lo with |lo| <= ulp(hi)/2)
+// from the error-free transformations of Knuth (two-sum), Dekker
+// (fast two-sum) and the FMA two-product; __fadd_rn / __fmul_rn keep the
+// compiler from contracting the steps whose rounding errors they recover.
+struct dsf {
+  float hi, lo;
+};
+__device__ __forceinline__ dsf ds_fast_two_sum(float a, float b) {  // |a| >= |b| or a = 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fadd_rn(b, -__fadd_rn(s, -a))};
+}
+__device__ __forceinline__ dsf ds_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fadd_rn(s, -a);
+  return {s, __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb))};
+}
+// (two-sum also in the final normalisation: after cancellation of the
+// high parts the low parts can be the larger)
+__device__ __forceinline__ dsf ds_add(dsf a, dsf b) {
+  const dsf s = ds_two_sum(a.hi, b.hi);
+  return ds_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dsf ds_sub(dsf a, dsf b) { return ds_add(a, {-b.hi, -b.lo}); }
+__device__ __forceinline__ dsf ds_mul(dsf a, dsf b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = fmaf(a.hi, b.hi, -p);
+  return ds_fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ dsf ds_sqr(dsf a) {
+  const float p = __fmul_rn(a.hi, a.hi);
+  const float e = fmaf(a.hi, a.hi, -p);
+  return ds_fast_two_sum(p, fmaf(2.0f * a.hi, a.lo, e));
+}
+
+// T = rho |P - Q|^2 of one primitive quartet in double-float arithmetic
+// from the two pairs' double-float P and zeta (b: bra, k: ket).  rho =
+// zeta eta / (zeta + eta) is the FP32 value rho0 (any estimate within
+// ~1e-6) plus the correction (zeta eta - rho0 (zeta + eta)) * oogpq, the
+// residual formed to 2^-46 and the correction (relative size ~1e-7) scaled
+// in FP32 with the FP32 1/(zeta + eta); relative error of rho ~1e-13.  The
+// representation of P (2^-48 |P|) bounds |P - Q| to ~4e-13 absolute for
+// |P| <= 50 bohr; T to ~2^-44 relative beyond that.
+__device__ __forceinline__ dsf ds_boys_arg(const float4& bh, const float4& bl, const float4& kh,
+                                           const float4& kl, float rho0, float oogpq) {
+  const dsf zb = {bh.w, bl.w}, zk = {kh.w, kl.w};
+  const dsf r = ds_sub(ds_mul(zb, zk), ds_mul({rho0, 0.0f}, ds_add(zb, zk)));
+  const dsf rho = ds_fast_two_sum(rho0, __fmul_rn(r.hi, oogpq));
+  const dsf dx = ds_sub({bh.x, bl.x}, {kh.x, kl.x});
+  const dsf dy = ds_sub({bh.y, bl.y}, {kh.y, kl.y});
+  const dsf dz = ds_sub({bh.z, bl.z}, {kh.z, kl.z});
+  return ds_mul(rho, ds_add(ds_add(ds_sqr(dx), ds_sqr(dy)), ds_sqr(dz)));
+}
 
 // A shell pair with its primitive-pair range (pair list, shell.h:1079-1329).
 struct PairRec {

@@ -9,7 +9,8 @@ namespace lgx {
 // ShellPair::init for every pair (s1 >= s2) of the basis, one thread per
 // primitive pair (shell.h:1138-1256, Original/Conservative screening).
 __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, PrimPairRec* pp,
-                                 const int* pp_pair, long long npp, double ln_prec, int method) {
+                                 PrimPairJKds* ppds, const int* pp_pair, long long npp,
+                                 double ln_prec, int method) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= npp) return;
   const int pi = pp_pair[t];
@@ -76,13 +77,14 @@ __global__ void shellpair_kernel(DevBasis b, const PairRec* pairs, int npairs, P
   r.fnonsph = float(nonsph);
   r.pad = 0.f;
   pp[t] = r;
+  ppds[t] = make_jkds(r.P[0], r.P[1], r.P[2], gamma);
 }
 
 // FP32 J/K records: record r takes primitive pair src[r] & 0x7fffffff,
 // oriented on its second centre when the sign bit is set.
 __global__ void jk_records_kernel(const PrimPairRec* __restrict__ pp, const int* __restrict__ src,
                                   long long n, PrimPairJK32* __restrict__ out,
-                                  PrimPairJK64* __restrict__ out64) {
+                                  PrimPairJKds* __restrict__ outds) {
   const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (r >= n) return;
   const unsigned v = unsigned(src[r]);
@@ -93,20 +95,15 @@ __global__ void jk_records_kernel(const PrimPairRec* __restrict__ pp, const int*
   o.pa = sw ? make_float4(q.fPA2[0], q.fPA2[1], q.fPA2[2], q.fnonsph)
             : make_float4(q.fPA1[0], q.fPA1[1], q.fPA1[2], q.fnonsph);
   out[r] = o;
-  PrimPairJK64 o64;
-  o64.P[0] = q.P[0];
-  o64.P[1] = q.P[1];
-  o64.P[2] = q.P[2];
-  o64.zeta = q.zeta;
-  out64[r] = o64;
+  outds[r] = make_jkds(q.P[0], q.P[1], q.P[2], q.zeta);
 }
 
 cudaError_t launch_jk_records(const PrimPairRec* pp, const int* src, long long n,
-                              PrimPairJK32* out, PrimPairJK64* out64, cudaStream_t st) {
+                              PrimPairJK32* out, PrimPairJKds* outds, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int block = 256;
   jk_records_kernel<<<(unsigned)((n + block - 1) / block), block, 0, st>>>(pp, src, n, out,
-                                                                           out64);
+                                                                           outds);
   return cudaGetLastError();
 }
 
@@ -187,13 +184,13 @@ cudaError_t launch_eri(const EriArgs& a, int mode, bool fp32, int grid, int bloc
 }
 
 cudaError_t launch_shellpairs(const DevBasis& b, const PairRec* pairs, int npairs,
-                              PrimPairRec* pp, const int* pp_pair, long long npp,
-                              double ln_prec, int method, cudaStream_t st) {
+                              PrimPairRec* pp, PrimPairJKds* ppds, const int* pp_pair,
+                              long long npp, double ln_prec, int method, cudaStream_t st) {
   if (npp == 0) return cudaSuccess;
   const int block = 256;
   const long long grid = (npp + block - 1) / block;
-  shellpair_kernel<<<(unsigned)grid, block, 0, st>>>(b, pairs, npairs, pp, pp_pair, npp, ln_prec,
-                                                     method);
+  shellpair_kernel<<<(unsigned)grid, block, 0, st>>>(b, pairs, npairs, pp, ppds, pp_pair, npp,
+                                                     ln_prec, method);
   return cudaGetLastError();
 }
 

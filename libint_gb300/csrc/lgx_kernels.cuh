@@ -99,8 +99,9 @@ struct EriArgs {
   DevBasis basis;
   const PairRec* pairs;
   const PrimPairRec* pprims;
+  const PrimPairJKds* ppds;  // double-float P and zeta per primitive pair (pprims index)
   const PrimPairJK32* jk32;  // J/K bins: coalesced FP32 records (may be null)
-  const PrimPairJK64* jk64;  // J/K bins: their FP64 P and zeta (same layout)
+  const PrimPairJKds* jkds;  // J/K bins: their double-float P and zeta (same layout)
   const unsigned char* pair_swap;  // per pair: 1 if its canonical bra1 is s2
   DevProg prog;
   const double* boys;     // [kBoysRows][kBoysCols] F_m(T_k)

@@ -218,18 +218,19 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
 // One primitive quartet into acc (FP32 VRR) with the Boys function in FP64
 // (the kModeJKB64 / kModeStoreB64 kernels of the mixed scheme).  The
 // screening, prefactor and VRR geometry are the FP32 ones of rk_prim above;
-// T = rho |P - Q|^2 is formed in FP64 from the pairs' FP64 centres and
-// exponent sums, with rho = zeta eta / (zeta + eta) the FP32 value refined by
-// one Newton step on (zeta + eta) rho - zeta eta = 0 (relative error below
-// 1e-13); F_m(T) comes from the FP64 evaluator (Taylor with the downward
-// recursion and e^{-T}, or the asymptotic branch; the branch and grid point
-// from the FP32 T, rk_boys_b64) and is rounded to FP32 with integer
-// operations before the FP32 pfac.
+// the Boys argument T = rho |P - Q|^2 is formed in double-float arithmetic
+// from the bins' double-float records bds / kds (ds_boys_arg: FP32
+// operations, relative error ~1e-13), or, for explicit quartet lists, in
+// FP64 from the primitive-pair table (rho refined from its FP32 value by one
+// Newton step); F_m(T) comes from the FP64 evaluator (Taylor with the
+// downward recursion and e^{-T}, or the asymptotic branch, rk_boys_b64) and
+// is rounded to FP32 with integer operations before the FP32 pfac.
 template <class C>
 __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<float>& q,
-                                            const PrimF32& bp, const PrimF32& kp, const double* Pb,
-                                            double zb, const double* Pk, double zk, int bidx,
-                                            int kidx, const PrimScreen& scr, float* acc) {
+                                            const PrimF32& bp, const PrimF32& kp,
+                                            const PrimPairJKds* bds, const PrimPairJKds* kds,
+                                            int bidx, int kidx, const PrimScreen& scr,
+                                            float* acc) {
   if (!ln_kept(a, bp.k.w + kp.k.w, bidx, kidx, scr)) return false;
   const float zeta = bp.k.y, eta = kp.k.y;
   const float gpq = zeta + eta;
@@ -242,13 +243,23 @@ __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<fl
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
               PQz = PA[2] - QC[2] + q.AC[2];
   const float rho = zeta * eta * oogpq;
-  const float Tf = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
-  const double r0 = f2d_int(rho);
-  const double rho64 = fma(-fma(zb + zk, r0, -(zb * zk)), f2d_int(oogpq), r0);
-  const double X = Pb[0] - Pk[0], Y = Pb[1] - Pk[1], Z = Pb[2] - Pk[2];
-  const double T64 = rho64 * fma(X, X, fma(Y, Y, Z * Z));
+  dsf T;
+  if (bds) {
+    T = ds_boys_arg(__ldg(&bds->hi), __ldg(&bds->lo), __ldg(&kds->hi), __ldg(&kds->lo), rho,
+                    oogpq);
+  } else {
+    const PrimPairRec& b64 = a.pprims[bidx];
+    const PrimPairRec& k64 = a.pprims[kidx];
+    const double zb = b64.zeta, zk = k64.zeta;
+    const double r0 = f2d_int(rho);
+    const double rho64 = fma(-fma(zb + zk, r0, -(zb * zk)), f2d_int(oogpq), r0);
+    const double X = b64.P[0] - k64.P[0], Y = b64.P[1] - k64.P[1], Z = b64.P[2] - k64.P[2];
+    const double T64 = rho64 * fma(X, X, fma(Y, Y, Z * Z));
+    T.hi = d2f_int(T64);
+    T.lo = d2f_int(T64 - f2d_int(T.hi));
+  }
   double F64[C::kMmax + 1];
-  rk_boys_b64<C::kMmax>(a.boys_tay, T64, Tf, F64);
+  rk_boys_b64<C::kMmax>(a.boys_tay, T, F64);
   float F[C::kMmax + 1];
 #pragma unroll
   for (int m = 0; m <= C::kMmax; ++m) F[m] = d2f_int(F64[m]) * pfac;
@@ -377,20 +388,11 @@ __global__ void __launch_bounds__(128, (rk_min_blocks<T, LA, LB, LC, LD, MODE, A
         const PrimF32 kp = rec ? rk_rec32(a.jk32 + krec.x + ik * krec.y)
                                : rk_pp32(a.pprims[q.ket_pp + ik], q.ksw);
         if constexpr (mode_b64(MODE)) {
-          double Pb[3], Pk[3], zb, zk;
-          if (rec) {
-            const PrimPairJK64& b64 = a.jk64[brec.x + ib * brec.y];
-            const PrimPairJK64& k64 = a.jk64[krec.x + ik * krec.y];
-            Pb[0] = b64.P[0]; Pb[1] = b64.P[1]; Pb[2] = b64.P[2]; zb = b64.zeta;
-            Pk[0] = k64.P[0]; Pk[1] = k64.P[1]; Pk[2] = k64.P[2]; zk = k64.zeta;
-          } else {
-            const PrimPairRec& b64 = a.pprims[q.bra_pp + ib];
-            const PrimPairRec& k64 = a.pprims[q.ket_pp + ik];
-            Pb[0] = b64.P[0]; Pb[1] = b64.P[1]; Pb[2] = b64.P[2]; zb = b64.zeta;
-            Pk[0] = k64.P[0]; Pk[1] = k64.P[1]; Pk[2] = k64.P[2]; zk = k64.zeta;
-          }
-          kept += rk_prim_b64<C>(a, q, bp, kp, Pb, zb, Pk, zk, q.bra_pp + ib, q.ket_pp + ik,
-                                 scr, acc) ? 1 : 0;
+          const PrimPairJKds* bds = rec ? a.jkds + brec.x + ib * brec.y : nullptr;
+          const PrimPairJKds* kds = rec ? a.jkds + krec.x + ik * krec.y : nullptr;
+          kept += rk_prim_b64<C>(a, q, bp, kp, bds, kds, q.bra_pp + ib, q.ket_pp + ik, scr, acc)
+                      ? 1
+                      : 0;
         } else {
           kept += rk_prim<C, ATT>(a, q, bp, kp, q.bra_pp + ib, q.ket_pp + ik, scr, acc) ? 1 : 0;
         }

@@ -86,6 +86,58 @@ __device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
   }
 }
 
+// The mixed scheme's FP64 Boys function for the program kernels' FP32
+// quartets (runtime mmax <= kBoysMaxM), from the double-float argument
+// T = T.hi + T.lo (ds_boys_arg) and rounded to FP32 with integer operations,
+// times the FP32 prefactor.  T <= 50: F_mmax by the 5-term Taylor series of
+// the pre-divided table (the register kernels' rows) about T_k, e^{-T} as
+// e^{-T_k} (the table's spare slot) times the 5-term series of e^{T_k - T},
+// the downward recursion in FP64; relative error below 7.8e-12 before the
+// rounding (|T_k - T| <= 1/64), with md = (T_k - T.hi) - T.lo exact in FP32
+// for its first part (Sterbenz).  T > 50: F_0 = sqrt(pi/T)/2 and the upward
+// recursion with its e^{-T} terms (they reach ~3e-8 of F_16 at T = 50).
+__device__ __forceinline__ void boys_b64_stage(const double* __restrict__ tay,
+                                               const double* __restrict__ inv_odd, dsf T,
+                                               int mmax, float pfac, float* __restrict__ F) {
+  const double T64 = f2d_int(T.hi) + f2d_int(T.lo);
+  if (T.hi > float(kBoysTmax)) {
+    const double eT = exp(-T64);
+    const double rs = rsqrt(T64);
+    double f = 0.88622692545275801365 * rs;
+    F[0] = d2f_int(f) * pfac;
+    const double oo2T = 0.5 * (rs * rs);
+    for (int m = 0; m < mmax; ++m) {
+      f = ((2 * m + 1) * f - eT) * oo2T;
+      F[m + 1] = d2f_int(f) * pfac;
+    }
+    return;
+  }
+  const int k = __float2int_rn(T.hi * float(kBoysInvDT));
+  const float mdh = __fadd_rn(__fmul_rn(float(k), float(kBoysDT)), -T.hi);
+  const double md = f2d_int(mdh) - f2d_int(T.lo);
+  const double* row = tay + size_t(k) * (kBoysMaxM + 1) * kBoysTaylorStride;
+  const double* c = row + mmax * kBoysTaylorStride;
+  double s = __ldg(c + 4);
+  s = fma(s, md, __ldg(c + 3));
+  s = fma(s, md, __ldg(c + 2));
+  s = fma(s, md, __ldg(c + 1));
+  s = fma(s, md, __ldg(c + 0));
+  F[mmax] = d2f_int(s) * pfac;
+  if (mmax > 0) {
+    double e = 1.0 / 24.0;
+    e = fma(e, md, 1.0 / 6.0);
+    e = fma(e, md, 0.5);
+    e = fma(e, md, 1.0);
+    e = fma(e, md, 1.0);
+    const double eT = __ldg(row + 7) * e;  // e^{-T_k} e^{T_k - T}
+    const double twoT = 2.0 * T64;
+    for (int m = mmax - 1; m >= 0; --m) {
+      s = fma(twoT, s, eT) * __ldg(inv_odd + m);
+      F[m] = d2f_int(s) * pfac;
+    }
+  }
+}
+
 // FP32 Boys (4-term Taylor on the same grid, FP32 recursion).
 __device__ __forceinline__ void boys_to_stage(const float* __restrict__ tab, float T, int mmax,
                                               float pfac, float* __restrict__ F) {
@@ -273,9 +325,10 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<dou
 }
 
 // B64: the mixed scheme's Boys function in FP64 (kModeJKB64 /
-// kModeStoreB64): T = rho |P - Q|^2 from the FP64 pair data, with
-// 1/(zeta + eta) the FP32 value refined by one Newton step (relative error
-// below 1e-13), and F_m(T) from the FP64 evaluator, rounded to FP32.
+// kModeStoreB64): T = rho |P - Q|^2 in double-float arithmetic from the
+// primitive pairs' double-float records (ds_boys_arg, relative error
+// ~1e-13) and F_m(T) from the FP64 evaluator (boys_b64_stage), rounded to
+// FP32.
 template <bool ATT, bool B64 = false>
 __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<float>& g, int idx,
                                          double npbraket, float* st) {
@@ -299,12 +352,11 @@ __device__ __forceinline__ bool prologue(const EriArgs& a, const QuartetGeom<flo
   const float rho = zeta * eta * oogpq;
   const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
   if constexpr (B64) {
-    const double g64 = bp.zeta + kp.zeta;
-    double r64 = f2d_int(oogpq);
-    r64 = fma(r64, fma(-g64, r64, 1.0), r64);
-    const double X = bp.P[0] - kp.P[0], Y = bp.P[1] - kp.P[1], Z = bp.P[2] - kp.P[2];
-    const double T64 = (bp.zeta * kp.zeta) * r64 * fma(X, X, fma(Y, Y, Z * Z));
-    boys_to_stage(a.boys, a.inv_odd, T64, a.prog.mmax, pfac, st + kStF);
+    const PrimPairJKds* bd = a.ppds + g.bra_pp + ib;
+    const PrimPairJKds* kd = a.ppds + g.ket_pp + ik;
+    const dsf T64 = ds_boys_arg(__ldg(&bd->hi), __ldg(&bd->lo), __ldg(&kd->hi), __ldg(&kd->lo),
+                                rho, oogpq);
+    boys_b64_stage(a.boys_tay, a.inv_odd, T64, a.prog.mmax, pfac, st + kStF);
   } else if constexpr (ATT) {
     if (a.op != 1) boys_to_stage(a.boys32, T, a.prog.mmax, pfac, st + kStF);
     attenuate<float>(a, T, rho, a.prog.mmax, pfac, st + kStF);

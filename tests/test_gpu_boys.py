@@ -71,12 +71,10 @@ def test_boys_rejects_bad_arguments(gpu_ctx, lgx):
 @pytest.mark.parametrize("v64,vb,mmax", [(0, 4, 16), (1, 5, 6)])
 def test_mixed_scheme_boys_is_fp64_rounded_to_fp32(gpu_ctx, v64, vb, mmax):
     # the LGX_MIXED scheme's FP32 kernels take FP64 Boys values rounded to
-    # nearest FP32 (integer-only conversion).  The program kernels' values
-    # are exactly numpy's float32 rounding of the FP64 evaluator's (wherever
-    # those are FP32 normals); the register kernels pick the Taylor grid
-    # point from the FP32 argument and stop the series at 5 terms (relative
-    # error below 7.8e-12), so their value may, rarely, round to the
-    # neighbouring float32
+    # nearest FP32 (integer-only conversion).  Both evaluators (program and
+    # register kernels) stop the FP64 series at 5 terms (relative error
+    # below 7.8e-12) and take T as a double-float pair, so their value may,
+    # rarely, round to the neighbouring float32 of the FP64 evaluator's
     rng = np.random.default_rng(13)
     T = np.concatenate([load("boys.npz")["T"], rng.uniform(0, 60, 4000),
                         rng.uniform(60, 2000, 500)])
@@ -85,9 +83,40 @@ def test_mixed_scheme_boys_is_fp64_rounded_to_fp32(gpu_ctx, v64, vb, mmax):
     normal = np.abs(F64) >= np.finfo(np.float32).tiny
     want = F64[normal].astype(np.float32)
     got = Fb[normal].astype(np.float32)
-    if vb == 4:
-        np.testing.assert_array_equal(got, want)
-    else:
-        ulps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
-        assert ulps.max() <= 1 and np.mean(ulps == 0) > 0.999, (ulps.max(), np.mean(ulps == 0))
+    ulps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    assert ulps.max() <= 1 and np.mean(ulps == 0) > 0.999, (ulps.max(), np.mean(ulps == 0))
     assert np.all(Fb[~normal & (np.abs(F64) < 0.5 * np.finfo(np.float32).tiny)] == 0.0)
+
+
+@pytest.mark.parametrize("mmax", [0, 1, 2, 4, 6])
+def test_mixed_register_path_from_pair_data(gpu_ctx, oracle_mod, mmax):
+    # the LGX_MIXED register kernels' whole Boys path from primitive-pair data
+    # (lgx_boys variant 6): double-float records of P and zeta, the
+    # double-float argument T = rho |Pb - Pk|^2, the FP64 evaluator, the FP32
+    # rounding; against the oracle's F_m at the argument formed in extended
+    # precision: within 1 FP32 ulp and almost always its rounding
+    rng = np.random.default_rng(14 + mmax)
+    n = 6000
+    zb = np.exp(rng.uniform(np.log(0.05), np.log(3e4), n))
+    zk = np.exp(rng.uniform(np.log(0.05), np.log(3e4), n))
+    Pb = rng.uniform(-30.0, 30.0, (n, 3))
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    d = np.exp(rng.uniform(np.log(1e-4), np.log(40.0), n))
+    d[:50] = 0.0  # coincident centres: T = 0
+    Pk = Pb + d[:, None] * u
+    pairs = np.column_stack([Pb, zb, Pk, zk])
+    # the argument from the same double inputs, in extended precision
+    L = np.longdouble
+    dd = (Pb.astype(L) - Pk.astype(L))
+    T = (zb.astype(L) * zk.astype(L) / (zb.astype(L) + zk.astype(L)) * (dd * dd).sum(1))
+    T = T.astype(np.float64)
+    ref = _ref_dense(oracle_mod, T, mmax)
+    F = gpu_ctx.boys(pairs, mmax, 6)
+    normal = np.abs(ref) >= np.finfo(np.float32).tiny
+    want = ref[normal].astype(np.float32)
+    got = F[normal].astype(np.float32)
+    ulps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    assert ulps.max() <= 1 and np.mean(ulps == 0) > 0.999, (ulps.max(), np.mean(ulps == 0))
+    assert np.all(F[~normal & (np.abs(ref) < 0.5 * np.finfo(np.float32).tiny)] == 0.0)
+    assert (T > 50).sum() > 100 and (T < 1).sum() > 100  # both branches exercised
