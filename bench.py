@@ -606,9 +606,10 @@ def run_gpu(args):
                                    "peak": peaks["fp64"], "unit": "TFLOP/s",
                                    "frac": roof64 / peaks["fp64"]}},
         "mixed_scheme": "FP32 VRR/HRR/contraction/transform for quartets with K12 K34 < "
-                        "%g; the Boys function of those quartets (its argument T, Taylor or "
-                        "asymptotic branch, e^-T, downward recursion) in FP64; all other "
-                        "quartets in FP64; J/K accumulated in FP64" % MIXED_THRESH,
+                        "%g; the Boys function of those quartets (Taylor or asymptotic "
+                        "branch, e^-T, downward recursion) in FP64 with its argument T in "
+                        "double-float arithmetic (~1e-13 relative), rounded to FP32; all "
+                        "other quartets in FP64; J/K accumulated in FP64" % MIXED_THRESH,
         "mixed_error": {"vs": "GPU FP64 pass of the same step (full pass)",
                         "dE_J": abs(emx[0] - e64[0]), "dE_K": abs(emx[1] - e64[1]),
                         "max_abs_dJ": float(np.max(np.abs(Jmx - J64))),

@@ -104,7 +104,7 @@ lgx_status lgx_set_operator(lgx_context* ctx, int op, double omega);
  * variant 0 the program kernels' FP64 evaluator (mmax <= 16), 1 the
  * register kernels' FP64 evaluator (mmax <= 6), 2 and 3 their FP32
  * counterparts, 4 and 5 the LGX_MIXED scheme's FP64 evaluators of the
- * program and register kernels (5-term series, T as a double-float pair,
+ * program and register kernels (4-term series, T as a double-float pair,
  * each value rounded to FP32; mmax <= 16 and <= 6), 6 the register
  * kernels' whole LGX_MIXED path from primitive-pair data: T then holds 8
  * values per argument (Pb.x, Pb.y, Pb.z, zeta, Pk.x, Pk.y, Pk.z, eta;

@@ -290,7 +290,7 @@ int fp32_kernel_mode(const lgx_context* ctx, int mode, int base_mode) {
 }
 
 // ------------------------------------------------------- host constants
-// Boys table: F_m(k/32), m < kBoysCols, from the Maclaurin series (top m)
+// Boys table: F_m(k/64), m < kBoysCols, from the Maclaurin series (top m)
 // and downward recursion in long double.
 std::vector<double> make_boys_table() {
   std::vector<double> t(size_t(kBoysRows) * kBoysCols);

@@ -7,11 +7,11 @@
 namespace lgx {
 
 // Boys F_0..F_MMAX(T) times the primitive prefactor pfac.
-//  T <= kBoysTmax: 7-term Taylor expansion about the nearest grid point
-//   T_k = k/32 of the pre-divided table; every m directly when MMAX <= 2,
-//   else the top m plus the downward recursion, with e^{-T} formed as the
-//   tabulated e^{-T_k} (slot 7 of the m = 0 row) times the 7-term Maclaurin
-//   series of e^{T_k - T} (|T_k - T| <= 1/64: relative error < 5e-17).
+//  T <= kBoysTmax: Taylor expansion about the nearest grid point T_k = k/64
+//   of the pre-divided table; every m directly when MMAX <= 2, else the top
+//   m plus the downward recursion, with e^{-T} formed as the tabulated
+//   e^{-T_k} (slot 7 of the m = 0 row) times the Maclaurin series of
+//   e^{T_k - T} (|T_k - T| <= 1/128).
 //  T > kBoysTmax (= 50): F_0 = sqrt(pi/T)/2 and the upward recursion
 //   F_{m+1} = (2m+1)/(2T) F_m with the e^{-T} terms dropped; the relative
 //   error of that, the regularised upper incomplete gamma Q(m+1/2, T), is
@@ -20,16 +20,25 @@ namespace lgx {
 // selects the asymptotic branch; otherwise k is the grid point and md =
 // T_k - T.  PF: multiply by pfac (the mixed scheme's FP32 kernels apply
 // their prefactor in FP32, so they skip the FP64 products by 1).  NT: terms
-// of the Taylor series and of the e^{T_k - T} series (7: remainder below
-// |md|^7/7! < 5e-17 of F_m; 5: below 7.8e-12, for values that are rounded
-// to FP32 next, whose half-ulp is 6e-8).
-template <int MMAX, bool PF = true, int NT = 7>
+// of the Taylor series and of the e^{T_k - T} series (the remainder is below
+// |md|^NT/NT! of F_m: 6 terms 3.2e-16 for the FP64 kernels; 4 terms 1.6e-10
+// for values that are rounded to FP32 next, whose half-ulp is 6e-8).  R32:
+// 1/sqrt(T) of the asymptotic branch by one FP64 Newton step from the FP32
+// estimate (relative error ~1.4e-13, again for values rounded to FP32 next)
+// instead of the full-precision FP64 rsqrt.
+template <int MMAX, bool PF = true, int NT = 6, bool R32 = false>
 __device__ __forceinline__ void rk_boys_core(const double* __restrict__ tay, double T, bool asym,
                                              int k, double md, double pfac, double* F) {
   static_assert(NT >= 2 && NT <= 7, "the table holds 7 Taylor coefficients per m");
   static_assert(MMAX <= 6, "asymptotic branch without e^{-T} is exact to 2e-15 only for m <= 6");
   if (asym) {
-    const double rs = rsqrt(T);
+    double rs;
+    if constexpr (R32) {
+      const double r0 = f2d_int(rsqrtf(d2f_int(T)));  // relative error <= ~3e-7
+      rs = fma(0.5 * r0, fma(-(T * r0), r0, 1.0), r0);
+    } else {
+      rs = rsqrt(T);
+    }
     const double oo2T = 0.5 * (rs * rs);
     double f = PF ? (0.88622692545275801365 * pfac) * rs : 0.88622692545275801365 * rs;
     F[0] = f;
@@ -87,22 +96,26 @@ __device__ __forceinline__ void rk_boys(const double* __restrict__ tay, double T
 // The mixed scheme's FP64 Boys function of an FP32 quartet, given its
 // argument T = T.hi + T.lo in double-float (ds_boys_arg): the branch and the
 // grid point come from T.hi; the offset md = T_k - T = (T_k - T.hi) - T.lo,
-// where T_k - T.hi is exact in FP32 (T_k = k/32 and T.hi are within a
+// where T_k - T.hi is exact in FP32 (T_k = k/64 and T.hi are within a
 // factor 2 of each other for k >= 1, Sterbenz; 0 - T.hi for k = 0), both
 // parts converted to FP64 with integer operations and subtracted in FP64;
 // T itself in FP64 (one addition) for the asymptotic branch and the
-// recursion.  T.hi <= 50 gives k <= 1600 < kBoysRows, and near T = 50 either
+// recursion.  T.hi <= 50 gives k <= 3200 < kBoysRows, and near T = 50 either
 // branch is exact (the asymptotic one drops Q(m+1/2, T) < 2e-15).  The
-// values are rounded to FP32 next, so the series stop at 5 terms: relative
-// error below 7.8e-12 (|md| <= 1/64), four orders under the FP32 half-ulp.
+// values are rounded to FP32 next, so the series stop at 4 terms: relative
+// error below 1.6e-10 (|md| <= 1/128), 400 times under the FP32 half-ulp.
 template <int MMAX>
 __device__ __forceinline__ void rk_boys_b64(const double* __restrict__ tay, dsf T, double* F) {
   const bool asym = T.hi > float(kBoysTmax);
   const int k = asym ? 0 : __float2int_rn(T.hi * float(kBoysInvDT));
   const float mdh = __fadd_rn(__fmul_rn(float(k), float(kBoysDT)), -T.hi);
   const double md = f2d_int(mdh) - f2d_int(T.lo);
+  if (MMAX <= 2 && !asym) {  // direct Taylor series: T itself is not needed
+    rk_boys_core<MMAX, false, 4>(tay, 0.0, false, k, md, 1.0, F);
+    return;
+  }
   const double T64 = f2d_int(T.hi) + f2d_int(T.lo);
-  rk_boys_core<MMAX, false, 5>(tay, T64, asym, k, md, 1.0, F);
+  rk_boys_core<MMAX, false, 4, true>(tay, T64, asym, k, md, 1.0, F);
 }
 
 template <int MMAX>

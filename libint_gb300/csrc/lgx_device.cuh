@@ -7,8 +7,8 @@ namespace lgx {
 
 // ------------------------------------------------------------------ Boys
 // F_m(T) = int_0^1 u^{2m} exp(-T u^2) du.
-// For T <= kBoysTmax: F_mmax by a 7-term Taylor expansion about the nearest
-// grid point T_k = k/32 of a table of F_0..F_{kBoysCols-1}(T_k), then the
+// For T <= kBoysTmax: F_mmax by a Taylor expansion about the nearest grid
+// point T_k = k/64 of a table of F_0..F_{kBoysCols-1}(T_k), then the
 // stable downward recursion F_m = (2T F_{m+1} + e^{-T})/(2m+1).
 // For T > kBoysTmax: F_0 = sqrt(pi/T)/2 (erf(sqrt T) == 1 to double there)
 // and the upward recursion F_{m+1} = ((2m+1) F_m - e^{-T})/(2T), stable for
@@ -16,13 +16,13 @@ namespace lgx {
 // are below 2e-15 relative there).  This is the scheme of libint's FmEval_Taylor
 // (include/libint2/boys.h:519-879); the table is generated on the host from
 // the Maclaurin series in extended precision.
-constexpr double kBoysInvDT = 32.0;
-constexpr double kBoysDT = 1.0 / 32.0;
+constexpr double kBoysInvDT = 64.0;
+constexpr double kBoysDT = 1.0 / 64.0;
 constexpr double kBoysTmax = 50.0;
 constexpr int kBoysTerms = 7;
 constexpr int kBoysMaxM = 16;                         // largest mmax served
 constexpr int kBoysCols = kBoysMaxM + kBoysTerms;     // 23 columns
-constexpr int kBoysRows = int(kBoysTmax * 32.0) + 2;  // 1602 grid points
+constexpr int kBoysRows = int(kBoysTmax * 64.0) + 2;  // 3202 grid points
 
 // Pre-divided Taylor table: [kBoysRows][kBoysMaxM+1][8] with
 // entry i = F_{m+i}(T_k) / i! (i < 7), so that

@@ -89,11 +89,11 @@ __device__ __forceinline__ void boys_to_stage(const double* __restrict__ tab,
 // The mixed scheme's FP64 Boys function for the program kernels' FP32
 // quartets (runtime mmax <= kBoysMaxM), from the double-float argument
 // T = T.hi + T.lo (ds_boys_arg) and rounded to FP32 with integer operations,
-// times the FP32 prefactor.  T <= 50: F_mmax by the 5-term Taylor series of
+// times the FP32 prefactor.  T <= 50: F_mmax by the 4-term Taylor series of
 // the pre-divided table (the register kernels' rows) about T_k, e^{-T} as
-// e^{-T_k} (the table's spare slot) times the 5-term series of e^{T_k - T},
-// the downward recursion in FP64; relative error below 7.8e-12 before the
-// rounding (|T_k - T| <= 1/64), with md = (T_k - T.hi) - T.lo exact in FP32
+// e^{-T_k} (the table's spare slot) times the 4-term series of e^{T_k - T},
+// the downward recursion in FP64; relative error below 1.6e-10 before the
+// rounding (|T_k - T| <= 1/128), with md = (T_k - T.hi) - T.lo exact in FP32
 // for its first part (Sterbenz).  T > 50: F_0 = sqrt(pi/T)/2 and the upward
 // recursion with its e^{-T} terms (they reach ~3e-8 of F_16 at T = 50).
 __device__ __forceinline__ void boys_b64_stage(const double* __restrict__ tay,
@@ -102,7 +102,9 @@ __device__ __forceinline__ void boys_b64_stage(const double* __restrict__ tay,
   const double T64 = f2d_int(T.hi) + f2d_int(T.lo);
   if (T.hi > float(kBoysTmax)) {
     const double eT = exp(-T64);
-    const double rs = rsqrt(T64);
+    // 1/sqrt(T): one FP64 Newton step from the FP32 estimate (~1.4e-13)
+    const double r0 = f2d_int(rsqrtf(T.hi));
+    const double rs = fma(0.5 * r0, fma(-(T64 * r0), r0, 1.0), r0);
     double f = 0.88622692545275801365 * rs;
     F[0] = d2f_int(f) * pfac;
     const double oo2T = 0.5 * (rs * rs);
@@ -117,15 +119,13 @@ __device__ __forceinline__ void boys_b64_stage(const double* __restrict__ tay,
   const double md = f2d_int(mdh) - f2d_int(T.lo);
   const double* row = tay + size_t(k) * (kBoysMaxM + 1) * kBoysTaylorStride;
   const double* c = row + mmax * kBoysTaylorStride;
-  double s = __ldg(c + 4);
-  s = fma(s, md, __ldg(c + 3));
+  double s = __ldg(c + 3);
   s = fma(s, md, __ldg(c + 2));
   s = fma(s, md, __ldg(c + 1));
   s = fma(s, md, __ldg(c + 0));
   F[mmax] = d2f_int(s) * pfac;
   if (mmax > 0) {
-    double e = 1.0 / 24.0;
-    e = fma(e, md, 1.0 / 6.0);
+    double e = 1.0 / 6.0;
     e = fma(e, md, 0.5);
     e = fma(e, md, 1.0);
     e = fma(e, md, 1.0);

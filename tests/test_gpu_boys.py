@@ -3,8 +3,8 @@ FmEval_Reference<long double> values (tests/golden/boys.npz, T in [0, 1000],
 m <= 16) and, on a dense grid of T, against the oracle (itself pinned to the
 same fixture at 1e-14).
 
-Bounds: FP64 evaluators 1e-14 relative (the Taylor truncation on the 1/32
-grid is below 5e-17; the register evaluator's asymptotic branch drops
+Bounds: FP64 evaluators 1e-14 relative (the Taylor truncation on the 1/64
+grid is below 3.2e-16; the register evaluator's asymptotic branch drops
 e^{-T} above T = 50, at most 1.7e-15 relative for m <= 6).  FP32 evaluators:
 |dF_m| <= 6e-8 (1 + T) F_{m+1}(T) + 8e-7 (mmax + 2) F_m(T) + 1e-44, where
 the first term is the rounding of T to FP32 (dF_m/dT = -F_{m+1}); the second
@@ -72,8 +72,8 @@ def test_boys_rejects_bad_arguments(gpu_ctx, lgx):
 def test_mixed_scheme_boys_is_fp64_rounded_to_fp32(gpu_ctx, v64, vb, mmax):
     # the LGX_MIXED scheme's FP32 kernels take FP64 Boys values rounded to
     # nearest FP32 (integer-only conversion).  Both evaluators (program and
-    # register kernels) stop the FP64 series at 5 terms (relative error
-    # below 7.8e-12) and take T as a double-float pair, so their value may,
+    # register kernels) stop the FP64 series at 4 terms (relative error
+    # below 1.6e-10) and take T as a double-float pair, so their value may,
     # rarely, round to the neighbouring float32 of the FP64 evaluator's
     rng = np.random.default_rng(13)
     T = np.concatenate([load("boys.npz")["T"], rng.uniform(0, 60, 4000),
