@@ -459,15 +459,8 @@ __global__ void __launch_bounds__(128, (rk_min_blocks<T, LA, LB, LC, LD, MODE, A
       T* tag = nullptr;
 #define V_(i, j, k, l) v[(((i) * N1 + (j)) * N2 + (k)) * N3 + (l)]
       int slot = 0;
-      // J(a,b) += sum_cd D(c,d) v.  With one lane per quartet the lanes of a
-      // warp take consecutive kets of (mostly) one bra pair, so their J(a,b)
-      // atomics hit the same addresses: when the whole warp is here with one
-      // bra pair, the FP64 contributions are summed across it first (one
-      // atomic per element instead of 32 to one address; the test is
-      // warp-uniform: every lane gets the same match mask)
+      // J(a,b) += sum_cd D(c,d) v
       {
-        const unsigned act = __activemask();
-        const bool wsum = G == 1 && act == 0xffffffffu && __match_any_sync(act, bpair) == act;
         T Dcd[N2 * N3];
 #pragma unroll
         for (int k = 0; k < N2; ++k)
@@ -482,14 +475,7 @@ __global__ void __launch_bounds__(128, (rk_min_blocks<T, LA, LB, LC, LD, MODE, A
             for (int k = 0; k < N2; ++k)
 #pragma unroll
               for (int l = 0; l < N3; ++l) s = fma(Dcd[k * N3 + l], V_(i, j, k, l), s);
-            if (wsum) {
-              double w = rk_f64(deg * s);
-#pragma unroll
-              for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
-              if (lane == 0) atomicAdd(a.Jacc + (o0 + i) * nbf + o1 + j, w);
-            } else if ((slot & (G - 1)) == g) {
-              atomicAdd(a.Jacc + (o0 + i) * nbf + o1 + j, rk_f64(deg * s));
-            }
+            if ((slot & (G - 1)) == g) atomicAdd(a.Jacc + (o0 + i) * nbf + o1 + j, rk_f64(deg * s));
           }
       }
       // J(c,d) += sum_ab D(a,b) v
