@@ -597,9 +597,13 @@ def run_gpu(args):
                    "quartets_fp64": stmx.quartets_fp64, "quartets_fp32": stmx.quartets_fp32,
                    "integrals_per_step": stmx.integrals,
                    "prim_quartets_per_step": stmx.prim_quartets},
+        "quartets_per_s": world * float(stmx.quartets_fp64 + stmx.quartets_fp32) * args.steps
+                          / tmx,
         "fp64": {"value": v64, "unit": "ERI/s", "dtype": "f64", "steps": args.fp64_steps,
                  "warmup": args.fp64_warmup, "ms_per_step": t64 / args.fp64_steps * 1e3,
-                 "quartets": st64.quartets_fp64, "E_J": e64[0], "E_K": e64[1],
+                 "quartets": st64.quartets_fp64,
+                 "quartets_per_s": world * float(st64.quartets_fp64) * args.fp64_steps / t64,
+                 "E_J": e64[0], "E_K": e64[1],
                  "roofline": dom64_ser or dom64,
                  "roofline_concurrent": dom64,
                  "roofline_pass": {"bound": "fp64-pipe", "achieved": roof64,
