@@ -219,10 +219,10 @@ __device__ __forceinline__ bool rk_prim(const EriArgs& a, const RkQuartet<float>
 // (the kModeJKB64 / kModeStoreB64 kernels of the mixed scheme).  The
 // screening, prefactor and VRR geometry are the FP32 ones of rk_prim above;
 // the Boys argument T = rho |P - Q|^2 is formed in double-float arithmetic
-// from the bins' double-float records bds / kds (ds_boys_arg: FP32
-// operations, relative error ~1e-13), or, for explicit quartet lists, in
-// FP64 from the primitive-pair table (rho refined from its FP32 value by one
-// Newton step); F_m(T) comes from the FP64 evaluator (Taylor with the
+// from the bins' double-float records bds / kds, or for explicit quartet
+// lists (null bds / kds) from those of the primitive pairs bidx / kidx
+// (ds_boys_arg: FP32 operations, relative error ~1e-13); F_m(T) comes from
+// the FP64 evaluator (Taylor with the
 // downward recursion and e^{-T}, or the asymptotic branch, rk_boys_b64) and
 // is rounded to FP32 with integer operations before the FP32 pfac.
 template <class C>
@@ -243,21 +243,12 @@ __device__ __forceinline__ bool rk_prim_b64(const EriArgs& a, const RkQuartet<fl
   const float PQx = PA[0] - QC[0] + q.AC[0], PQy = PA[1] - QC[1] + q.AC[1],
               PQz = PA[2] - QC[2] + q.AC[2];
   const float rho = zeta * eta * oogpq;
-  dsf T;
-  if (bds) {
-    T = ds_boys_arg(__ldg(&bds->hi), __ldg(&bds->lo), __ldg(&kds->hi), __ldg(&kds->lo), rho,
-                    oogpq);
-  } else {
-    const PrimPairRec& b64 = a.pprims[bidx];
-    const PrimPairRec& k64 = a.pprims[kidx];
-    const double zb = b64.zeta, zk = k64.zeta;
-    const double r0 = f2d_int(rho);
-    const double rho64 = fma(-fma(zb + zk, r0, -(zb * zk)), f2d_int(oogpq), r0);
-    const double X = b64.P[0] - k64.P[0], Y = b64.P[1] - k64.P[1], Z = b64.P[2] - k64.P[2];
-    const double T64 = rho64 * fma(X, X, fma(Y, Y, Z * Z));
-    T.hi = d2f_int(T64);
-    T.lo = d2f_int(T64 - f2d_int(T.hi));
+  if (!bds) {  // explicit quartet lists: the primitive pairs' own records
+    bds = a.ppds + bidx;
+    kds = a.ppds + kidx;
   }
+  const dsf T =
+      ds_boys_arg(__ldg(&bds->hi), __ldg(&bds->lo), __ldg(&kds->hi), __ldg(&kds->lo), rho, oogpq);
   double F64[C::kMmax + 1];
   rk_boys_b64<C::kMmax>(a.boys_tay, T, F64);
   float F[C::kMmax + 1];
